@@ -1,0 +1,244 @@
+/*
+ * ctraj.h -- C ABI of the GB300 trajectory engine (libctraj.so).
+ *
+ * The engine propagates molecules through a z-sorted beamline the way the
+ * reference package ``trajectories`` does in pure Python:
+ *
+ *   TrajectorySimulator.run_simulation     src/trajectories/trajectory_simulator.py:34-103
+ *   Beamline.propagate_through             src/trajectories/beamline.py:20-38
+ *   Molecule.x/v/update_trajectory         src/trajectories/molecule.py:26-68
+ *   CircularAperture.propagate_through     src/trajectories/beamline_elements/apertures.py:92-115
+ *   RectangularAperture.propagate_through  src/trajectories/beamline_elements/apertures.py:165-189
+ *   FieldPlates.propagate_through          src/trajectories/beamline_elements/apertures.py:227-270
+ *   ElectrostaticLens.propagate_through    src/trajectories/beamline_elements/electrostatic_lens.py:48-118
+ *   ElectrostaticLens.lens_acceleration    src/trajectories/beamline_elements/electrostatic_lens.py:168-227
+ *   Distribution.draw (known subclasses)   src/trajectories/distributions.py:40-41,69-76,112-119,155-162
+ *   Counter.increment_counter              src/trajectories/trajectory_simulator.py:117-124
+ *
+ * The reference has no foreign-function interface of its own (it is ~2 kLoC of
+ * Python); every entry point below replaces the Python function cited beside
+ * it, and the Python package shipped with this library binds them through
+ * ctypes (INTEGRATION.md shows the binding).
+ *
+ * Conventions: every function returns an int status (CTRAJ_OK == 0, negative
+ * on error) and never throws.  ctraj_last_error() returns a message for the
+ * last failing call on the calling thread.  Host pointers are owned by the
+ * caller; device memory is owned by the context.  A context is bound to one
+ * CUDA device and one stream; calls on one context must not overlap in time.
+ */
+#ifndef CTRAJ_H_
+#define CTRAJ_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CTRAJ_ABI_VERSION 1
+
+/* ---- status codes -------------------------------------------------------- */
+enum {
+  CTRAJ_OK = 0,
+  CTRAJ_EINVAL = -1,    /* bad argument (unknown element type, n < 0, ...)              */
+  CTRAJ_ECUDA = -2,     /* CUDA runtime error                                            */
+  CTRAJ_ENOMEM = -3,    /* device allocation failed                                      */
+  CTRAJ_ERANGE = -4,    /* bounded force table looked up outside its knots; the reference
+                           raises ValueError from interp1d there (electrostatic_lens.py:217) */
+  CTRAJ_ESTEPS = -5,    /* lens step count rint(L/dz) not finite or above CTRAJ_MAX_LENS_STEPS;
+                           the reference raises OverflowError/MemoryError there (:87)     */
+  CTRAJ_EOVERFLOW = -6, /* trajectory record buffer too small                            */
+  CTRAJ_ESTATE = -7,    /* call order violated (run before set_beamline, ...)            */
+};
+
+#define CTRAJ_MAX_ELEMENTS 64
+#define CTRAJ_MAX_LABELS 64
+#define CTRAJ_MAX_TABLES 8
+#define CTRAJ_MAX_LENS_STEPS 100000000LL
+
+/* ---- beamline elements ---------------------------------------------------- */
+enum {
+  CTRAJ_CIRCULAR_APERTURE = 1,    /* apertures.py:84-122  */
+  CTRAJ_RECTANGULAR_APERTURE = 2, /* apertures.py:147-196 */
+  CTRAJ_FIELD_PLATES = 3,         /* apertures.py:213-277 */
+  CTRAJ_ELECTROSTATIC_LENS = 4,   /* electrostatic_lens.py:23-125 */
+};
+
+enum { CTRAJ_STEP_DZ = 0, CTRAJ_STEP_DT = 1 };           /* lens step mode  */
+enum { CTRAJ_RK4_REFERENCE = 0, CTRAJ_RK4_CLASSIC = 1 }; /* lens RK4 scheme */
+
+/*
+ * One beamline element, in the order the molecules meet them (sorted by z0,
+ * beamline.py:40-45).  Geometry is passed exactly as the reference computes it
+ * in __post_init__ (z1 = z0 + L, x1 = x0 - w/2, ...) so both sides compare the
+ * same doubles.
+ *
+ *   p[] per type
+ *   circular aperture : p[0] = d (diameter)
+ *   rectangular       : p[0] = x1, p[1] = x2, p[2] = y1, p[3] = y2 (w spans X, h spans Y)
+ *   field plates      : p[0] = x1, p[1] = x2
+ *   electrostatic lens: p[0] = d (bore diameter), p[1] = dz, p[2] = dt,
+ *                       p[3] = V (electrode voltage), p[4] = R (field radius),
+ *                       p[5] = mass (kg), p[6] = alpha with |E| = alpha r^n
+ *                       (c V / R^(n+1), computed by the caller so every
+ *                       backend sees the same double), p[7] = L
+ *
+ * label        counter slot credited when a molecule is lost on this element
+ *              (for the lens: the "Lens entrance" slot, electrostatic_lens.py:63)
+ * label_inside lens only: the "Inside lens" slot (electrostatic_lens.py:117)
+ * table        lens only: force table id (ctraj_set_force_table)
+ * step_mode    lens only: CTRAJ_STEP_DZ -> N = rint(L/dz), dt = dz/vz (:87-88);
+ *              CTRAJ_STEP_DT -> dz = vz*dt per molecule, then as DZ
+ * scheme       lens only: CTRAJ_RK4_REFERENCE reproduces the reference's stage-2
+ *              point x + dt*k1 (:97); CTRAJ_RK4_CLASSIC uses x + dt*k1/2
+ * field_order  lens + W(E) table only: |E| = c V r^n / R^(n+1), n = 1 (c = 2, the
+ *              reference's own field model, :200) or n = 2 (c = 3, hexapole)
+ */
+typedef struct ctraj_element {
+  int32_t type;
+  int32_t label;
+  int32_t label_inside;
+  int32_t table;
+  int32_t step_mode;
+  int32_t scheme;
+  int32_t field_order;
+  int32_t reserved;
+  double z0, z1, x0, y0;
+  double p[8];
+} ctraj_element;
+
+/* ---- lens force tables ---------------------------------------------------- */
+enum {
+  /* Stark energy W(E) as a piecewise cubic on uniform knots in |E| (V/m); the
+   * force is -dW/dE * grad|E| / m.  coef is (n_knots-1) x 4 in scipy PPoly
+   * order (t^3, t^2, t, 1) per interval, t = E - knots[i].  Lookups beyond the
+   * knots extrapolate the boundary piece, as scipy CubicSpline does.          */
+  CTRAJ_TABLE_STARK_SPLINE = 1,
+  /* Radial acceleration a(r) (m/s^2) linear between uniform knots in r (m),
+   * the reference's interp1d table (electrostatic_lens.py:194-209).  Lookups
+   * above the last knot are errors (CTRAJ_ERANGE), as interp1d raises.        */
+  CTRAJ_TABLE_RADIAL_LINEAR = 2,
+};
+
+typedef struct ctraj_force_table {
+  int32_t kind;
+  int32_t n_knots;
+  const double* knots;  /* n_knots, ascending and uniformly spaced            */
+  const double* coef;   /* STARK_SPLINE: (n_knots - 1) * 4                    */
+  const double* values; /* RADIAL_LINEAR: n_knots                             */
+} ctraj_force_table;
+
+/* ---- initial-condition distributions (distributions.py) ------------------- */
+enum {
+  CTRAJ_DIST_NONE = 0,
+  CTRAJ_DIST_GAUSSIAN_POSITION = 1, /* p = {sigmax, sigmay, z}            (:144-162) */
+  CTRAJ_DIST_DISC_POSITION = 2,     /* p = {d, z}                         (:101-119) */
+  CTRAJ_DIST_GAUSSIAN_VELOCITY = 3, /* p = {vx, sigmax, vy, sigmay, vz, sigmaz} (:55-76) */
+};
+
+typedef struct ctraj_distribution {
+  int32_t kind;
+  int32_t reserved;
+  double p[6];
+} ctraj_distribution;
+
+enum { CTRAJ_IC_DEVICE_DRAW = 0, CTRAJ_IC_HOST = 1, CTRAJ_IC_DEVICE = 2 };
+enum { CTRAJ_OUT_NONE = 0, CTRAJ_OUT_HOST = 1, CTRAJ_OUT_DEVICE = 2 };
+
+/*
+ * One propagation run of n molecules (the body of trajectory_simulator.py:52-78
+ * for all chunks at once).
+ *
+ * precision  32: FP32 state, transverse force from the table with z held
+ *            relative to element planes; 64: FP64 with the reference's own
+ *            operation order (bit-for-bit the reference on ballistic paths).
+ * ic_mode    CTRAJ_IC_DEVICE_DRAW: positions from xdist and velocities from
+ *            vdist drawn on the device with Philox-4x32-10 keyed by seed,
+ *            molecule i using counter (offset + i); CTRAJ_IC_HOST/DEVICE: ics
+ *            points to a (6, n) row-major float64 array x, y, z, vx, vy, vz
+ *            (the reference's xs / vs stacked, trajectory_simulator.py:57-58).
+ * out_*      optional per-molecule results (out_mode says host or device
+ *            pointers; NULL entries are skipped): out_label[i] counter slot,
+ *            or -1 for "Detected"; out_final (10, n) last trajectory row
+ *            x, y, z, vx, vy, vz, ax, ay, az, t; out_rows[i] = len(t) - 1 of
+ *            the reference trajectory; out_margin[i] smallest distance to an
+ *            edge seen by any hit test along the path (m).
+ * counts     host array of n_labels + 1 int64: per-label losses, then the
+ *            "Detected" count in counts[n_labels].
+ */
+typedef struct ctraj_run_args {
+  int64_t n;
+  int32_t precision;
+  int32_t ic_mode;
+  const double* ics;
+  ctraj_distribution xdist;
+  ctraj_distribution vdist;
+  uint64_t seed;
+  uint64_t offset;
+  double g;
+  int32_t out_mode;
+  int32_t reserved;
+  int32_t* out_label;
+  double* out_final;
+  int32_t* out_rows;
+  double* out_margin;
+  int64_t* counts;
+} ctraj_run_args;
+
+typedef struct ctraj_run_stats {
+  int64_t molecules;        /* molecules propagated                           */
+  int64_t molecule_steps;   /* sum over molecules of len(trajectory.t) - 1    */
+  int64_t lens_steps;       /* RK4 steps (subset of molecule_steps)           */
+  int64_t edge_band;        /* molecules whose smallest edge distance < 1 um  */
+  int64_t table_range;      /* lookups outside a table's knots                */
+  int64_t bad_steps;        /* molecules with a non-finite lens step count    */
+  int32_t kernels;          /* kernel launches issued by this run             */
+  int32_t reserved;
+} ctraj_run_stats;
+
+/* ---- context -------------------------------------------------------------- */
+typedef struct ctraj_context ctraj_context;
+
+int ctraj_version(void);
+const char* ctraj_last_error(void);
+
+int ctraj_create(int device, ctraj_context** out);
+int ctraj_destroy(ctraj_context* ctx);
+/* Launch on an existing cudaStream_t (e.g. torch.cuda.current_stream()). NULL
+ * restores the context's own stream. */
+int ctraj_set_stream(ctraj_context* ctx, void* cuda_stream);
+int ctraj_synchronize(ctraj_context* ctx);
+
+/* Beamline.__post_init__ / sort_elements (beamline.py:17-18,40-45): elements
+ * must already be sorted by z0; n_labels counter slots. */
+int ctraj_set_beamline(ctraj_context* ctx, const ctraj_element* elements,
+                       int32_t n_elements, int32_t n_labels);
+
+/* ElectrostaticLens.a_interp / lens_acceleration table (electrostatic_lens.py:174-213). */
+int ctraj_set_force_table(ctraj_context* ctx, int32_t table_id,
+                          const ctraj_force_table* table);
+
+/* TrajectorySimulator.run_simulation body (trajectory_simulator.py:52-97):
+ * propagate, tally into counts, report stats.  Blocks until the counts are on
+ * the host. */
+int ctraj_run(ctraj_context* ctx, const ctraj_run_args* args,
+              ctraj_run_stats* stats);
+
+/*
+ * Trajectory recording (trajectory_simulator.py:75-76 keeps full Trajectory
+ * objects, molecule.py:111-167).  Re-propagates the molecules whose indices
+ * are in ids (same ICs as the run that produced them: same seed/offset or the
+ * same ics array) and writes every `stride`-th trajectory row plus the last
+ * one into rows: (n_ids, max_rows, 10) float64 x, y, z, vx, vy, vz, ax, ay,
+ * az, t, on the host.  row_count[k] receives the rows written for ids[k];
+ * CTRAJ_EOVERFLOW when a molecule needs more than max_rows.
+ */
+int ctraj_record(ctraj_context* ctx, const ctraj_run_args* args,
+                 const int64_t* ids, int64_t n_ids, int32_t stride,
+                 int32_t max_rows, double* rows, int32_t* row_count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CTRAJ_H_ */

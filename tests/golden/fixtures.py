@@ -1,0 +1,58 @@
+"""Load the golden fixtures written by make_golden.py and rebuild their
+beamlines from this package's classes (no reference import needed)."""
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+CASES = ["config0", "config1", "example_lens", "kat_circle", "kat_rect", "kat_plates", "kat_lens"]
+
+
+def available():
+    return [c for c in CASES if (HERE / f"{c}.npz").exists()]
+
+
+def load(name):
+    z = np.load(HERE / f"{name}.npz", allow_pickle=False)
+    return {k: z[k] for k in z.files}
+
+
+def build_beamline(fx, V=None):
+    """Beamline of this package's element classes from a fixture's spec."""
+    import ctraj
+    from scipy.interpolate import interp1d
+
+    spec = json.loads(str(fx["spec"]))
+    elems = []
+    for s in spec["elements"]:
+        kw = {k: v for k, v in s.items() if k not in ("cls", "force")}
+        if s["cls"] == "ElectrostaticLens":
+            f = s["force"]
+            knots = fx[f"table_{f['table']}_knots"]
+            if f"table_{f['table']}_coef" in fx:
+                kw["a_interp"] = ctraj.StarkForce(knots, fx[f"table_{f['table']}_coef"], V=f["V"],
+                                                  R=f["R"], mass=f["mass"], field_order=f["order"])
+            else:
+                kw["a_interp"] = interp1d(knots, fx[f"table_{f['table']}_values"])
+        elems.append(getattr(ctraj, s["cls"])(**kw))
+    return ctraj.Beamline(elems)
+
+
+def expected_labels(fx):
+    names = [str(s) for s in fx["label_names"]]
+    return [names[i] for i in fx["label"]]
+
+
+def traces(fx):
+    """{molecule index: (rows, row_index or None, full length)}"""
+    out = {}
+    for k in fx:
+        if k.startswith("trace_") and k.count("_") == 1:
+            j = int(k.split("_")[1])
+            idx = fx.get(f"trace_{j}_idx")
+            n = int(fx[f"trace_{j}_len"]) if f"trace_{j}_len" in fx else fx[k].shape[0]
+            out[j] = (fx[k], idx, n)
+    return out
