@@ -82,7 +82,7 @@ def test_planted_error_is_detected():
     """A mistake planted in the oracle's inputs (a shifted aperture) must break parity."""
     fx = fixtures.load("config0")
     bl = fixtures.build_beamline(fx)
-    bl.elements[0].d *= 1.001
+    bl.elements[0].d *= 1.05
     cb = compile_beamline(bl)
     r = oracle.run(cb, fx["ics"])
     got = [cb.label_of(s) for s in r["label"]]
