@@ -1,0 +1,317 @@
+#!/usr/bin/env python
+"""Benchmark of the trajectory hot path on GB300.
+
+Workload: the electrostatic-lens beamline (aperture r = 6 mm at 0.30 m,
+hexapole lens 0.80-1.40 m with a 4096-knot Stark spline and RK4 at dt = 1 us,
+detection plane at 3 m), 1e7 molecules per GPU, FP32, initial conditions drawn
+on the device from x, y ~ N(0, 1.5 mm), vx, vy ~ N(0, 20 m/s), vz ~ N(184, 16).
+One step = one full propagation of all molecules (ctraj_run).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Metric: molecule-steps/s = sum over molecules of len(trajectory.t) - 1 (the
+reference's trajectory rows after the initial one), counted on the device.
+
+`value` times ctraj_run with CUDA events on its stream (L2 flushed between
+steps).  `e2e` times the public drop-in TrajectorySimulator.run_simulation
+(host Beamline / Distribution objects in, Counter out) with perf_counter.
+`cpu_baseline` and --impl reference time the FP64 C restatement of the
+reference (oracle/) on the host cores on a bounded sample of the same workload.
+For N > 1 (torchrun) every rank propagates its own 1e7 molecules on disjoint
+Philox counters (replicas, weak scaling); time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "centrex-molecule-trajectories_gb300"))
+sys.path.insert(0, str(ROOT))
+
+METRIC = "molecule-steps/s (1e7 lens beamline)"
+UNIT = "molecule-steps/s"
+# Algorithmic FP32 work per molecule-step, FMA counted as 2 (the lens RK4 step:
+# four table-driven force evaluations, stage points, RK4 combination, bore test).
+FLOP_PER_RK4_STEP = 114
+FLOP_PER_BALLISTIC_STEP = 12
+WORKLOAD = ("lens beamline: aperture r=6mm@0.30m, hexapole lens z0=0.80m L=0.60m R=17.5mm V=30kV "
+            "(4096-knot Stark spline, a=h*6.7GHz, d=4.2D), RK4 dt=1us, detection@3.0m; "
+            "x,y~N(0,1.5mm) vx,vy~N(0,20m/s) vz~N(184,16m/s)")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--molecules", type=float, default=1e7)
+    p.add_argument("--cpu-sample", type=float, default=2e6, help="molecules per CPU sample")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(n: int, threads: int, seed: int):
+    """The oracle (FP64 C restatement of the reference) on n molecules: host draw + propagation."""
+    import ctraj
+    from ctraj.compiler import compile_beamline
+    from ctraj.distributions import host_draw
+    from ctraj.workloads import lens_beamline, source
+    from oracle import oracle
+
+    cb = compile_beamline(lens_beamline())
+    xd, vd = source()
+    t0 = time.perf_counter()
+    ics = host_draw(xd, vd, n, seed=seed)
+    r = oracle.run(cb, ics, threads=threads, outputs=False)
+    dt = time.perf_counter() - t0
+    return r["steps"], dt
+
+
+def cpu_baseline(n: int, reps: int = 1):
+    threads = os.cpu_count() or 1
+    steps = secs = 0
+    for k in range(reps):
+        s, dt = cpu_sample(n, threads, seed=100 + k)
+        steps += s
+        secs += dt
+    return {"value": steps / secs, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} molecules of the same workload per repetition x {reps}, ICs drawn on the "
+                      f"host (numpy), FP64 oracle/ctraj_oracle.c on {threads} threads"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    n = int(args.cpu_sample)
+    threads = os.cpu_count() or 1
+    for k in range(args.warmup):
+        cpu_sample(max(n // 10, 1000), threads, seed=k)
+    steps = secs = 0
+    for k in range(args.steps):
+        s, dt = cpu_sample(n, threads, seed=1000 + k)
+        steps += s
+        secs += dt
+    v = steps / secs
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy draws)",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "molecules_per_step": n},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{n} molecules per step; the reference is pure Python and cannot "
+                                       f"run on the GPU machine, so its FP64 C restatement (oracle/) is timed"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.2)
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.seek(0)
+        rows = [r.split(",") for r in self.file.read().strip().splitlines() if r.count(",") >= 8]
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows]
+        mx = max(float(r[2]) for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].strip() == "Active"})
+        busy = [s for s in sm if s > 0.5 * mx] or sm
+        return {"sm_mhz": statistics.median(busy), "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows)}
+
+
+def fp32_peak(device: int):
+    from ctraj.build import PEAK_OUT
+
+    lib = ctypes.CDLL(str(PEAK_OUT))
+    lib.ctraj_peak_fp32.restype = ctypes.c_int
+    lib.ctraj_peak_fp32.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                    ctypes.POINTER(ctypes.c_double)]
+    best = 0.0
+    for _ in range(3):
+        tf, ms = ctypes.c_double(), ctypes.c_double()
+        if lib.ctraj_peak_fp32(device, 20000, ctypes.byref(tf), ctypes.byref(ms)) == 0:
+            best = max(best, tf.value)
+    return best
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    from __graft_entry__ import build
+    from ctraj.compiler import compile_beamline
+    from ctraj.distributions import device_spec
+    from ctraj.engine import Engine
+    from ctraj.trajectory_simulator import TrajectorySimulator
+    from ctraj.workloads import lens_beamline, source
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    if rank == 0:
+        build()
+    if world > 1:
+        dist.barrier()
+
+    n = int(args.molecules)
+    bl = lens_beamline()
+    cb = compile_beamline(bl)
+    xdist, vdist = source()
+    xs, vs = device_spec(xdist, "position"), device_spec(vdist, "velocity")
+    eng = Engine(local)
+    stream = torch.cuda.current_stream()
+    eng.set_stream(stream.cuda_stream)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB of L2
+
+    def step(seed):
+        return eng.run(cb, n, precision=32, xdist=xs, vdist=vs, seed=seed, offset=rank * n, timing=True)
+
+    for k in range(args.warmup):
+        step(seed=k)
+    peak = fp32_peak(local)
+
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    times, results = [], []
+    with Clocks(local) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            ev0.record(stream)
+            r = step(seed=1000 + k)
+            ev1.record(stream)
+            ev1.synchronize()
+            times.append(ev0.elapsed_time(ev1))
+            results.append(r)
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = clk.summary()
+    total_ms = sum(times)
+    steps = sum(r.molecule_steps for r in results)
+    lens_steps = sum(r.lens_steps for r in results)
+    lens_ms = sum(r.extra["lens_ms"] for r in results)
+    front_ms = sum(r.extra["front_ms"] for r in results)
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        s = torch.tensor([steps], dtype=torch.float64, device="cuda")
+        dist.all_reduce(s, op=dist.ReduceOp.SUM)
+        total_ms, steps_all = float(t.item()), float(s.item())
+    else:
+        steps_all = float(steps)
+    value = steps_all / (total_ms / 1e3)
+
+    # end to end through the public drop-in API
+    e2e = None
+    if not args.no_e2e:
+        sim = TrajectorySimulator(device=local)
+        for k in range(max(1, args.warmup)):
+            sim.run_simulation(bl, "warm", vdist=vdist, xdist=xdist, N_traj=n, seed=k)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_steps = 0
+        for k in range(args.steps):
+            sim.run_simulation(bl, f"run{k}", vdist=vdist, xdist=xdist, N_traj=n, seed=2000 + k)
+            e2e_steps += sim.last_run.molecule_steps
+        e2e_s = time.perf_counter() - t0
+        tab = cb.tables[0]
+        h2d = (tab.knots.nbytes + tab.coef.nbytes + (tab.knots.size - 1) * 16
+               + ctypes.sizeof(cb.elements))
+        d2h = 8 * (len(cb.labels) + 1) + 64
+        if world > 1:
+            t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+            s = torch.tensor([e2e_steps], dtype=torch.float64, device="cuda")
+            dist.all_reduce(s, op=dist.ReduceOp.SUM)
+            e2e_steps = float(s.item())
+        e2e = {"value": e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h),
+               "api": "ctraj.TrajectorySimulator.run_simulation(beamline, run_name, vdist, xdist, N_traj=1e7)",
+               "ms_per_step": e2e_s / args.steps * 1e3}
+
+    if rank != 0:
+        return
+    achieved = lens_steps * FLOP_PER_RK4_STEP / (lens_ms / 1e3) / 1e12
+    roofline = {"bound": "fp32", "kernel": "k_lens (RK4 through the hexapole lens)",
+                "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+                "peak_source": "measured in this run: FMA-chain kernel (csrc/peak/fp32_peak.cu), "
+                               "MEASURED_PEAKS.json has no FP32 CUDA-core figure",
+                "flop_per_step": FLOP_PER_RK4_STEP, "lens_steps_per_launch": lens_steps / args.steps,
+                "lens_ms_per_launch": lens_ms / args.steps, "front_ms_per_launch": front_ms / args.steps,
+                "traffic": None}
+    cpu = None if args.no_cpu or world > 1 else cpu_baseline(int(args.cpu_sample))
+    r0 = results[-1]
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic: Philox-4x32-10 initial conditions drawn on the device",
+            "config": {"workload": WORKLOAD, "molecules_per_gpu": n, "precision": "fp32",
+                       "l2": "flushed between steps (256 MiB write outside the timed events)",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+            "gpu_launches": int(sum(r.kernels for r in results)),
+            "molecule_steps_per_step": steps / args.steps, "counts_last_step": r0.counter_dict()}
+    print(json.dumps(line), flush=True)
+    eng.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

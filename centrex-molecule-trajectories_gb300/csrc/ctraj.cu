@@ -1,0 +1,639 @@
+// libctraj.so: C ABI of the GB300 trajectory engine (declared in include/ctraj.h).
+//
+// A context owns one CUDA stream (or borrows the caller's), the device copies
+// of the beamline's force tables, the FP32 lens tables derived from them, and
+// grow-only work buffers (survivor queues, injected initial conditions,
+// per-molecule outputs).  ctraj_run enqueues k_front and one k_lens per lens
+// and copies the per-label counts back; nothing is allocated on a repeated
+// run of the same or a smaller size.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "ctraj.h"
+#include "kernels.cuh"
+
+namespace ctraj {
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_error = buf;
+  return code;
+}
+
+#define CT_CUDA(call)                                                                   \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) return fail(CTRAJ_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t want) {
+    if (want <= bytes) return CTRAJ_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return fail(CTRAJ_ENOMEM, "cudaMalloc(%zu): %s", want, cudaGetErrorString(e));
+    }
+    bytes = want;
+    return CTRAJ_OK;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <class T>
+  T* as(size_t offset_bytes = 0) const {
+    return reinterpret_cast<T*>(static_cast<char*>(p) + offset_bytes);
+  }
+};
+
+struct HostTable {
+  int kind = 0;
+  int n = 0;
+  std::vector<double> knots, coef, values;
+  DevBuf dev;  // knots | coef | values
+  bool uploaded = false;
+};
+
+}  // namespace
+}  // namespace ctraj
+
+using namespace ctraj;
+
+struct ctraj_context {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::vector<ctraj_element> elements;
+  int n_labels = 0;
+  bool have_beamline = false;
+  HostTable tables[CTRAJ_MAX_TABLES];
+  DevBuf lens_tables;           // FP32 lens tables, one region per lens element
+  bool lens_tables_dirty = true;
+  std::vector<size_t> lens_offset;
+  std::vector<int> lens_n_int, lens_n_smem;
+  DevBuf queue[2];
+  DevBuf qctl;                  // queue counters (4 x unsigned) + counts + stats
+  DevBuf ics;
+  DevBuf outs;
+  DevBuf rec_rows, rec_ids, rec_count;
+  int refill = 16;
+  bool timing = false;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // before front, after front, after lenses
+};
+
+namespace ctraj {
+namespace {
+
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// Queue layout inside one buffer of capacity cap.
+Queue make_queue(const DevBuf& b, size_t cap, int precision, unsigned* ctl) {
+  Queue q{};
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off += align256(bytes);
+    return o;
+  };
+  if (precision == 32) {
+    q.x = b.as<float>(take(cap * 4));
+    q.y = b.as<float>(take(cap * 4));
+    q.vx = b.as<float>(take(cap * 4));
+    q.vy = b.as<float>(take(cap * 4));
+    q.vz = b.as<float>(take(cap * 4));
+    q.t = b.as<float>(take(cap * 4));
+  } else {
+    q.dx = b.as<double>(take(cap * 8));
+    q.dy = b.as<double>(take(cap * 8));
+    q.dz = b.as<double>(take(cap * 8));
+    q.dvx = b.as<double>(take(cap * 8));
+    q.dvy = b.as<double>(take(cap * 8));
+    q.dvz = b.as<double>(take(cap * 8));
+    q.dt = b.as<double>(take(cap * 8));
+  }
+  q.margin = b.as<double>(take(cap * 8));
+  q.rows = b.as<int32_t>(take(cap * 4));
+  q.id = b.as<int32_t>(take(cap * 4));
+  q.count = ctl;
+  q.head = ctl + 1;
+  return q;
+}
+
+size_t queue_bytes(size_t cap, int precision) {
+  size_t per = precision == 32 ? 6 * align256(cap * 4) : 7 * align256(cap * 8);
+  return per + align256(cap * 8) + 2 * align256(cap * 4);
+}
+
+int lens_force_kind(const ctraj_context* c, const ctraj_element& e) {
+  const HostTable& t = c->tables[e.table];
+  if (t.kind == CTRAJ_TABLE_RADIAL_LINEAR) return kForceRadial;
+  return e.field_order == 1 ? kForceStark1 : kForceStark2;
+}
+
+// FP32 lens tables: coefficients of the per-interval polynomial in the local
+// coordinate u (0..1), pre-multiplied by the lens's force prefactor.
+int build_lens_tables(ctraj_context* c) {
+  const int n_el = int(c->elements.size());
+  c->lens_offset.assign(n_el, 0);
+  c->lens_n_int.assign(n_el, 0);
+  c->lens_n_smem.assign(n_el, 0);
+  std::vector<float4> host;
+  for (int i = 0; i < n_el; ++i) {
+    const ctraj_element& e = c->elements[i];
+    if (e.type != CTRAJ_ELECTROSTATIC_LENS) continue;
+    const HostTable& t = c->tables[e.table];
+    const double x0 = t.knots[0], h = (t.knots[t.n - 1] - t.knots[0]) / double(t.n - 1);
+    const int n_int = t.n - 1;
+    c->lens_offset[i] = host.size();
+    c->lens_n_int[i] = n_int;
+    const double bore = e.p[0] * 0.5;
+    int n_cover;
+    if (t.kind == CTRAJ_TABLE_RADIAL_LINEAR) {
+      for (int j = 0; j < n_int; ++j)
+        host.push_back(make_float4(float(t.values[j]), float(t.values[j + 1] - t.values[j]), 0.f, 0.f));
+      n_cover = n_int;
+    } else {
+      const double alpha = e.p[6], mass = e.p[5];
+      const double kappa = e.field_order == 1 ? alpha / mass : 2.0 * alpha / mass;
+      for (int j = 0; j < n_int; ++j) {
+        const double* cj = &t.coef[size_t(j) * 4];
+        host.push_back(make_float4(float(-kappa * cj[2]), float(-kappa * 2.0 * cj[1] * h),
+                                   float(-kappa * 3.0 * cj[0] * h * h), 0.f));
+      }
+      const double rcap = 1.1 * bore;
+      const double ecap = e.field_order == 1 ? alpha * rcap : alpha * rcap * rcap;
+      n_cover = int(std::min<double>(n_int, std::ceil((ecap - x0) / h) + 2.0));
+    }
+    // at most 96 KiB of shared memory per CTA for the staged part
+    c->lens_n_smem[i] = std::max(0, std::min(n_cover, 6144));
+  }
+  if (!host.empty()) {
+    int st = c->lens_tables.ensure(host.size() * sizeof(float4));
+    if (st) return st;
+    CT_CUDA(cudaMemcpyAsync(c->lens_tables.p, host.data(), host.size() * sizeof(float4),
+                            cudaMemcpyHostToDevice, c->stream));
+  }
+  c->lens_tables_dirty = false;
+  return CTRAJ_OK;
+}
+
+int build_plan(ctraj_context* c, const ctraj_run_args* a, Plan& P) {
+  std::memset(&P, 0, sizeof P);
+  const int n_el = int(c->elements.size());
+  P.n_el = n_el;
+  P.n_labels = c->n_labels;
+  P.first_lens = n_el;
+  P.g = a->g;
+  P.gf = float(a->g);
+  for (int i = 0; i < n_el; ++i) {
+    const ctraj_element& e = c->elements[i];
+    P.el[i] = e;
+    ElemF& f = P.ef[i];
+    f.gap = i > 0 ? float(e.z0 - c->elements[i - 1].z1) : 0.f;
+    f.len = float(e.z1 - e.z0);
+    switch (e.type) {
+      case CTRAJ_CIRCULAR_APERTURE:
+      case CTRAJ_ELECTROSTATIC_LENS: {
+        const double h = e.p[0] * 0.5;
+        f.c[0] = float(h * h);
+        f.c[1] = float(h);
+        break;
+      }
+      case CTRAJ_RECTANGULAR_APERTURE:
+        for (int k = 0; k < 4; ++k) f.c[k] = float(e.p[k]);
+        break;
+      case CTRAJ_FIELD_PLATES:
+        f.c[0] = float(e.p[0]);
+        f.c[1] = float(e.p[1]);
+        break;
+    }
+    if (e.type == CTRAJ_ELECTROSTATIC_LENS) {
+      if (P.first_lens == n_el) P.first_lens = i;
+      const HostTable& t = c->tables[e.table];
+      LensF& L = P.lf[i];
+      const double x0 = t.knots[0], h = (t.knots[t.n - 1] - t.knots[0]) / double(t.n - 1);
+      L.q = c->lens_tables.as<float4>(c->lens_offset[i] * sizeof(float4));
+      L.n_int = c->lens_n_int[i];
+      L.n_smem = c->lens_n_smem[i];
+      L.force = lens_force_kind(c, e);
+      if (t.kind == CTRAJ_TABLE_RADIAL_LINEAR) {
+        L.beta = float(1.0 / h);
+        L.s0 = float(x0 / h);
+        L.r_max = float(t.knots[t.n - 1]);
+      } else {
+        L.beta = float(e.p[6] / h);
+        L.s0 = float(x0 / h);
+        L.r_max = INFINITY;
+      }
+    }
+  }
+  for (int k = 0; k < CTRAJ_MAX_TABLES; ++k) {
+    const HostTable& t = c->tables[k];
+    if (!t.n) continue;
+    TableD& d = P.td[k];
+    d.kind = t.kind;
+    d.n = t.n;
+    d.x0 = t.knots[0];
+    d.h = (t.knots[t.n - 1] - t.knots[0]) / double(t.n - 1);
+    d.knots = t.dev.as<double>(0);
+    d.coef = t.coef.empty() ? nullptr : t.dev.as<double>(align256(t.n * 8));
+    d.values = t.values.empty() ? nullptr : t.dev.as<double>(align256(t.n * 8));
+  }
+  return CTRAJ_OK;
+}
+
+int check_beamline(const ctraj_context* c) {
+  for (size_t i = 0; i < c->elements.size(); ++i) {
+    const ctraj_element& e = c->elements[i];
+    if (e.type == CTRAJ_ELECTROSTATIC_LENS) {
+      if (e.table < 0 || e.table >= CTRAJ_MAX_TABLES || !c->tables[e.table].n)
+        return fail(CTRAJ_ESTATE, "lens element %zu uses force table %d, which is not set", i, e.table);
+      const HostTable& t = c->tables[e.table];
+      if (t.kind == CTRAJ_TABLE_STARK_SPLINE && e.field_order != 1 && e.field_order != 2)
+        return fail(CTRAJ_EINVAL, "lens element %zu: field_order must be 1 or 2", i);
+    }
+  }
+  return CTRAJ_OK;
+}
+
+template <class KernelT>
+int blocks_per_sm(KernelT k, int threads, size_t smem) {
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, threads, smem) != cudaSuccess || b < 1) b = 1;
+  return b;
+}
+
+// The lens kernel for lens element i: FP32 is specialised on the force law,
+// FP64 evaluates the reference's force code for every table kind.
+template <bool k64, bool kOut>
+using LensKernel = void (*)(const Plan, const RunDev, const int, const Queue, const Queue, const int);
+
+template <bool k64, bool kOut>
+LensKernel<k64, kOut> lens_kernel(int force) {
+  if (k64) return k_lens<Mol64<false>, kOut, 0, true>;
+  switch (force) {
+    case kForceStark2: return k_lens<Mol32<kOut, false>, kOut, kForceStark2, false>;
+    case kForceStark1: return k_lens<Mol32<kOut, false>, kOut, kForceStark1, false>;
+    default: return k_lens<Mol32<kOut, false>, kOut, kForceRadial, false>;
+  }
+}
+
+template <bool k64, bool kOut>
+int launch_all(ctraj_context* c, const Plan& P, const RunDev& R, Queue* q, int* launches) {
+  using MolT = typename std::conditional<k64, Mol64<false>, Mol32<kOut, false>>::type;
+  const int64_t n = R.n;
+  cudaStream_t s = c->stream;
+  if (c->timing) CT_CUDA(cudaEventRecord(c->ev[0], s));
+  if (n > 0) {
+    auto kf = k_front<MolT, kOut>;
+    int bps = blocks_per_sm(kf, kThreads, 0);
+    int64_t want = (n + kThreads - 1) / kThreads;
+    int grid = int(std::min<int64_t>(want, int64_t(bps) * c->sm_count * 4));
+    kf<<<grid, kThreads, 0, s>>>(P, R, q[0]);
+    CT_CUDA(cudaGetLastError());
+    ++*launches;
+  }
+  if (c->timing) CT_CUDA(cudaEventRecord(c->ev[1], s));
+  int cur = 0;
+  for (int i = 0; i < P.n_el; ++i) {
+    if (P.el[i].type != CTRAJ_ELECTROSTATIC_LENS) continue;
+    const int nxt = cur ^ 1;
+    CT_CUDA(cudaMemsetAsync(q[nxt].count, 0, 2 * sizeof(unsigned), s));
+    const size_t smem = k64 ? 0 : size_t(P.lf[i].n_smem) * sizeof(float4);
+    LensKernel<k64, kOut> kl = lens_kernel<k64, kOut>(P.lf[i].force);
+    CT_CUDA(cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    const int grid = blocks_per_sm(kl, kThreads, smem) * c->sm_count;
+    if (n > 0) {
+      kl<<<grid, kThreads, smem, s>>>(P, R, i, q[cur], q[nxt], c->refill);
+      CT_CUDA(cudaGetLastError());
+      ++*launches;
+    }
+    cur = nxt;
+  }
+  if (c->timing) CT_CUDA(cudaEventRecord(c->ev[2], s));
+  return CTRAJ_OK;
+}
+
+int validate_run(const ctraj_context* c, const ctraj_run_args* a) {
+  if (!a) return fail(CTRAJ_EINVAL, "args is NULL");
+  if (!c->have_beamline) return fail(CTRAJ_ESTATE, "ctraj_set_beamline was not called");
+  if (a->n < 0 || a->n > int64_t(0x7fffffff)) return fail(CTRAJ_EINVAL, "n = %lld out of range [0, 2^31)", (long long)a->n);
+  if (a->precision != 32 && a->precision != 64) return fail(CTRAJ_EINVAL, "precision must be 32 or 64");
+  if (a->ic_mode == CTRAJ_IC_DEVICE_DRAW) {
+    if (a->xdist.kind != CTRAJ_DIST_GAUSSIAN_POSITION && a->xdist.kind != CTRAJ_DIST_DISC_POSITION)
+      return fail(CTRAJ_EINVAL, "unknown position distribution kind %d", a->xdist.kind);
+    if (a->vdist.kind != CTRAJ_DIST_GAUSSIAN_VELOCITY)
+      return fail(CTRAJ_EINVAL, "unknown velocity distribution kind %d", a->vdist.kind);
+  } else if (a->ic_mode == CTRAJ_IC_HOST || a->ic_mode == CTRAJ_IC_DEVICE) {
+    if (!a->ics && a->n > 0) return fail(CTRAJ_EINVAL, "ics is NULL");
+  } else {
+    return fail(CTRAJ_EINVAL, "unknown ic_mode %d", a->ic_mode);
+  }
+  if (a->out_mode < CTRAJ_OUT_NONE || a->out_mode > CTRAJ_OUT_DEVICE) return fail(CTRAJ_EINVAL, "bad out_mode");
+  if (!a->counts) return fail(CTRAJ_EINVAL, "counts is NULL");
+  return check_beamline(c);
+}
+
+// Shared by ctraj_run and ctraj_record: plan, ICs on the device, RunDev.
+int prepare(ctraj_context* c, const ctraj_run_args* a, Plan& P, RunDev& R) {
+  CT_CUDA(cudaSetDevice(c->device));
+  int st;
+  for (int k = 0; k < CTRAJ_MAX_TABLES; ++k) {
+    HostTable& t = c->tables[k];
+    if (t.n && !t.uploaded) {
+      const size_t nb = align256(t.n * 8);
+      const size_t cb = t.coef.empty() ? 0 : t.coef.size() * 8;
+      const size_t vb = t.values.empty() ? 0 : t.values.size() * 8;
+      if ((st = t.dev.ensure(nb + std::max(cb, vb)))) return st;
+      CT_CUDA(cudaMemcpyAsync(t.dev.p, t.knots.data(), t.n * 8, cudaMemcpyHostToDevice, c->stream));
+      if (cb) CT_CUDA(cudaMemcpyAsync(t.dev.as<char>(nb), t.coef.data(), cb, cudaMemcpyHostToDevice, c->stream));
+      if (vb) CT_CUDA(cudaMemcpyAsync(t.dev.as<char>(nb), t.values.data(), vb, cudaMemcpyHostToDevice, c->stream));
+      t.uploaded = true;
+    }
+  }
+  if (c->lens_tables_dirty && (st = build_lens_tables(c))) return st;
+  if ((st = build_plan(c, a, P))) return st;
+  std::memset(&R, 0, sizeof R);
+  R.n = a->n;
+  R.seed = a->seed;
+  R.offset = a->offset;
+  R.ic_mode = a->ic_mode;
+  R.xd = a->xdist;
+  R.vd = a->vdist;
+  if (a->ic_mode == CTRAJ_IC_DEVICE_DRAW) {
+    const double zd = a->xdist.kind == CTRAJ_DIST_DISC_POSITION ? a->xdist.p[1] : a->xdist.p[2];
+    R.gap0f = P.n_el > 0 ? float(P.el[0].z0 - zd) : 0.f;
+  } else if (a->ic_mode == CTRAJ_IC_HOST && a->n > 0) {
+    const size_t b = size_t(a->n) * 6 * 8;
+    if ((st = c->ics.ensure(b))) return st;
+    CT_CUDA(cudaMemcpyAsync(c->ics.p, a->ics, b, cudaMemcpyHostToDevice, c->stream));
+    R.ics = c->ics.as<double>();
+  } else {
+    R.ics = a->ics;
+  }
+  return CTRAJ_OK;
+}
+
+}  // namespace
+}  // namespace ctraj
+
+// ============================================================================
+// C ABI
+// ============================================================================
+extern "C" {
+
+int ctraj_version(void) { return CTRAJ_ABI_VERSION; }
+
+const char* ctraj_last_error(void) { return g_error.c_str(); }
+
+int ctraj_create(int device, ctraj_context** out) {
+  if (!out) return fail(CTRAJ_EINVAL, "out is NULL");
+  *out = nullptr;
+  int n_dev = 0;
+  CT_CUDA(cudaGetDeviceCount(&n_dev));
+  if (device < 0 || device >= n_dev) return fail(CTRAJ_EINVAL, "device %d not present (%d devices)", device, n_dev);
+  CT_CUDA(cudaSetDevice(device));
+  auto* c = new ctraj_context();
+  c->device = device;
+  cudaError_t e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+  for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
+  if (e != cudaSuccess) {
+    delete c;
+    return fail(CTRAJ_ECUDA, "context setup: %s", cudaGetErrorString(e));
+  }
+  c->stream = c->own_stream;
+  int st = c->qctl.ensure(4096);
+  if (st) {
+    cudaStreamDestroy(c->own_stream);
+    delete c;
+    return st;
+  }
+  *out = c;
+  return CTRAJ_OK;
+}
+
+int ctraj_destroy(ctraj_context* c) {
+  if (!c) return CTRAJ_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto& t : c->tables) t.dev.release();
+  c->lens_tables.release();
+  c->queue[0].release();
+  c->queue[1].release();
+  c->qctl.release();
+  c->ics.release();
+  c->outs.release();
+  c->rec_rows.release();
+  c->rec_ids.release();
+  c->rec_count.release();
+  for (auto& ev : c->ev)
+    if (ev) cudaEventDestroy(ev);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+  return CTRAJ_OK;
+}
+
+int ctraj_set_stream(ctraj_context* c, void* stream) {
+  if (!c) return fail(CTRAJ_EINVAL, "ctx is NULL");
+  c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+  return CTRAJ_OK;
+}
+
+int ctraj_synchronize(ctraj_context* c) {
+  if (!c) return fail(CTRAJ_EINVAL, "ctx is NULL");
+  CT_CUDA(cudaSetDevice(c->device));
+  CT_CUDA(cudaStreamSynchronize(c->stream));
+  return CTRAJ_OK;
+}
+
+int ctraj_set_beamline(ctraj_context* c, const ctraj_element* el, int32_t n_el, int32_t n_labels) {
+  if (!c) return fail(CTRAJ_EINVAL, "ctx is NULL");
+  if (n_el < 0 || n_el > CTRAJ_MAX_ELEMENTS) return fail(CTRAJ_EINVAL, "n_elements %d out of range", n_el);
+  if (n_labels < 0 || n_labels > CTRAJ_MAX_LABELS) return fail(CTRAJ_EINVAL, "n_labels %d out of range", n_labels);
+  if (n_el > 0 && !el) return fail(CTRAJ_EINVAL, "elements is NULL");
+  for (int i = 0; i < n_el; ++i) {
+    const ctraj_element& e = el[i];
+    if (e.type < CTRAJ_CIRCULAR_APERTURE || e.type > CTRAJ_ELECTROSTATIC_LENS)
+      return fail(CTRAJ_EINVAL, "element %d: unknown type %d", i, e.type);
+    if (e.label < -1 || e.label >= n_labels || e.label_inside < -1 || e.label_inside >= n_labels)
+      return fail(CTRAJ_EINVAL, "element %d: label out of range", i);
+    if (i > 0 && e.z0 < el[i - 1].z0) return fail(CTRAJ_EINVAL, "elements are not sorted by z0 (element %d)", i);
+    if (e.type == CTRAJ_ELECTROSTATIC_LENS && (e.table < 0 || e.table >= CTRAJ_MAX_TABLES))
+      return fail(CTRAJ_EINVAL, "element %d: force table id %d out of range", i, e.table);
+  }
+  c->elements.assign(el, el + n_el);
+  c->n_labels = n_labels;
+  c->have_beamline = true;
+  c->lens_tables_dirty = true;
+  return CTRAJ_OK;
+}
+
+int ctraj_set_force_table(ctraj_context* c, int32_t id, const ctraj_force_table* t) {
+  if (!c || !t) return fail(CTRAJ_EINVAL, "NULL argument");
+  if (id < 0 || id >= CTRAJ_MAX_TABLES) return fail(CTRAJ_EINVAL, "table id %d out of range", id);
+  if (t->n_knots < 2 || !t->knots) return fail(CTRAJ_EINVAL, "table needs at least 2 knots");
+  if (t->kind == CTRAJ_TABLE_STARK_SPLINE && !t->coef) return fail(CTRAJ_EINVAL, "spline table without coef");
+  if (t->kind == CTRAJ_TABLE_RADIAL_LINEAR && !t->values) return fail(CTRAJ_EINVAL, "radial table without values");
+  if (t->kind != CTRAJ_TABLE_STARK_SPLINE && t->kind != CTRAJ_TABLE_RADIAL_LINEAR)
+    return fail(CTRAJ_EINVAL, "unknown table kind %d", t->kind);
+  const double h = (t->knots[t->n_knots - 1] - t->knots[0]) / double(t->n_knots - 1);
+  if (!(h > 0)) return fail(CTRAJ_EINVAL, "table knots must ascend");
+  for (int j = 1; j < t->n_knots; ++j)
+    if (std::fabs((t->knots[j] - t->knots[j - 1]) - h) > 1e-6 * h)
+      return fail(CTRAJ_EINVAL, "table knots must be uniformly spaced (knot %d)", j);
+  HostTable& ht = c->tables[id];
+  ht.kind = t->kind;
+  ht.n = t->n_knots;
+  ht.knots.assign(t->knots, t->knots + t->n_knots);
+  ht.coef.clear();
+  ht.values.clear();
+  if (t->kind == CTRAJ_TABLE_STARK_SPLINE) ht.coef.assign(t->coef, t->coef + size_t(t->n_knots - 1) * 4);
+  else ht.values.assign(t->values, t->values + t->n_knots);
+  ht.uploaded = false;
+  c->lens_tables_dirty = true;
+  return CTRAJ_OK;
+}
+
+int ctraj_run(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* stats) {
+  if (!c) return fail(CTRAJ_EINVAL, "ctx is NULL");
+  int st = validate_run(c, a);
+  if (st) return st;
+  Plan P;
+  RunDev R;
+  if ((st = prepare(c, a, P, R))) return st;
+  const int64_t n = a->n;
+  const size_t cap = size_t(std::max<int64_t>(n, 1));
+  int n_lens = 0;
+  for (int i = 0; i < P.n_el; ++i) n_lens += P.el[i].type == CTRAJ_ELECTROSTATIC_LENS;
+  if ((st = c->queue[0].ensure(queue_bytes(cap, a->precision)))) return st;
+  if (n_lens > 1 && (st = c->queue[1].ensure(queue_bytes(cap, a->precision)))) return st;
+  unsigned* ctl = c->qctl.as<unsigned>();
+  unsigned long long* counts = c->qctl.as<unsigned long long>(256);
+  unsigned long long* dstats = c->qctl.as<unsigned long long>(256 + 8 * (CTRAJ_MAX_LABELS + 1));
+  Queue q[2] = {make_queue(c->queue[0], cap, a->precision, ctl),
+                make_queue(n_lens > 1 ? c->queue[1] : c->queue[0], cap, a->precision, ctl + 2)};
+  CT_CUDA(cudaMemsetAsync(c->qctl.p, 0, 4096, c->stream));
+  R.counts = counts;
+  R.stats = dstats;
+  const bool out = a->out_mode != CTRAJ_OUT_NONE;
+  if (a->out_mode == CTRAJ_OUT_HOST && n > 0) {
+    const size_t b = align256(n * 4) * 2 + align256(n * 8) + align256(n * 80);
+    if ((st = c->outs.ensure(b))) return st;
+    R.out_label = a->out_label ? c->outs.as<int32_t>(0) : nullptr;
+    R.out_rows = a->out_rows ? c->outs.as<int32_t>(align256(n * 4)) : nullptr;
+    R.out_margin = a->out_margin ? c->outs.as<double>(2 * align256(n * 4)) : nullptr;
+    R.out_final = a->out_final ? c->outs.as<double>(2 * align256(n * 4) + align256(n * 8)) : nullptr;
+  } else if (a->out_mode == CTRAJ_OUT_DEVICE) {
+    R.out_label = a->out_label;
+    R.out_rows = a->out_rows;
+    R.out_margin = a->out_margin;
+    R.out_final = a->out_final;
+  }
+  int launches = 0;
+  c->timing = a->timing != 0;
+  if (a->precision == 32)
+    st = out ? launch_all<false, true>(c, P, R, q, &launches) : launch_all<false, false>(c, P, R, q, &launches);
+  else
+    st = out ? launch_all<true, true>(c, P, R, q, &launches) : launch_all<true, false>(c, P, R, q, &launches);
+  if (st) return st;
+  unsigned long long hc[CTRAJ_MAX_LABELS + 1], hs[kStatCount];
+  CT_CUDA(cudaMemcpyAsync(hc, counts, sizeof hc, cudaMemcpyDeviceToHost, c->stream));
+  CT_CUDA(cudaMemcpyAsync(hs, dstats, sizeof hs, cudaMemcpyDeviceToHost, c->stream));
+  if (a->out_mode == CTRAJ_OUT_HOST && n > 0) {
+    if (a->out_label) CT_CUDA(cudaMemcpyAsync(a->out_label, R.out_label, n * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (a->out_rows) CT_CUDA(cudaMemcpyAsync(a->out_rows, R.out_rows, n * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (a->out_margin) CT_CUDA(cudaMemcpyAsync(a->out_margin, R.out_margin, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (a->out_final) CT_CUDA(cudaMemcpyAsync(a->out_final, R.out_final, n * 80, cudaMemcpyDeviceToHost, c->stream));
+  }
+  CT_CUDA(cudaStreamSynchronize(c->stream));
+  for (int k = 0; k <= c->n_labels; ++k) a->counts[k] = int64_t(hc[k]);
+  if (stats) {
+    std::memset(stats, 0, sizeof *stats);
+    stats->molecules = n;
+    stats->molecule_steps = int64_t(hs[kStatSteps]);
+    stats->lens_steps = int64_t(hs[kStatLensSteps]);
+    stats->edge_band = (a->precision == 64 || out) ? int64_t(hs[kStatEdgeBand]) : -1;
+    stats->table_range = int64_t(hs[kStatTableRange]);
+    stats->bad_steps = int64_t(hs[kStatBadSteps]);
+    stats->kernels = launches;
+    if (c->timing) {
+      stats->timed = 1;
+      CT_CUDA(cudaEventElapsedTime(&stats->front_ms, c->ev[0], c->ev[1]));
+      CT_CUDA(cudaEventElapsedTime(&stats->lens_ms, c->ev[1], c->ev[2]));
+    }
+  }
+  if (hs[kStatRangeError])
+    return fail(CTRAJ_ERANGE, "%llu molecules looked up the lens table above its last knot "
+                "(interp1d would raise ValueError)", hs[kStatRangeError]);
+  if (hs[kStatBadSteps])
+    return fail(CTRAJ_ESTEPS, "%llu molecules have a non-finite or oversize lens step count rint(L/dz)",
+                hs[kStatBadSteps]);
+  return CTRAJ_OK;
+}
+
+int ctraj_record(ctraj_context* c, const ctraj_run_args* a, const int64_t* ids, int64_t n_ids,
+                 int32_t stride, int32_t max_rows, double* rows, int32_t* row_count) {
+  if (!c) return fail(CTRAJ_EINVAL, "ctx is NULL");
+  int st = validate_run(c, a);
+  if (st) return st;
+  if (n_ids < 0 || (n_ids > 0 && (!ids || !rows || !row_count)) || stride < 1 || max_rows < 1)
+    return fail(CTRAJ_EINVAL, "bad record arguments");
+  for (int64_t k = 0; k < n_ids; ++k)
+    if (ids[k] < 0 || ids[k] >= a->n) return fail(CTRAJ_EINVAL, "id %lld out of range", (long long)ids[k]);
+  if (n_ids == 0) return CTRAJ_OK;
+  Plan P;
+  RunDev R;
+  if ((st = prepare(c, a, P, R))) return st;
+  for (int i = 0; i < P.n_el; ++i) P.lf[i].n_smem = 0;  // the replay reads tables from global memory
+  const size_t rb = size_t(n_ids) * size_t(max_rows) * 10 * 8;
+  if ((st = c->rec_rows.ensure(rb))) return st;
+  if ((st = c->rec_ids.ensure(size_t(n_ids) * 8))) return st;
+  if ((st = c->rec_count.ensure(align256(size_t(n_ids) * 4) + 256))) return st;
+  unsigned* overflow = c->rec_count.as<unsigned>(align256(size_t(n_ids) * 4));
+  CT_CUDA(cudaMemcpyAsync(c->rec_ids.p, ids, size_t(n_ids) * 8, cudaMemcpyHostToDevice, c->stream));
+  CT_CUDA(cudaMemsetAsync(overflow, 0, 4, c->stream));
+  const int threads = 128;
+  const int grid = int((n_ids + threads - 1) / threads);
+  if (a->precision == 32)
+    k_record<Mol32<true, true>, false><<<grid, threads, 0, c->stream>>>(
+        P, R, c->rec_ids.as<int64_t>(), n_ids, stride, max_rows, c->rec_rows.as<double>(),
+        c->rec_count.as<int32_t>(), overflow);
+  else
+    k_record<Mol64<true>, true><<<grid, threads, 0, c->stream>>>(
+        P, R, c->rec_ids.as<int64_t>(), n_ids, stride, max_rows, c->rec_rows.as<double>(),
+        c->rec_count.as<int32_t>(), overflow);
+  CT_CUDA(cudaGetLastError());
+  unsigned ovf = 0;
+  CT_CUDA(cudaMemcpyAsync(rows, c->rec_rows.p, rb, cudaMemcpyDeviceToHost, c->stream));
+  CT_CUDA(cudaMemcpyAsync(row_count, c->rec_count.p, size_t(n_ids) * 4, cudaMemcpyDeviceToHost, c->stream));
+  CT_CUDA(cudaMemcpyAsync(&ovf, overflow, 4, cudaMemcpyDeviceToHost, c->stream));
+  CT_CUDA(cudaStreamSynchronize(c->stream));
+  if (ovf) return fail(CTRAJ_EOVERFLOW, "%u molecules need more than max_rows = %d rows", ovf, max_rows);
+  return CTRAJ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,310 @@
+// Propagation kernels.
+//
+// One run = k_front over all molecules, then one k_lens per electrostatic
+// lens in beamline order.
+//
+// k_front (one thread per molecule, grid-stride): draws or loads the initial
+//   conditions, walks the ballistic elements in closed form and stops at the
+//   first lens entrance.  Molecules lost on the way (98 % on the lens-beamline
+//   workload) are tallied at once; survivors are appended to a queue with one
+//   atomic per warp (ballot + prefix popcount), which is the stream compaction
+//   between element segments.
+// k_lens (persistent, one table copy in shared memory per CTA): each warp
+//   takes molecules from the queue and integrates the lens interior with RK4.
+//   A lane whose molecule is lost or reaches the lens exit is refilled from the
+//   queue at the next refill point (every `refill` steps), so warps stay full
+//   while molecules die at different steps.  Finished molecules do the exit
+//   snap and the ballistic elements after the lens, then are tallied or queued
+//   for the next lens.
+// k_record: replays chosen molecules one thread each and writes their
+//   trajectory rows (trajectory recording for apertures of interest).
+//
+// Tallies: each warp combines equal labels with __match_any_sync and adds the
+// popcount to a shared-memory counter; each CTA flushes its counters to global
+// memory once (integer atomics, so the totals do not depend on order).
+#pragma once
+#include "molecule.cuh"
+
+namespace ctraj {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kThreads = 256;
+
+struct BlockTally {
+  unsigned long long cnt[CTRAJ_MAX_LABELS + 1];
+  unsigned long long stat[kStatCount];
+};
+
+__device__ __forceinline__ void tally_init(BlockTally& S) {
+  for (int k = threadIdx.x; k < CTRAJ_MAX_LABELS + 1; k += blockDim.x) S.cnt[k] = 0;
+  for (int k = threadIdx.x; k < kStatCount; k += blockDim.x) S.stat[k] = 0;
+}
+
+// all 32 lanes must call this together
+__device__ __forceinline__ void tally_warp(BlockTally& S, int label, int n_labels) {
+  const unsigned peers = __match_any_sync(kFull, label);
+  const int lane = threadIdx.x & 31;
+  if (label != kNone && label != kQueued && lane == __ffs(peers) - 1) {
+    const int slot = label < 0 ? n_labels : label;
+    atomicAdd(&S.cnt[slot], (unsigned long long)__popc(peers));
+  }
+}
+
+__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+// all 32 lanes must call this together
+__device__ __forceinline__ void stat_add(BlockTally& S, int k, unsigned long long v) {
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(&S.stat[k], v);
+}
+
+__device__ __forceinline__ void tally_flush(BlockTally& S, const RunDev& R, int n_labels) {
+  __syncthreads();
+  for (int k = threadIdx.x; k <= n_labels; k += blockDim.x)
+    if (S.cnt[k]) atomicAdd(&R.counts[k], S.cnt[k]);
+  for (int k = threadIdx.x; k < kStatCount; k += blockDim.x)
+    if (S.stat[k]) atomicAdd(&R.stats[k], S.stat[k]);
+}
+
+// Reserve queue slots for the lanes with push == true (all lanes call).
+__device__ __forceinline__ unsigned queue_slot(bool push, unsigned* count) {
+  const unsigned m = __ballot_sync(kFull, push);
+  const int lane = threadIdx.x & 31;
+  unsigned base = 0;
+  if (m) {
+    const int leader = __ffs(m) - 1;
+    if (lane == leader) base = atomicAdd(count, unsigned(__popc(m)));
+    base = __shfl_sync(kFull, base, leader);
+  }
+  return base + unsigned(__popc(m & ((1u << lane) - 1u)));
+}
+
+template <class M, bool kOut>
+__device__ __forceinline__ void write_outputs(const RunDev& R, const M& m, int label) {
+  if (!kOut) return;
+  const int64_t i = m.id;
+  if (R.out_label) R.out_label[i] = label;
+  if (R.out_rows) R.out_rows[i] = m.rows;
+  if (R.out_margin) R.out_margin[i] = double(m.margin);
+  if (R.out_final) m.final_row(R.out_final, i, R.n);
+}
+
+// ---------------------------------------------------------------------------
+template <class M, bool kOut>
+__global__ void __launch_bounds__(kThreads) k_front(const __grid_constant__ Plan P, const RunDev R,
+                                                    const Queue Q) {
+  __shared__ BlockTally S;
+  tally_init(S);
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  unsigned long long steps = 0, band = 0;
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t base = int64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31); base < R.n; base += stride) {
+    const int64_t i = base + lane;
+    int label = kNone;
+    M m;
+    if (i < R.n) {
+      m.init(P, R, i);
+      int lens_at = -1;
+      label = walk(m, P, 0, &lens_at);
+      if (label != kQueued) {
+        steps += unsigned(m.rows);
+        band += (m.margin < double(kEdgeBand)) ? 1 : 0;
+        write_outputs<M, kOut>(R, m, label);
+      }
+    }
+    const unsigned slot = queue_slot(label == kQueued, Q.count);
+    if (label == kQueued) m.store(Q, slot);
+    tally_warp(S, label, P.n_labels);
+  }
+  stat_add(S, kStatSteps, steps);
+  stat_add(S, kStatEdgeBand, band);
+  tally_flush(S, R, P.n_labels);
+}
+
+// ---------------------------------------------------------------------------
+enum : int { kFree = 0, kRun = 1, kLost = 2, kExit = 3, kExhausted = 4 };
+
+template <class M, bool kOut, int F, bool k64>
+__global__ void __launch_bounds__(kThreads) k_lens(const __grid_constant__ Plan P, const RunDev R,
+                                                   const int li, const Queue Qin, const Queue Qout,
+                                                   const int refill) {
+  extern __shared__ float4 s_tab[];
+  __shared__ BlockTally S;
+  tally_init(S);
+  const LensF& L = P.lf[li];
+  if (!k64)
+    for (int k = threadIdx.x; k < L.n_smem; k += blockDim.x) s_tab[k] = __ldg(L.q + k);
+  __syncthreads();
+
+  const ctraj_element& e = P.el[li];
+  const unsigned n_in = *(volatile unsigned*)Qin.count;
+  const int lane = threadIdx.x & 31;
+  unsigned long long steps = 0, lsteps = 0, band = 0, bad = 0, range = 0, rerr = 0;
+
+  M m;
+  LensStep st;
+  float dt = 0.f, hdt = 0.f, c2 = 0.f, dt6 = 0.f, dt26 = 0.f;
+  int phase = kFree;
+  unsigned flags = 0;
+  const bool classic = e.scheme == CTRAJ_RK4_CLASSIC;
+
+  for (;;) {
+    // refill lanes without a molecule
+    for (;;) {
+      const unsigned need = __ballot_sync(kFull, phase == kFree);
+      if (!need) break;
+      const int leader = __ffs(need) - 1;
+      unsigned base = 0;
+      if (lane == leader) base = atomicAdd(Qin.head, unsigned(__popc(need)));
+      base = __shfl_sync(kFull, base, leader);
+      int label = kNone;
+      if (phase == kFree) {
+        const unsigned idx = base + unsigned(__popc(need & ((1u << lane) - 1u)));
+        if (idx >= n_in) {
+          phase = kExhausted;
+        } else {
+          m.load(Qin, idx, P);
+          flags = 0;
+          if (!lens_setup(e, m.vel_z(), st)) {
+            // rint(L/dz) not finite or too large: the reference raises here
+            ++bad;
+            label = e.label_inside;
+            steps += unsigned(m.rows);
+            write_outputs<M, kOut>(R, m, label);
+          } else {
+            m.lens_begin(P, li, st);
+            dt = float(st.dt);
+            hdt = 0.5f * dt;
+            c2 = classic ? hdt : dt;
+            dt6 = dt * (1.0f / 6.0f);
+            dt26 = float(st.dt * st.dt / 6.0);
+            phase = st.n_total > 0 ? kRun : kExit;
+          }
+        }
+      }
+      tally_warp(S, label, P.n_labels);
+    }
+    if (__all_sync(kFull, phase == kExhausted)) break;
+
+    // integrate
+    for (int k = 0; k < refill; ++k) {
+      if (phase == kRun) {
+        bool lost;
+        if constexpr (k64) {
+          int rg = 0, er = 0;
+          lost = m.lens_step(P, li, st, rg, er);
+          flags |= (rg ? 1u : 0u) | (er ? 2u : 0u);
+        } else {
+          lost = m.template lens_step<F>(P, li, dt, hdt, c2, dt6, dt26, s_tab, flags);
+          if (F == kForceRadial && (flags & 2u)) lost = true;
+        }
+        ++st.n_done;
+        m.lens_row(P, li, st);
+        if (lost) phase = kLost;
+        else if (st.n_done == st.n_total) phase = kExit;
+      }
+    }
+
+    // finish molecules that left the lens or were lost in it
+    int label = kNone;
+    const bool done = phase == kLost || phase == kExit;
+    if (done) {
+      lsteps += unsigned(st.n_done);
+      range += (flags & 1u) ? 1 : 0;
+      rerr += (flags & 2u) ? 1 : 0;
+      m.lens_end(P, li, st, phase == kLost);
+      if (phase == kLost) {
+        label = e.label_inside;
+      } else {
+        int lens_at = -1;
+        label = walk(m, P, li + 1, &lens_at);
+      }
+      if (label != kQueued) {
+        steps += unsigned(m.rows);
+        band += (m.margin < double(kEdgeBand)) ? 1 : 0;
+        write_outputs<M, kOut>(R, m, label);
+      }
+    }
+    const unsigned slot = queue_slot(label == kQueued, Qout.count);
+    if (label == kQueued) m.store(Qout, slot);
+    tally_warp(S, label, P.n_labels);
+    if (done) phase = kFree;
+  }
+  stat_add(S, kStatSteps, steps);
+  stat_add(S, kStatLensSteps, lsteps);
+  stat_add(S, kStatEdgeBand, band);
+  stat_add(S, kStatBadSteps, bad);
+  stat_add(S, kStatTableRange, range);
+  stat_add(S, kStatRangeError, rerr);
+  tally_flush(S, R, P.n_labels);
+}
+
+// ---------------------------------------------------------------------------
+// Replay of selected molecules with row recording (one thread per molecule).
+template <class M>
+__device__ __forceinline__ bool step_any(M& m, const Plan& P, int li, const float dt, const float hdt,
+                                         const float c2, const float dt6, const float dt26,
+                                         unsigned& flags) {
+  switch (P.lf[li].force) {
+    case kForceStark2:
+      return m.template lens_step<kForceStark2>(P, li, dt, hdt, c2, dt6, dt26, nullptr, flags);
+    case kForceStark1:
+      return m.template lens_step<kForceStark1>(P, li, dt, hdt, c2, dt6, dt26, nullptr, flags);
+    default:
+      return m.template lens_step<kForceRadial>(P, li, dt, hdt, c2, dt6, dt26, nullptr, flags) ||
+             (flags & 2u);
+  }
+}
+
+// The replay plan has n_smem = 0 for every lens, so table reads go to global memory.
+template <class M, bool k64>
+__global__ void __launch_bounds__(128) k_record(const __grid_constant__ Plan P, const RunDev R,
+                                                const int64_t* ids, int64_t n_ids, int stride,
+                                                int max_rows, double* rows_out, int32_t* count_out,
+                                                unsigned* overflow) {
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n_ids) return;
+  RowSink sink{rows_out + size_t(k) * size_t(max_rows) * 10, max_rows, stride, 0, 0, false};
+  M m;
+  m.sink = &sink;
+  m.init(P, R, ids[k]);
+  int from = 0;
+  for (;;) {
+    int lens_at = -1;
+    const int label = walk(m, P, from, &lens_at);
+    if (label != kQueued) break;
+    const ctraj_element& e = P.el[lens_at];
+    LensStep st;
+    if (!lens_setup(e, m.vel_z(), st)) break;
+    m.lens_begin(P, lens_at, st);
+    const float dt = float(st.dt), hdt = 0.5f * dt;
+    const float c2 = e.scheme == CTRAJ_RK4_CLASSIC ? hdt : dt;
+    const float dt6 = dt * (1.0f / 6.0f), dt26 = float(st.dt * st.dt / 6.0);
+    bool lost = false;
+    unsigned flags = 0;
+    while (st.n_done < st.n_total) {
+      if constexpr (k64) {
+        int rg = 0, er = 0;
+        lost = m.lens_step(P, lens_at, st, rg, er);
+      } else {
+        lost = step_any(m, P, lens_at, dt, hdt, c2, dt6, dt26, flags);
+      }
+      ++st.n_done;
+      m.lens_row(P, lens_at, st);
+      if (lost) break;
+    }
+    m.lens_end(P, lens_at, st, lost);
+    if (lost) break;
+    from = lens_at + 1;
+  }
+  m.flush_last();
+  count_out[k] = sink.written;
+  if (sink.written > max_rows) atomicAdd(overflow, 1u);
+}
+
+}  // namespace ctraj

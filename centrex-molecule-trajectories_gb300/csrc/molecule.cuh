@@ -1,0 +1,619 @@
+// Per-molecule state and element physics, in two precisions.
+//
+// Mol64 follows the reference's float64 operation order step for step, using
+// __dadd_rn/__dmul_rn (never contracted into FMA) and IEEE division and square
+// root, so on ballistic paths it reproduces the reference bit for bit:
+//   update_trajectory    molecule.py:26-68
+//   aperture hit tests   apertures.py:101-115, 174-189
+//   field plates         apertures.py:227-270
+//   lens force           electrostatic_lens.py:215-227 with scipy's PPoly
+//                        (nu = 1) or numpy.interp evaluation order
+//   lens RK4 step        electrostatic_lens.py:91-118
+//
+// Mol32 restates the same physics for speed.  The molecule always sits on the
+// last plane it reached, so a flight is (plane gap) * (1/vz) with the gap
+// precomputed in double on the host; z itself is never accumulated in float.
+// Inside the lens only the transverse state (x, y, vx, vy) evolves (a_z = 0)
+// and the force is a_perp = w(|r|) * (x, y) - g y^, w read from a per-interval
+// polynomial table.  The RK4 combination is rewritten exactly:
+//   x' = x + dt v + dt^2/6 (l1 + l2 + l3),  v' = v + dt/6 (l1 + 2 l2 + 2 l3 + l4)
+// (the reference's k1..k4 substituted), and the step count, step size and
+// exit-snap time are computed once per molecule in double.
+#pragma once
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+
+#include "philox.cuh"
+#include "plan.cuh"
+
+namespace ctraj {
+
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+
+// ---------------------------------------------------------------------------
+// FP64 force table lookups (reference evaluation order)
+// ---------------------------------------------------------------------------
+
+// scipy PPoly.__call__(E, nu=1): interval knots[i] <= E < knots[i+1], end
+// pieces extrapolated; res = 0 + c2*1*1; res += (c1*s)*2; res += (c0*(s*s))*3.
+__device__ inline double spline_deriv64(const TableD& T, double E, int& range) {
+  const int n = T.n;
+  int i;
+  if (isnan(E)) return E;
+  if (E < T.x0) {
+    i = 0;
+    range = 1;
+  } else if (E >= __ldg(T.knots + n - 1)) {
+    i = n - 2;
+    if (E > __ldg(T.knots + n - 1)) range = 1;
+  } else {
+    i = int(floor((E - T.x0) / T.h));
+    i = max(0, min(i, n - 2));
+    while (i > 0 && E < __ldg(T.knots + i)) --i;
+    while (i < n - 2 && E >= __ldg(T.knots + i + 1)) ++i;
+  }
+  const double* c = T.coef + 4 * size_t(i);
+  const double s = dadd(E, -__ldg(T.knots + i));
+  double res = 0.0;
+  res = dadd(res, dmul(dmul(__ldg(c + 2), 1.0), 1.0));
+  res = dadd(res, dmul(dmul(__ldg(c + 1), s), 2.0));
+  res = dadd(res, dmul(dmul(__ldg(c + 0), dmul(s, s)), 3.0));
+  return res;
+}
+
+// numpy.interp(r, knots, values) (what scipy's float64 linear interp1d calls),
+// with interp1d's bounds error above the last knot reported through err.
+__device__ inline double radial64(const TableD& T, double r, int& err) {
+  const int n = T.n;
+  const double last = __ldg(T.knots + n - 1);
+  if (r < T.x0 || r > last) {
+    err = 1;
+    return nan("");
+  }
+  if (isnan(r)) return r;
+  int j = int(floor((r - T.x0) / T.h));
+  j = max(0, min(j, n - 1));
+  while (j > 0 && __ldg(T.knots + j) > r) --j;
+  while (j < n - 1 && __ldg(T.knots + j + 1) <= r) ++j;
+  const double xj = __ldg(T.knots + j), yj = __ldg(T.values + j);
+  if (j == n - 1 || xj == r) return yj;
+  const double slope = (__ldg(T.values + j + 1) - yj) / (__ldg(T.knots + j + 1) - xj);
+  return dadd(dmul(slope, dadd(r, -xj)), yj);
+}
+
+// ElectrostaticLens.lens_acceleration (electrostatic_lens.py:215-227).
+__device__ inline void lens_force64(const Plan& P, const ctraj_element& e, double x0, double x1,
+                                    double& a0, double& a1, int& range, int& err) {
+  const TableD& T = P.td[e.table];
+  const double r = __dsqrt_rn(dadd(dmul(x0, x0), dmul(x1, x1)));
+  double a_r;
+  if (T.kind == CTRAJ_TABLE_RADIAL_LINEAR) {
+    a_r = radial64(T, r, err);
+  } else {
+    const double alpha = e.p[6], mass = e.p[5];
+    if (e.field_order == 1) {
+      const double E = dmul(alpha, r);
+      a_r = -dmul(spline_deriv64(T, E, range), alpha) / mass;
+    } else {
+      const double E = dmul(alpha, dmul(r, r));
+      a_r = -dmul(spline_deriv64(T, E, range), dmul(dmul(2.0, alpha), r)) / mass;
+    }
+  }
+  a0 = 0.0;
+  a1 = 0.0;
+  if (r != 0.0) {
+    a0 = dmul(a_r, x0) / r;
+    a1 = dmul(a_r, x1) / r;
+  }
+  a1 = dadd(a1, -P.g);
+}
+
+// ---------------------------------------------------------------------------
+// FP32 force: w such that a_perp = w * (x, y)
+// ---------------------------------------------------------------------------
+template <int F, bool kFirst = false>
+__device__ __forceinline__ float wforce(float px, float py, const LensF& L, const float4* s_tab,
+                                        unsigned& flags) {
+  const float r2 = __fmaf_rn(py, py, __fmul_rn(px, px));
+  float s, r = 0.0f;
+  if (F == kForceStark2) {
+    s = __fmaf_rn(L.beta, r2, -L.s0);
+  } else {
+    r = sqrtf(r2);
+    s = __fmaf_rn(L.beta, r, -L.s0);
+    if (F == kForceRadial) flags |= (r > L.r_max) ? 2u : 0u;
+  }
+  if (kFirst && F != kForceRadial) flags |= (s > float(L.n_int) || s < 0.0f) ? 1u : 0u;
+  int i = __float2int_rz(s);
+  i = max(0, min(i, L.n_int - 1));
+  const float u = __fadd_rn(s, -__int2float_rn(i));
+  const float4 q = (i < L.n_smem) ? s_tab[i] : __ldg(L.q + i);
+  if (F == kForceRadial) {
+    const float a_r = __fmaf_rn(u, q.y, q.x);
+    return r > 0.0f ? __fdividef(a_r, r) : 0.0f;
+  }
+  const float w = __fmaf_rn(u, __fmaf_rn(u, q.z, q.y), q.x);
+  if (F == kForceStark1) return r > 0.0f ? __fdividef(w, r) : 0.0f;
+  return w;
+}
+
+// Per-molecule lens integration parameters (both precisions).
+struct LensStep {
+  int64_t n_total;  // rint(L/dz)
+  int64_t n_done;
+  double dt;        // dz / vz
+  double snap;      // FP32: exit-snap time (z1 - z0 - N dz) / vz
+  double dz;
+};
+
+// Step count and step size exactly as electrostatic_lens.py:87-88, in double.
+__device__ __forceinline__ bool lens_setup(const ctraj_element& e, double vz, LensStep& s) {
+  const double dz = e.step_mode == CTRAJ_STEP_DT ? dmul(vz, e.p[2]) : e.p[1];
+  const double nf = rint(e.p[7] / dz);
+  s.dz = dz;
+  s.n_done = 0;
+  if (!(fabs(nf) <= double(CTRAJ_MAX_LENS_STEPS))) {  // also catches NaN / inf
+    s.n_total = 0;
+    s.dt = 0.0;
+    s.snap = 0.0;
+    return false;
+  }
+  s.n_total = nf < 0.0 ? 0 : int64_t(nf);
+  s.dt = dz / vz;
+  s.snap = ((e.z1 - e.z0) - double(s.n_total) * dz) / vz;
+  return true;
+}
+
+// Trajectory row sink used by the replay kernel.
+struct RowSink {
+  double* out;   // (max_rows, 10)
+  int max_rows;
+  int stride;
+  int64_t row;   // index of the last stored row (0 = initial)
+  int written;
+  bool last_written;
+  __device__ void put(double x, double y, double z, double vx, double vy, double vz, double ax,
+                      double ay, double az, double t) {
+    ++row;
+    last_written = false;
+    if (row % stride == 0) write(x, y, z, vx, vy, vz, ax, ay, az, t);
+  }
+  __device__ void write(double x, double y, double z, double vx, double vy, double vz, double ax,
+                        double ay, double az, double t) {
+    if (written < max_rows) {
+      double* o = out + size_t(written) * 10;
+      o[0] = x; o[1] = y; o[2] = z; o[3] = vx; o[4] = vy; o[5] = vz;
+      o[6] = ax; o[7] = ay; o[8] = az; o[9] = t;
+    }
+    ++written;
+    last_written = true;
+  }
+};
+
+// ===========================================================================
+// FP64: the reference's arithmetic
+// ===========================================================================
+template <bool kRec>
+struct Mol64 {
+  double x[3], v[3], a[3], t;
+  double margin;
+  int rows;
+  int32_t id;
+  RowSink* sink;
+
+  __device__ void row_out() {
+    if (kRec) sink->put(x[0], x[1], x[2], v[0], v[1], v[2], a[0], a[1], a[2], t);
+  }
+
+  __device__ void init(const Plan& P, const RunDev& R, int64_t i) {
+    id = int32_t(i);
+    margin = INFINITY;
+    rows = 0;
+    if (R.ic_mode == CTRAJ_IC_DEVICE_DRAW) {
+      const Words8 w = molecule_words(R.offset + uint64_t(i), R.seed);
+      double n0, n1, n2, n3, n4, n5;
+      box_muller(u01d(w.w[0]), u01d(w.w[1]), n0, n1);
+      box_muller(u01d(w.w[2]), u01d(w.w[3]), n2, n3);
+      box_muller(u01d(w.w[4]), u01d(w.w[5]), n4, n5);
+      const double* vp = R.vd.p;
+      v[0] = __fma_rn(vp[1], n0, vp[0]);
+      v[1] = __fma_rn(vp[3], n1, vp[2]);
+      v[2] = __fma_rn(vp[5], n2, vp[4]);
+      const double* xp = R.xd.p;
+      if (R.xd.kind == CTRAJ_DIST_DISC_POSITION) {
+        double s, c;
+        sincospi(2.0 * u01d(w.w[6]), &s, &c);
+        const double rr = dmul(sqrt(u01d(w.w[7])), dmul(xp[0], 0.5));
+        x[0] = dmul(rr, c);
+        x[1] = dmul(rr, s);
+        x[2] = xp[1];
+      } else {
+        x[0] = dmul(xp[0], n3);
+        x[1] = dmul(xp[1], n4);
+        x[2] = xp[2];
+      }
+    } else {
+      const size_t n = size_t(R.n);
+      for (int k = 0; k < 3; ++k) {
+        x[k] = R.ics[k * n + size_t(i)];
+        v[k] = R.ics[(3 + k) * n + size_t(i)];
+      }
+    }
+    a[0] = 0.0;
+    a[1] = -P.g;
+    a[2] = 0.0;
+    t = 0.0;
+    if (kRec) sink->write(x[0], x[1], x[2], v[0], v[1], v[2], a[0], a[1], a[2], t);
+  }
+
+  // Molecule.update_trajectory(delta_t, a=(0,-g,0))
+  __device__ void update(double dt, const Plan& P) {
+    if (dt != 0.0) {  // `if not delta_t` keeps x and v (molecule.py:31,41)
+      const double dt2 = dmul(dt, dt);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        x[k] = dadd(dadd(x[k], dmul(v[k], dt)), dmul(dmul(a[k], dt2), 0.5));
+        v[k] = dadd(v[k], dmul(a[k], dt));
+      }
+    }
+    t = dadd(t, dt);
+    a[0] = 0.0;
+    a[1] = -P.g;
+    a[2] = 0.0;
+    rows += isfinite(t) ? 1 : 0;
+    row_out();
+  }
+
+  __device__ void fly(const Plan& P, int i, int which) {
+    const double z = which ? P.el[i].z1 : P.el[i].z0;
+    update((z - x[2]) / v[2], P);
+  }
+
+  __device__ double rho() const { return __dsqrt_rn(dadd(dmul(x[0], x[0]), dmul(x[1], x[1]))); }
+
+  __device__ void note(double d) { margin = fmin(margin, fabs(d)); }
+
+  __device__ bool circle_out(const Plan& P, int i) {
+    const double r = rho(), h = dmul(P.el[i].p[0], 0.5);
+    note(dadd(r, -h));
+    return r > h;
+  }
+  __device__ bool rect_out(const Plan& P, int i) {
+    const double* p = P.el[i].p;
+    note(dadd(x[0], -p[0])); note(dadd(x[0], -p[1])); note(dadd(x[1], -p[2])); note(dadd(x[1], -p[3]));
+    return !((p[0] < x[0] && x[0] < p[1]) && (p[2] < x[1] && x[1] < p[3]));
+  }
+  // FieldPlates after the z0 flight: returns true when lost (apertures.py:238-270)
+  __device__ bool plates(const Plan& P, int i) {
+    const double x1 = P.el[i].p[0], x2 = P.el[i].p[1];
+    note(dadd(x[0], -x1)); note(dadd(x[0], -x2));
+    if (!(x1 < x[0] && x[0] < x2)) return true;
+    double dt = (P.el[i].z1 - x[2]) / v[2];
+    const double xe = dt != 0.0 ? dadd(dadd(x[0], dmul(v[0], dt)), dmul(dmul(a[0], dmul(dt, dt)), 0.5)) : x[0];
+    note(dadd(xe, -x1)); note(dadd(xe, -x2));
+    if (!(x1 < xe && xe < x2)) {
+      if (v[0] < 0) dt = (x1 - x[0]) / v[0];
+      else if (v[0] > 0) dt = (x2 - x[0]) / v[0];
+      update(dt, P);
+      return true;
+    }
+    update(dt, P);
+    return false;
+  }
+  __device__ bool lens_entrance_out(const Plan& P, int i) { return circle_out(P, i); }
+
+  __device__ double vel_z() const { return v[2]; }
+
+  // One reference RK4 step (electrostatic_lens.py:91-118); returns true when lost.
+  __device__ bool lens_step(const Plan& P, int i, const LensStep& s, int& range, int& err) {
+    const ctraj_element& e = P.el[i];
+    const double dt = s.dt;
+    const bool classic = e.scheme == CTRAJ_RK4_CLASSIC;
+    double k1[3], l1[3], k2[3], l2[3], k3[3], l3[3], k4[3], l4[3], p[3];
+    for (int k = 0; k < 3; ++k) k1[k] = v[k];
+    lens_force64(P, e, x[0], x[1], l1[0], l1[1], range, err);
+    l1[2] = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      k2[k] = dadd(k1[k], dmul(dmul(dt, l1[k]), 0.5));
+      p[k] = classic ? dadd(x[k], dmul(dmul(dt, k1[k]), 0.5)) : dadd(x[k], dmul(dt, k1[k]));
+    }
+    lens_force64(P, e, p[0], p[1], l2[0], l2[1], range, err);
+    l2[2] = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      k3[k] = dadd(k1[k], dmul(dmul(dt, l2[k]), 0.5));
+      p[k] = dadd(x[k], dmul(dmul(dt, k2[k]), 0.5));
+    }
+    lens_force64(P, e, p[0], p[1], l3[0], l3[1], range, err);
+    l3[2] = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      k4[k] = dadd(k1[k], dmul(dt, l3[k]));
+      p[k] = dadd(x[k], dmul(dt, k3[k]));
+    }
+    lens_force64(P, e, p[0], p[1], l4[0], l4[1], range, err);
+    l4[2] = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      const double sk = dadd(dadd(dadd(k1[k], dmul(2.0, k2[k])), dmul(2.0, k3[k])), k4[k]);
+      const double sl = dadd(dadd(dadd(l1[k], dmul(2.0, l2[k])), dmul(2.0, l3[k])), l4[k]);
+      x[k] = dadd(x[k], dmul(dt, sk) / 6.0);
+      v[k] = dadd(k1[k], dmul(dt, sl) / 6.0);
+      a[k] = l1[k];
+    }
+    t = dadd(t, dt);
+    rows += isfinite(t) ? 1 : 0;
+    row_out();
+    if (err) return true;
+    const double r = rho(), h = dmul(e.p[0], 0.5);
+    note(dadd(r, -h));
+    return r > h;
+  }
+
+  __device__ void lens_begin(const Plan&, int, const LensStep&) {}
+  __device__ void lens_row(const Plan&, int, const LensStep&) {}
+  // After the last step: the exit snap with the stored acceleration l1
+  // (electrostatic_lens.py:74-77) unless the molecule was lost inside.
+  __device__ void lens_end(const Plan& P, int i, const LensStep&, bool lost) {
+    if (!lost) fly(P, i, 1);
+  }
+
+  __device__ void final_row(double* f, int64_t i, int64_t n) const {
+    const double vals[10] = {x[0], x[1], x[2], v[0], v[1], v[2], a[0], a[1], a[2], t};
+    for (int k = 0; k < 10; ++k) f[size_t(k) * size_t(n) + size_t(i)] = vals[k];
+  }
+  __device__ void flush_last() {
+    if (kRec && !sink->last_written) sink->write(x[0], x[1], x[2], v[0], v[1], v[2], a[0], a[1], a[2], t);
+  }
+
+  __device__ void store(const Queue& Q, unsigned s) const {
+    Q.dx[s] = x[0]; Q.dy[s] = x[1]; Q.dz[s] = x[2];
+    Q.dvx[s] = v[0]; Q.dvy[s] = v[1]; Q.dvz[s] = v[2];
+    Q.dt[s] = t; Q.margin[s] = margin; Q.rows[s] = rows; Q.id[s] = id;
+  }
+  __device__ void load(const Queue& Q, unsigned s, const Plan& P) {
+    x[0] = Q.dx[s]; x[1] = Q.dy[s]; x[2] = Q.dz[s];
+    v[0] = Q.dvx[s]; v[1] = Q.dvy[s]; v[2] = Q.dvz[s];
+    t = Q.dt[s]; margin = Q.margin[s]; rows = Q.rows[s]; id = Q.id[s];
+    a[0] = 0.0; a[1] = -P.g; a[2] = 0.0;
+  }
+};
+
+// ===========================================================================
+// FP32 fast path
+// ===========================================================================
+template <bool kOut, bool kRec>
+struct Mol32 {
+  float x, y, vx, vy, vz, inv_vz, t;
+  float gap0;     // first flight length (from the initial z)
+  float margin;
+  int rows;
+  int32_t id;
+  double zc;      // current z, kept only for outputs / recording
+  float ax, ay;   // stored acceleration (recording)
+  double t0;      // time at the lens entrance
+  RowSink* sink;
+
+  __device__ void row_out() {
+    if (kRec) sink->put(x, y, zc, vx, vy, vz, ax, ay, 0.0, t);
+  }
+
+  __device__ void init(const Plan& P, const RunDev& R, int64_t i) {
+    id = int32_t(i);
+    margin = INFINITY;
+    rows = 0;
+    double z_ic;
+    if (R.ic_mode == CTRAJ_IC_DEVICE_DRAW) {
+      const Words8 w = molecule_words(R.offset + uint64_t(i), R.seed);
+      float n0, n1, n2, n3, n4, n5;
+      box_muller(u01f(w.w[0]), u01f(w.w[1]), n0, n1);
+      box_muller(u01f(w.w[2]), u01f(w.w[3]), n2, n3);
+      box_muller(u01f(w.w[4]), u01f(w.w[5]), n4, n5);
+      const double* vp = R.vd.p;
+      vx = __fmaf_rn(float(vp[1]), n0, float(vp[0]));
+      vy = __fmaf_rn(float(vp[3]), n1, float(vp[2]));
+      vz = __fmaf_rn(float(vp[5]), n2, float(vp[4]));
+      const double* xp = R.xd.p;
+      if (R.xd.kind == CTRAJ_DIST_DISC_POSITION) {
+        float s, c;
+        sincospif(2.0f * u01f(w.w[6]), &s, &c);
+        const float rr = __fmul_rn(sqrtf(u01f(w.w[7])), float(xp[0] * 0.5));
+        x = __fmul_rn(rr, c);
+        y = __fmul_rn(rr, s);
+        z_ic = xp[1];
+      } else {
+        x = __fmul_rn(float(xp[0]), n3);
+        y = __fmul_rn(float(xp[1]), n4);
+        z_ic = xp[2];
+      }
+      gap0 = R.gap0f;
+    } else {
+      const size_t n = size_t(R.n);
+      x = float(R.ics[size_t(i)]);
+      y = float(R.ics[n + size_t(i)]);
+      z_ic = R.ics[2 * n + size_t(i)];
+      vx = float(R.ics[3 * n + size_t(i)]);
+      vy = float(R.ics[4 * n + size_t(i)]);
+      vz = float(R.ics[5 * n + size_t(i)]);
+      gap0 = P.n_el > 0 ? float(P.el[0].z0 - z_ic) : 0.0f;
+    }
+    inv_vz = __frcp_rn(vz);
+    t = 0.0f;
+    ax = 0.0f;
+    ay = -P.gf;
+    if (kOut || kRec) zc = z_ic;
+    if (kRec) sink->write(x, y, zc, vx, vy, vz, ax, ay, 0.0, t);
+  }
+
+  // ballistic flight of dt with stored acceleration (ax, ay); afterwards a = (0, -g)
+  __device__ void flight(float dt, const Plan& P) {
+    const float h = __fmul_rn(__fmul_rn(0.5f, dt), dt);
+    x = __fmaf_rn(ax, h, __fmaf_rn(vx, dt, x));
+    y = __fmaf_rn(ay, h, __fmaf_rn(vy, dt, y));
+    vx = __fmaf_rn(ax, dt, vx);
+    vy = __fmaf_rn(ay, dt, vy);
+    t = __fadd_rn(t, dt);
+    ax = 0.0f;
+    ay = -P.gf;
+    rows += isfinite(t) ? 1 : 0;
+  }
+
+  __device__ void fly(const Plan& P, int i, int which) {
+    const float gap = which ? P.ef[i].len : (i == 0 ? gap0 : P.ef[i].gap);
+    flight(__fmul_rn(gap, inv_vz), P);
+    if (kOut || kRec) zc = which ? P.el[i].z1 : P.el[i].z0;
+    row_out();
+  }
+
+  __device__ void note(float d) {
+    if (kOut) margin = fminf(margin, fabsf(d));
+  }
+
+  __device__ bool circle_out(const Plan& P, int i) {
+    const float r2 = __fmaf_rn(y, y, __fmul_rn(x, x));
+    if (kOut) note(__fadd_rn(sqrtf(r2), -P.ef[i].c[1]));
+    return r2 > P.ef[i].c[0];
+  }
+  __device__ bool rect_out(const Plan& P, int i) {
+    const float* c = P.ef[i].c;
+    if (kOut) { note(x - c[0]); note(x - c[1]); note(y - c[2]); note(y - c[3]); }
+    return !((c[0] < x && x < c[1]) && (c[2] < y && y < c[3]));
+  }
+  __device__ bool plates(const Plan& P, int i) {
+    const float x1 = P.ef[i].c[0], x2 = P.ef[i].c[1];
+    if (kOut) { note(x - x1); note(x - x2); }
+    if (!(x1 < x && x < x2)) return true;
+    float dt = __fmul_rn(P.ef[i].len, inv_vz);
+    const float xe = __fmaf_rn(vx, dt, x);  // a_x = 0 after a ballistic flight
+    if (kOut) { note(xe - x1); note(xe - x2); }
+    if (!(x1 < xe && xe < x2)) {
+      if (vx < 0.0f) dt = __fdiv_rn(x1 - x, vx);
+      else if (vx > 0.0f) dt = __fdiv_rn(x2 - x, vx);
+      flight(dt, P);
+      if (kOut || kRec) zc += double(dt) * double(vz);
+      row_out();
+      return true;
+    }
+    flight(dt, P);
+    if (kOut || kRec) zc = P.el[i].z1;
+    row_out();
+    return false;
+  }
+  __device__ bool lens_entrance_out(const Plan& P, int i) { return circle_out(P, i); }
+
+  __device__ double vel_z() const { return double(vz); }
+
+  template <int F>
+  __device__ bool lens_step(const Plan& P, int i, const float dt, const float hdt, const float c2,
+                            const float dt6, const float dt26, const float4* s_tab, unsigned& flags) {
+    const LensF& L = P.lf[i];
+    const float g = P.gf;
+    const float w1 = wforce<F, true>(x, y, L, s_tab, flags);
+    const float l1x = __fmul_rn(w1, x), l1y = __fmaf_rn(w1, y, -g);
+    const float k2x = __fmaf_rn(hdt, l1x, vx), k2y = __fmaf_rn(hdt, l1y, vy);
+    const float p2x = __fmaf_rn(c2, vx, x), p2y = __fmaf_rn(c2, vy, y);
+    const float w2 = wforce<F>(p2x, p2y, L, s_tab, flags);
+    const float l2x = __fmul_rn(w2, p2x), l2y = __fmaf_rn(w2, p2y, -g);
+    const float k3x = __fmaf_rn(hdt, l2x, vx), k3y = __fmaf_rn(hdt, l2y, vy);
+    const float p3x = __fmaf_rn(hdt, k2x, x), p3y = __fmaf_rn(hdt, k2y, y);
+    const float w3 = wforce<F>(p3x, p3y, L, s_tab, flags);
+    const float l3x = __fmul_rn(w3, p3x), l3y = __fmaf_rn(w3, p3y, -g);
+    const float p4x = __fmaf_rn(dt, k3x, x), p4y = __fmaf_rn(dt, k3y, y);
+    const float w4 = wforce<F>(p4x, p4y, L, s_tab, flags);
+    const float l4x = __fmul_rn(w4, p4x), l4y = __fmaf_rn(w4, p4y, -g);
+    const float sx = __fadd_rn(__fadd_rn(l1x, l2x), l3x);
+    const float sy = __fadd_rn(__fadd_rn(l1y, l2y), l3y);
+    x = __fmaf_rn(dt26, sx, __fmaf_rn(dt, vx, x));
+    y = __fmaf_rn(dt26, sy, __fmaf_rn(dt, vy, y));
+    vx = __fmaf_rn(dt6, __fmaf_rn(2.0f, __fadd_rn(l2x, l3x), __fadd_rn(l1x, l4x)), vx);
+    vy = __fmaf_rn(dt6, __fmaf_rn(2.0f, __fadd_rn(l2y, l3y), __fadd_rn(l1y, l4y)), vy);
+    ax = l1x;
+    ay = l1y;
+    const float r2 = __fmaf_rn(y, y, __fmul_rn(x, x));
+    if (kOut) note(__fadd_rn(sqrtf(r2), -P.ef[i].c[1]));
+    return r2 > P.ef[i].c[0];
+  }
+
+  // Inside the lens t and z follow from the step count (t0 + n dt, z0 + n dz)
+  // instead of being accumulated in float.
+  __device__ void lens_begin(const Plan&, int, const LensStep&) { t0 = double(t); }
+  __device__ void lens_row(const Plan& P, int i, const LensStep& s) {
+    if (kRec) {
+      zc = P.el[i].z0 + double(s.n_done) * s.dz;
+      sink->put(x, y, zc, vx, vy, vz, ax, ay, 0.0, t0 + double(s.n_done) * s.dt);
+    }
+  }
+  // After the last step: t from the step count, then the exit snap of
+  // (z1 - z0 - N dz) / vz with the stored acceleration l1 unless lost inside.
+  __device__ void lens_end(const Plan& P, int i, const LensStep& s, bool lost) {
+    t = float(t0 + double(s.n_done) * s.dt);
+    rows += int(s.n_done);
+    if (kOut || kRec) zc = P.el[i].z0 + double(s.n_done) * s.dz;
+    if (lost) return;
+    flight(float(s.snap), P);
+    if (kOut || kRec) zc = P.el[i].z1;
+    row_out();
+  }
+
+  __device__ void final_row(double* f, int64_t i, int64_t n) const {
+    const double vals[10] = {x, y, zc, vx, vy, vz, ax, ay, 0.0, t};
+    for (int k = 0; k < 10; ++k) f[size_t(k) * size_t(n) + size_t(i)] = vals[k];
+  }
+  __device__ void flush_last() {
+    if (kRec && !sink->last_written) sink->write(x, y, zc, vx, vy, vz, ax, ay, 0.0, t);
+  }
+
+  __device__ void store(const Queue& Q, unsigned s) const {
+    Q.x[s] = x; Q.y[s] = y; Q.vx[s] = vx; Q.vy[s] = vy; Q.vz[s] = vz; Q.t[s] = t;
+    Q.rows[s] = rows; Q.id[s] = id;
+    if (kOut) Q.margin[s] = margin;
+  }
+  __device__ void load(const Queue& Q, unsigned s, const Plan& P) {
+    x = Q.x[s]; y = Q.y[s]; vx = Q.vx[s]; vy = Q.vy[s]; vz = Q.vz[s]; t = Q.t[s];
+    rows = Q.rows[s]; id = Q.id[s];
+    inv_vz = __frcp_rn(vz);
+    ax = 0.0f;
+    ay = -P.gf;
+    margin = kOut ? float(Q.margin[s]) : INFINITY;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Element walk shared by both precisions (beamline.py:20-38).  Starts at
+// element `from`; returns the counter slot of the element the molecule was
+// lost on, kLabelDetected when it leaves the beamline, or kQueued when it
+// passed the entrance of the lens at element index *lens_at.
+// ---------------------------------------------------------------------------
+template <class M>
+__device__ int walk(M& m, const Plan& P, int from, int* lens_at) {
+  for (int i = from; i < P.n_el; ++i) {
+    const ctraj_element& e = P.el[i];
+    switch (e.type) {
+      case CTRAJ_CIRCULAR_APERTURE:
+        m.fly(P, i, 0);
+        if (m.circle_out(P, i)) return e.label;
+        m.fly(P, i, 1);
+        if (m.circle_out(P, i)) return e.label;
+        break;
+      case CTRAJ_RECTANGULAR_APERTURE:
+        m.fly(P, i, 0);
+        if (m.rect_out(P, i)) return e.label;
+        m.fly(P, i, 1);
+        if (m.rect_out(P, i)) return e.label;
+        break;
+      case CTRAJ_FIELD_PLATES:
+        m.fly(P, i, 0);
+        if (m.plates(P, i)) return e.label;
+        break;
+      case CTRAJ_ELECTROSTATIC_LENS:
+        m.fly(P, i, 0);
+        if (m.lens_entrance_out(P, i)) return e.label;
+        *lens_at = i;
+        return kQueued;
+      default:
+        return e.label;
+    }
+  }
+  return kLabelDetected;
+}
+
+}  // namespace ctraj

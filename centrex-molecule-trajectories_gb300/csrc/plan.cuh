@@ -1,0 +1,109 @@
+// Launch-time description of a beamline, shared by every kernel.
+//
+// The host builds one Plan per run from the ctraj_element table (kept
+// verbatim for the FP64 path) plus FP32 constants precomputed in double on the
+// host (plane-to-plane gaps, squared radii, table scale factors), and passes it
+// by value as a __grid_constant__ kernel parameter: every thread of a warp
+// reads the same element at the same time, so the constant cache broadcasts.
+#pragma once
+#include <cstdint>
+
+#include "ctraj.h"
+
+namespace ctraj {
+
+enum : int {
+  kForceStark2 = 0,  // W(E) table, |E| = alpha r^2
+  kForceStark1 = 1,  // W(E) table, |E| = alpha r
+  kForceRadial = 2,  // a(r) linear table
+};
+
+// FP32 constants of one element.
+struct ElemF {
+  float gap;   // (float)(z0 - z1 of the previous element); flight into this element
+  float len;   // (float)(z1 - z0)
+  float c[4];  // circle: (d/2)^2; rect: x1, x2, y1, y2; plates: x1, x2; lens: (d/2)^2
+};
+
+// FP32 constants of one lens (indexed by element).
+struct LensF {
+  const float4* q;  // per interval: stark (q0, q1, q2, 0) scaled by -kappa; radial (y_j, y_{j+1}-y_j, 0, 0)
+  float beta;       // table coordinate s = beta * r^n - s0 (stark) or r * beta (radial, beta = 1/h)
+  float s0;
+  float r_max;      // radial: last knot; lookups above it are errors
+  int n_int;        // intervals in the table
+  int n_smem;       // leading intervals staged in shared memory
+  int force;        // kForce*
+};
+
+// FP64 view of a force table (device pointers).
+struct TableD {
+  const double* knots;
+  const double* coef;    // (n-1) x 4
+  const double* values;  // n
+  double x0, h;          // first knot, uniform spacing
+  int n;
+  int kind;
+};
+
+struct Plan {
+  int n_el;
+  int n_labels;
+  int first_lens;  // index of the first lens element, n_el if none
+  int pad;
+  double g;
+  float gf;
+  float pad2;
+  ctraj_element el[CTRAJ_MAX_ELEMENTS];
+  ElemF ef[CTRAJ_MAX_ELEMENTS];
+  LensF lf[CTRAJ_MAX_ELEMENTS];
+  TableD td[CTRAJ_MAX_TABLES];
+};
+
+// Per-run device pointers and scalars.
+struct RunDev {
+  int64_t n;
+  uint64_t seed;
+  uint64_t offset;
+  int ic_mode;
+  int pad;
+  const double* ics;  // (6, n) when injected
+  ctraj_distribution xd, vd;
+  float gap0f;         // FP32 first flight for drawn ICs: (float)(el[0].z0 - xd.z)
+  float pad3;
+  int32_t* out_label;
+  double* out_final;   // (10, n)
+  int32_t* out_rows;
+  double* out_margin;
+  unsigned long long* counts;  // n_labels + 1
+  unsigned long long* stats;   // kStat*
+};
+
+enum : int {
+  kStatSteps = 0,
+  kStatLensSteps = 1,
+  kStatEdgeBand = 2,
+  kStatTableRange = 3,
+  kStatBadSteps = 4,
+  kStatRangeError = 5,
+  kStatCount = 8,
+};
+
+// Molecules waiting at a lens entrance (SoA, capacity n).  FP32 queues use the
+// float arrays, FP64 queues the double ones.
+struct Queue {
+  float *x, *y, *vx, *vy, *vz, *t;
+  double *dx, *dy, *dz, *dvx, *dvy, *dvz, *dt;
+  double* margin;
+  int32_t* rows;
+  int32_t* id;
+  unsigned int* count;  // entries written
+  unsigned int* head;   // entries taken
+};
+
+constexpr int kLabelDetected = -1;  // counts[n_labels]
+constexpr int kQueued = -2;         // waiting at a lens entrance
+constexpr int kNone = -3;           // no tally (inactive lane)
+constexpr float kEdgeBand = 1e-6f;  // molecules nearer than this to an edge are reported
+
+}  // namespace ctraj

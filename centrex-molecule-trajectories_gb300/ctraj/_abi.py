@@ -30,7 +30,7 @@ ESTATE = -7
 MAX_ELEMENTS = 64
 MAX_LABELS = 64
 MAX_TABLES = 8
-MAX_LENS_STEPS = 100_000_000
+MAX_LENS_STEPS = 10_000_000
 
 # element types
 CIRCULAR_APERTURE = 1
@@ -110,7 +110,7 @@ class RunArgs(ctypes.Structure):
         ("offset", ctypes.c_uint64),
         ("g", ctypes.c_double),
         ("out_mode", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("timing", ctypes.c_int32),
         ("out_label", ctypes.c_void_p),
         ("out_final", ctypes.c_void_p),
         ("out_rows", ctypes.c_void_p),
@@ -128,7 +128,9 @@ class RunStats(ctypes.Structure):
         ("table_range", ctypes.c_int64),
         ("bad_steps", ctypes.c_int64),
         ("kernels", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("timed", ctypes.c_int32),
+        ("front_ms", ctypes.c_float),
+        ("lens_ms", ctypes.c_float),
     ]
 
 

@@ -1,0 +1,91 @@
+"""Build libctraj.so with nvcc for sm_103a (GB300), in-tree.
+
+    python -m ctraj.build            # from centrex-molecule-trajectories_gb300/
+
+The library is a plain shared object with a C ABI (include/ctraj.h), linked
+against the static CUDA runtime, so it needs no PyTorch at build or load time.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG.parent / "csrc"
+INCLUDE = PKG.parent.parent / "include"
+OUT = PKG / "_lib" / "libctraj.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
+              "-Xptxas", "-warn-spills"]
+
+
+def sources():
+    return sorted(CSRC.glob("*.cu"))
+
+
+def headers():
+    return sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
+
+
+def nvcc() -> str:
+    exe = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(exe).exists():
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libctraj.so")
+    return exe
+
+
+def up_to_date() -> bool:
+    if not OUT.exists():
+        return False
+    t = OUT.stat().st_mtime
+    return all(p.stat().st_mtime <= t for p in sources() + headers() + [Path(__file__)])
+
+
+def build_library(force: bool = False, verbose: bool = False, extra: list[str] | None = None) -> Path:
+    if not force and up_to_date():
+        return OUT
+    OUT.parent.mkdir(parents=True, exist_ok=True)
+    tmp = OUT.with_name(OUT.name + f".tmp{os.getpid()}")
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, f"-I{INCLUDE}", f"-I{CSRC}", *(extra or []),
+           *map(str, sources()), "-o", str(tmp)]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    subprocess.run(cmd, check=True)
+    tmp.replace(OUT)
+    return OUT
+
+
+PEAK_SRC = CSRC / "peak" / "fp32_peak.cu"
+PEAK_OUT = PKG / "_lib" / "libctraj_peak.so"
+
+
+def build_peak_library(force: bool = False) -> Path:
+    """The FP32-throughput probe used by bench.py for the roofline denominator."""
+    if not force and PEAK_OUT.exists() and PEAK_OUT.stat().st_mtime >= PEAK_SRC.stat().st_mtime:
+        return PEAK_OUT
+    PEAK_OUT.parent.mkdir(parents=True, exist_ok=True)
+    tmp = PEAK_OUT.with_name(PEAK_OUT.name + f".tmp{os.getpid()}")
+    subprocess.run([nvcc(), *ARCH, "-O3", "-Xcompiler", "-fPIC", "-shared", str(PEAK_SRC), "-o", str(tmp)],
+                   check=True)
+    tmp.replace(PEAK_OUT)
+    return PEAK_OUT
+
+
+def build_all(force: bool = False) -> None:
+    """Both libraries, compiled in parallel."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    with ThreadPoolExecutor(2) as ex:
+        futs = [ex.submit(build_library, force), ex.submit(build_peak_library, force)]
+        for f in futs:
+            f.result()
+
+
+if __name__ == "__main__":
+    build_library(force="--force" in sys.argv, verbose=True,
+                  extra=["-Xptxas", "-v"] if "-v" in sys.argv else None)
+    build_peak_library(force="--force" in sys.argv)

@@ -1,0 +1,179 @@
+"""Thin ctypes layer over libctraj.so: one Engine = one ctraj_context.
+
+Every call maps a C status to the exception the reference would raise
+(``_abi.check``); ctypes releases the GIL for the duration of each call.
+There is no CPU fallback: a missing library raises on construction.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi
+from .compiler import CompiledBeamline
+
+G = 9.80665  # scipy.constants.g, the reference's gravity (molecule.py:15-16,58)
+
+
+@dataclass
+class RunResult:
+    counts: np.ndarray                # n_labels + 1 (last = "Detected")
+    labels: list                      # slot -> label string
+    molecules: int
+    molecule_steps: int
+    lens_steps: int
+    edge_band: int
+    table_range: int
+    kernels: int
+    label: np.ndarray | None = None   # per molecule counter slot (-1 = Detected)
+    final: np.ndarray | None = None   # (10, n) last row x, y, z, vx, vy, vz, ax, ay, az, t
+    rows: np.ndarray | None = None    # per molecule len(trajectory.t) - 1
+    margin: np.ndarray | None = None  # per molecule smallest edge distance (m)
+    extra: dict = field(default_factory=dict)
+
+    def counter_dict(self) -> dict:
+        names = list(self.labels) + ["Detected"]
+        out: dict = {}
+        for slot, c in enumerate(self.counts):
+            if c:
+                out[names[slot]] = out.get(names[slot], 0) + int(c)
+        return out
+
+    def label_names(self) -> list:
+        names = list(self.labels)
+        return [names[s] if s >= 0 else "Detected" for s in self.label]
+
+
+def _dev_ptr(t):
+    """Device pointer of a torch CUDA tensor (or an object exposing data_ptr)."""
+    return ctypes.c_void_p(int(t.data_ptr()))
+
+
+class Engine:
+    def __init__(self, device: int = 0):
+        self.lib = _abi.load_library()
+        self.ctx = ctypes.c_void_p()
+        _abi.check(self.lib.ctraj_create(int(device), ctypes.byref(self.ctx)), self.lib)
+        self.device = device
+        self._loaded = None
+        self._keep = None
+
+    def close(self):
+        if self.ctx:
+            self.lib.ctraj_destroy(self.ctx)
+            self.ctx = ctypes.c_void_p()
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: int | None):
+        _abi.check(self.lib.ctraj_set_stream(self.ctx, ctypes.c_void_p(stream_handle or 0)), self.lib)
+
+    def synchronize(self):
+        _abi.check(self.lib.ctraj_synchronize(self.ctx), self.lib)
+
+    def load(self, cb: CompiledBeamline):
+        """Upload a compiled beamline and its force tables (skipped when already loaded)."""
+        if self._loaded is cb:
+            return
+        for tid, t in enumerate(cb.tables):
+            st = t.as_struct()
+            _abi.check(self.lib.ctraj_set_force_table(self.ctx, tid, ctypes.byref(st)), self.lib)
+        _abi.check(self.lib.ctraj_set_beamline(self.ctx, cb.elements, cb.n_elements, len(cb.labels)),
+                   self.lib)
+        self._loaded = cb
+
+    def _args(self, n, precision, ics, xdist, vdist, seed, offset, g):
+        a = _abi.RunArgs()
+        a.n = int(n)
+        a.precision = int(precision)
+        a.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+        a.offset = int(offset) & 0xFFFFFFFFFFFFFFFF
+        a.g = float(g)
+        keep = []
+        if ics is None:
+            if xdist is None or vdist is None:
+                raise ValueError("either ics or both device distributions are required")
+            a.ic_mode = _abi.IC_DEVICE_DRAW
+            a.xdist = xdist
+            a.vdist = vdist
+        elif isinstance(ics, np.ndarray):
+            arr = np.ascontiguousarray(ics, dtype=np.float64)
+            if arr.shape != (6, n):
+                raise ValueError(f"ics must have shape (6, {n}), got {arr.shape}")
+            keep.append(arr)
+            a.ic_mode = _abi.IC_HOST
+            a.ics = arr.ctypes.data
+        else:  # torch CUDA tensor (6, n) float64, contiguous
+            if tuple(ics.shape) != (6, n) or not ics.is_contiguous() or str(ics.dtype) != "torch.float64":
+                raise ValueError("device ics must be a contiguous (6, n) float64 tensor")
+            keep.append(ics)
+            a.ic_mode = _abi.IC_DEVICE
+            a.ics = int(ics.data_ptr())
+        return a, keep
+
+    def run(self, cb: CompiledBeamline, n: int, precision: int = 32, ics=None, xdist=None,
+            vdist=None, seed: int = 0, offset: int = 0, g: float = G, outputs: bool = False,
+            device_outputs: dict | None = None, timing: bool = False) -> RunResult:
+        self.load(cb)
+        a, keep = self._args(n, precision, ics, xdist, vdist, seed, offset, g)
+        a.timing = 1 if timing else 0
+        nl = len(cb.labels)
+        counts = np.zeros(nl + 1, np.int64)
+        a.counts = counts.ctypes.data
+        res_extra = {}
+        label = final = rows = margin = None
+        if device_outputs is not None:
+            a.out_mode = _abi.OUT_DEVICE
+            for k in ("label", "final", "rows", "margin"):
+                if k in device_outputs:
+                    setattr(a, f"out_{k}", int(device_outputs[k].data_ptr()))
+        elif outputs:
+            a.out_mode = _abi.OUT_HOST
+            label = np.empty(n, np.int32)
+            final = np.empty((10, n), np.float64)
+            rows = np.empty(n, np.int32)
+            margin = np.empty(n, np.float64)
+            a.out_label, a.out_final = label.ctypes.data, final.ctypes.data
+            a.out_rows, a.out_margin = rows.ctypes.data, margin.ctypes.data
+        st = _abi.RunStats()
+        status = self.lib.ctraj_run(self.ctx, ctypes.byref(a), ctypes.byref(st))
+        del keep
+        _abi.check(status, self.lib)
+        if st.timed:
+            res_extra.update(front_ms=float(st.front_ms), lens_ms=float(st.lens_ms))
+        return RunResult(counts=counts, labels=list(cb.labels), molecules=st.molecules,
+                         molecule_steps=st.molecule_steps, lens_steps=st.lens_steps,
+                         edge_band=st.edge_band, table_range=st.table_range, kernels=st.kernels,
+                         label=label, final=final, rows=rows, margin=margin, extra=res_extra)
+
+    def record(self, cb: CompiledBeamline, n: int, ids, stride: int = 1, max_rows: int = 64,
+               precision: int = 32, ics=None, xdist=None, vdist=None, seed: int = 0,
+               offset: int = 0, g: float = G):
+        """Replay molecules `ids` of a run and return their rows: list of (k_i, 10) arrays."""
+        self.load(cb)
+        a, keep = self._args(n, precision, ics, xdist, vdist, seed, offset, g)
+        counts = np.zeros(len(cb.labels) + 1, np.int64)
+        a.counts = counts.ctypes.data
+        ids = np.ascontiguousarray(ids, dtype=np.int64)
+        out = np.empty((ids.size, max_rows, 10), np.float64)
+        cnt = np.zeros(ids.size, np.int32)
+        status = self.lib.ctraj_record(self.ctx, ctypes.byref(a), ids.ctypes.data, ids.size,
+                                       int(stride), int(max_rows), out.ctypes.data, cnt.ctypes.data)
+        del keep
+        _abi.check(status, self.lib)
+        return [out[k, :cnt[k]].copy() for k in range(ids.size)]
+
+
+_default: dict[int, Engine] = {}
+
+
+def default_engine(device: int = 0) -> Engine:
+    if device not in _default:
+        _default[device] = Engine(device)
+    return _default[device]

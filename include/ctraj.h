@@ -55,7 +55,7 @@ enum {
 #define CTRAJ_MAX_ELEMENTS 64
 #define CTRAJ_MAX_LABELS 64
 #define CTRAJ_MAX_TABLES 8
-#define CTRAJ_MAX_LENS_STEPS 100000000LL
+#define CTRAJ_MAX_LENS_STEPS 10000000LL
 
 /* ---- beamline elements ---------------------------------------------------- */
 enum {
@@ -178,7 +178,7 @@ typedef struct ctraj_run_args {
   uint64_t offset;
   double g;
   int32_t out_mode;
-  int32_t reserved;
+  int32_t timing;           /* nonzero: time the kernels with CUDA events (stats) */
   int32_t* out_label;
   double* out_final;
   int32_t* out_rows;
@@ -194,7 +194,9 @@ typedef struct ctraj_run_stats {
   int64_t table_range;      /* lookups outside a table's knots                */
   int64_t bad_steps;        /* molecules with a non-finite lens step count    */
   int32_t kernels;          /* kernel launches issued by this run             */
-  int32_t reserved;
+  int32_t timed;            /* 1 when the *_ms fields below were measured     */
+  float front_ms;           /* CUDA-event time of the ballistic front kernel  */
+  float lens_ms;            /* CUDA-event time of all lens kernels            */
 } ctraj_run_stats;
 
 /* ---- context -------------------------------------------------------------- */

@@ -284,7 +284,7 @@ static void lens(mol_t* m, const beam_t* b, const ctraj_element* e, int* range_c
   const double L = e->p[7];
   double dz = e->step_mode == CTRAJ_STEP_DT ? m->s.v[2] * e->p[2] : e->p[1];
   const double nf = rint(L / dz);
-  if (!isfinite(nf) || nf > (double)CTRAJ_MAX_LENS_STEPS) {
+  if (!isfinite(nf) || fabs(nf) > (double)CTRAJ_MAX_LENS_STEPS) {
     m->err = CTRAJ_ESTEPS;
     kill(m, e->label_inside);
     return;

@@ -1,0 +1,81 @@
+"""C ABI checks that need no GPU: the library loads, exports every function
+declared in include/ctraj.h, and the ctypes structs match the C layout."""
+import ctypes
+import re
+import subprocess
+import tempfile
+from pathlib import Path
+
+import pytest
+
+from ctraj import _abi
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "ctraj.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*|int64_t)\s+(ctraj_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_header_functions_are_bound():
+    names = declared_functions()
+    assert "ctraj_run" in names and "ctraj_create" in names
+    assert set(names) == set(_abi.SIGNATURES), set(names) ^ set(_abi.SIGNATURES)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from ctraj.build import build_library
+
+    build_library()
+    return ctypes.CDLL(str(_abi.LIB_PATH))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+    out = subprocess.run(["nm", "-D", "--defined-only", str(_abi.LIB_PATH)], capture_output=True,
+                         text=True).stdout
+    exported = set(re.findall(r"\b(ctraj_\w+)\b", out))
+    assert set(declared_functions()) <= exported
+
+
+def test_version_and_error_without_gpu(lib):
+    lib.ctraj_version.restype = ctypes.c_int
+    assert lib.ctraj_version() == _abi.ABI_VERSION
+    lib.ctraj_last_error.restype = ctypes.c_char_p
+    assert isinstance(lib.ctraj_last_error(), bytes)
+
+
+def test_struct_layout_matches_header():
+    src = r"""
+    #include <stdio.h>
+    #include <stddef.h>
+    #include "ctraj.h"
+    int main(void) {
+      printf("%zu %zu %zu %zu %zu\n", sizeof(ctraj_element), sizeof(ctraj_force_table),
+             sizeof(ctraj_distribution), sizeof(ctraj_run_args), sizeof(ctraj_run_stats));
+      printf("%zu %zu %zu %zu\n", offsetof(ctraj_element, z0), offsetof(ctraj_element, p),
+             offsetof(ctraj_run_args, g), offsetof(ctraj_run_args, counts));
+      return 0;
+    }
+    """
+    with tempfile.TemporaryDirectory() as d:
+        c = Path(d) / "s.c"
+        c.write_text(src)
+        exe = Path(d) / "s"
+        subprocess.run(["gcc", f"-I{ROOT / 'include'}", str(c), "-o", str(exe)], check=True)
+        sizes, offs = subprocess.run([str(exe)], capture_output=True, text=True).stdout.split("\n")[:2]
+    assert list(map(int, sizes.split())) == [ctypes.sizeof(_abi.Element), ctypes.sizeof(_abi.ForceTable),
+                                            ctypes.sizeof(_abi.Distribution), ctypes.sizeof(_abi.RunArgs),
+                                            ctypes.sizeof(_abi.RunStats)]
+    assert list(map(int, offs.split())) == [_abi.Element.z0.offset, _abi.Element.p.offset,
+                                           _abi.RunArgs.g.offset, _abi.RunArgs.counts.offset]
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    with pytest.raises(RuntimeError, match="not built"):
+        _abi.load_library(tmp_path / "nope.so")

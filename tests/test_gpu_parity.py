@@ -1,0 +1,225 @@
+"""CUDA path against the oracle and the reference's golden outputs.
+
+FP64 runs follow the reference's float64 operation order and must match the
+reference fixtures exactly (labels, row counts, final rows).  FP32 runs must
+give the same label for every molecule farther than 1 um from an edge (as
+measured by the FP64 oracle) and final positions within 1 um of the FP64
+result (tolerance written below).
+"""
+import numpy as np
+import pytest
+
+import fixtures
+from ctraj.compiler import compile_beamline
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+POS_TOL = 1e-6     # m, final position FP32 vs FP64
+VEL_TOL = 1e-4     # m/s, final velocity FP32 vs FP64
+TIME_TOL = 1e-8    # s
+
+
+@pytest.fixture(scope="module")
+def engine():
+    from ctraj.engine import Engine
+
+    e = Engine(0)
+    yield e
+    e.close()
+
+
+CASES = fixtures.available()
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_fp64_matches_reference_exactly(engine, case):
+    fx = fixtures.load(case)
+    cb = compile_beamline(fixtures.build_beamline(fx))
+    n = fx["ics"].shape[1]
+    r = engine.run(cb, n, precision=64, ics=fx["ics"], outputs=True)
+    assert r.label_names() == fixtures.expected_labels(fx)
+    np.testing.assert_array_equal(r.rows, fx["rows"])
+    both = np.isfinite(r.final).all(0) & np.isfinite(fx["final"]).all(0)
+    np.testing.assert_array_equal(r.final[:, both], fx["final"][:, both])
+    assert r.molecule_steps == int(fx["rows"].sum())
+    o = oracle.run(cb, fx["ics"])
+    np.testing.assert_array_equal(r.counts, o["counts"])
+    np.testing.assert_array_equal(r.margin, o["margin"])
+    assert r.edge_band == o["edge_band"]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_fp32_within_tolerance(engine, case):
+    fx = fixtures.load(case)
+    cb = compile_beamline(fixtures.build_beamline(fx))
+    n = fx["ics"].shape[1]
+    o = oracle.run(cb, fx["ics"])
+    r = engine.run(cb, n, precision=32, ics=fx["ics"], outputs=True)
+    far = o["margin"] >= 1e-6
+    assert np.array_equal(r.label[far], o["label"][far])
+    same = (r.label == o["label"]) & np.isfinite(o["final"]).all(0) & far
+    # molecules of the lens beamline travel ~3 m; positions within 1 um
+    dpos = np.abs(r.final[0:2, same] - o["final"][0:2, same])
+    assert dpos.max(initial=0) < POS_TOL, dpos.max(initial=0)
+    np.testing.assert_allclose(r.final[2, same], o["final"][2, same], atol=POS_TOL, rtol=0)
+    dvel = np.abs(r.final[3:6, same] - o["final"][3:6, same])
+    assert dvel.max(initial=0) < VEL_TOL, dvel.max(initial=0)
+    np.testing.assert_allclose(r.final[9, same], o["final"][9, same], atol=TIME_TOL, rtol=0)
+    # row counts agree except where rint(L/dz) sits on a rounding tie of vz
+    assert np.mean(r.rows[same] == o["rows"][same]) > 0.999
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c in ("config0", "config1", "example_lens", "kat_lens")])
+def test_record_traces_match_reference(engine, case):
+    fx = fixtures.load(case)
+    cb = compile_beamline(fixtures.build_beamline(fx))
+    n = fx["ics"].shape[1]
+    tr = fixtures.traces(fx)
+    ids = np.array(sorted(tr), dtype=np.int64)
+    max_rows = max(t[2] for t in tr.values()) + 2
+    rows64 = engine.record(cb, n, ids, stride=1, max_rows=max_rows, precision=64, ics=fx["ics"])
+    rows32 = engine.record(cb, n, ids, stride=1, max_rows=max_rows, precision=32, ics=fx["ics"])
+    for j, r64, r32 in zip(ids, rows64, rows32):
+        ref, idx, full = tr[j]
+        assert r64.shape[0] == full
+        np.testing.assert_array_equal(r64 if idx is None else r64[idx], ref)
+        if r32.shape[0] == full:
+            d = np.abs((r32 if idx is None else r32[idx])[:, 0:2] - ref[:, 0:2])
+            assert np.nanmax(d) < POS_TOL
+
+
+def test_record_stride_keeps_last_row(engine):
+    fx = fixtures.load("config1")
+    cb = compile_beamline(fixtures.build_beamline(fx))
+    n = fx["ics"].shape[1]
+    j = max(fixtures.traces(fx), key=lambda k: fixtures.traces(fx)[k][2])
+    full = engine.record(cb, n, [j], stride=1, max_rows=5000, precision=64, ics=fx["ics"])[0]
+    sub = engine.record(cb, n, [j], stride=50, max_rows=200, precision=64, ics=fx["ics"])[0]
+    expect = list(range(0, full.shape[0], 50))
+    if expect[-1] != full.shape[0] - 1:
+        expect.append(full.shape[0] - 1)
+    np.testing.assert_array_equal(sub, full[expect])
+
+
+def test_record_overflow_is_reported(engine):
+    fx = fixtures.load("config1")
+    cb = compile_beamline(fixtures.build_beamline(fx))
+    n = fx["ics"].shape[1]
+    j = max(fixtures.traces(fx), key=lambda k: fixtures.traces(fx)[k][2])
+    from ctraj._abi import CtrajError
+
+    with pytest.raises(CtrajError):
+        engine.record(cb, n, [j], stride=1, max_rows=5, precision=64, ics=fx["ics"])
+
+
+def test_device_draw_fp32_vs_fp64(engine):
+    """Same Philox stream drawn in both precisions: the FP32 run must agree with
+    the FP64 run molecule by molecule (labels off the 1 um band, positions)."""
+    import ctraj
+    from ctraj.distributions import device_spec
+
+    fx = fixtures.load("config1")
+    cb = compile_beamline(fixtures.build_beamline(fx))
+    xd = device_spec(ctraj.GaussianPositionDistribution(1.5e-3, 1.5e-3, 0.0), "position")
+    vd = device_spec(ctraj.CeNTREXVelocityDistribution(sigmax=20.0, sigmay=20.0), "velocity")
+    n = 400_000
+    r64 = engine.run(cb, n, precision=64, xdist=xd, vdist=vd, seed=7, offset=123, outputs=True)
+    r32 = engine.run(cb, n, precision=32, xdist=xd, vdist=vd, seed=7, offset=123, outputs=True)
+    far = r64.margin >= 1e-6
+    assert np.array_equal(r32.label[far], r64.label[far])
+    same = (r32.label == r64.label) & far
+    d = np.abs(r32.final[0:2, same] - r64.final[0:2, same]).max()
+    assert d < POS_TOL, d
+    assert r64.molecule_steps > n
+
+
+def test_device_draw_statistics(engine):
+    """ICs drawn on the device follow the distributions (a zero-length plane at
+    the source leaves every molecule at its initial state)."""
+    import ctraj
+    from ctraj.distributions import device_spec
+
+    bl = ctraj.Beamline([ctraj.CircularAperture(name="src", z0=0.25, L=0.0, d=float("inf"))])
+    cb = compile_beamline(bl)
+    n = 1_000_000
+    for prec in (32, 64):
+        for xdist in (ctraj.GaussianPositionDistribution(1.5e-3, 2.5e-3, 0.25),
+                      ctraj.CeNTREXPositionDistribution(d=0.02, z=0.25)):
+            vdist = ctraj.CeNTREXVelocityDistribution(vx=1.0, sigmax=20.0, vy=-2.0, sigmay=30.0)
+            r = engine.run(cb, n, precision=prec, xdist=device_spec(xdist, "position"),
+                           vdist=device_spec(vdist, "velocity"), seed=3, outputs=True)
+            f = r.final
+            assert np.all(f[2] == 0.25)
+            for row, mu, sd in ((3, 1.0, 20.0), (4, -2.0, 30.0), (5, 184.0, 16.0)):
+                assert abs(f[row].mean() - mu) < 5 * sd / np.sqrt(n)
+                assert abs(f[row].std() / sd - 1) < 5 / np.sqrt(2 * n)
+            if isinstance(xdist, ctraj.GaussianPositionDistribution):
+                assert abs(f[0].std() / 1.5e-3 - 1) < 5 / np.sqrt(2 * n)
+                assert abs(f[1].std() / 2.5e-3 - 1) < 5 / np.sqrt(2 * n)
+            else:
+                rr = np.hypot(f[0], f[1])
+                assert rr.max() <= 0.01 * (1 + 1e-6)
+                # uniform disc: P(r < R/2) = 1/4
+                assert abs(np.mean(rr < 0.005) - 0.25) < 5 * np.sqrt(0.25 * 0.75 / n)
+            # molecules get distinct draws (FP32 rounding merges ~1 % near the mode)
+            assert np.unique(f[3]).size > 0.95 * n
+
+
+def test_seeded_large_run_matches_oracle(engine):
+    """1e5 seeded molecules of the lens beamline: FP64 GPU == oracle exactly."""
+    import ctraj
+    from ctraj.distributions import host_draw
+
+    fx = fixtures.load("config1")
+    cb = compile_beamline(fixtures.build_beamline(fx))
+    ics = host_draw(ctraj.GaussianPositionDistribution(1.5e-3, 1.5e-3, 0.0),
+                    ctraj.CeNTREXVelocityDistribution(sigmax=20.0, sigmay=20.0), 100_000, seed=0)
+    o = oracle.run(cb, ics, threads=8)
+    r = engine.run(cb, ics.shape[1], precision=64, ics=ics, outputs=True)
+    np.testing.assert_array_equal(r.label, o["label"])
+    np.testing.assert_array_equal(r.final, o["final"])
+    assert r.molecule_steps == o["steps"]
+    assert r.lens_steps == o["lens_steps"]
+
+
+def test_run_is_deterministic_and_offsets_partition(engine):
+    """Counts of a run equal the sum over disjoint offset ranges (replica sharding)."""
+    import ctraj
+    from ctraj.distributions import device_spec
+
+    fx = fixtures.load("config1")
+    cb = compile_beamline(fixtures.build_beamline(fx))
+    xd = device_spec(ctraj.GaussianPositionDistribution(1.5e-3, 1.5e-3, 0.0), "position")
+    vd = device_spec(ctraj.CeNTREXVelocityDistribution(sigmax=20.0, sigmay=20.0), "velocity")
+    full = engine.run(cb, 300_000, xdist=xd, vdist=vd, seed=11)
+    again = engine.run(cb, 300_000, xdist=xd, vdist=vd, seed=11)
+    np.testing.assert_array_equal(full.counts, again.counts)
+    assert full.molecule_steps == again.molecule_steps
+    parts = [engine.run(cb, 100_000, xdist=xd, vdist=vd, seed=11, offset=k * 100_000) for k in range(3)]
+    np.testing.assert_array_equal(sum(p.counts for p in parts), full.counts)
+    assert sum(p.molecule_steps for p in parts) == full.molecule_steps
+
+
+def test_radial_table_range_error_raises(engine):
+    import ctraj
+    from scipy.interpolate import interp1d
+
+    r = np.linspace(0, 0.0101, 50)
+    lens = ctraj.ElectrostaticLens(name="L", z0=0.1, L=0.3, d=0.02, dz=5e-3, a_interp=interp1d(r, -1e5 * r))
+    cb = compile_beamline(ctraj.Beamline([lens]))
+    ics = np.array([[9.9e-3], [0.0], [0.1], [200.0], [0.0], [184.0]])
+    for prec in (32, 64):
+        with pytest.raises(ValueError):
+            engine.run(cb, 1, precision=prec, ics=ics)
+
+
+def test_empty_and_tiny_runs(engine):
+    fx = fixtures.load("config0")
+    cb = compile_beamline(fixtures.build_beamline(fx))
+    r = engine.run(cb, 0, precision=32, ics=np.zeros((6, 0)))
+    assert r.counts.sum() == 0 and r.molecule_steps == 0
+    for n in (1, 31, 33):
+        ics = np.ascontiguousarray(fx["ics"][:, :n])
+        r = engine.run(cb, n, precision=64, ics=ics, outputs=True)
+        assert r.label_names() == fixtures.expected_labels(fx)[:n]
