@@ -17,8 +17,10 @@
 // and the force is a_perp = w(|r|) * (x, y) - g y^, w read from a per-interval
 // polynomial table.  The RK4 combination is rewritten exactly:
 //   x' = x + dt v + dt^2/6 (l1 + l2 + l3),  v' = v + dt/6 (l1 + 2 l2 + 2 l3 + l4)
-// (the reference's k1..k4 substituted), and the step count, step size and
-// exit-snap time are computed once per molecule in double.
+// (the reference's k1..k4 substituted); each increment is formed in full
+// precision and added with a carried rounding error (compensated summation),
+// and the step count, step size and exit-snap time are computed once per
+// molecule in double.
 #pragma once
 #include <cfloat>
 #include <cmath>
@@ -390,8 +392,18 @@ struct Mol32 {
   int32_t id;
   double zc;      // current z, kept only for outputs / recording
   float ax, ay;   // stored acceleration (recording)
+  float cx, cy, cvx, cvy;  // rounding errors carried by the lens integration
   double t0;      // time at the lens entrance
   RowSink* sink;
+
+  // s += inc with the rounding error carried in c (Fast2Sum: |s| >= |inc + c|
+  // holds because one step changes x and v by far less than their size)
+  __device__ __forceinline__ static void accumulate(float& s, float& c, float inc) {
+    const float d = __fadd_rn(inc, c);
+    const float t = __fadd_rn(s, d);
+    c = __fadd_rn(d, -__fadd_rn(t, -s));
+    s = t;
+  }
 
   __device__ void row_out() {
     if (kRec) sink->put(x, y, zc, vx, vy, vz, ax, ay, 0.0, t);
@@ -522,10 +534,13 @@ struct Mol32 {
     const float l4x = __fmul_rn(w4, p4x), l4y = __fmaf_rn(w4, p4y, -g);
     const float sx = __fadd_rn(__fadd_rn(l1x, l2x), l3x);
     const float sy = __fadd_rn(__fadd_rn(l1y, l2y), l3y);
-    x = __fmaf_rn(dt26, sx, __fmaf_rn(dt, vx, x));
-    y = __fmaf_rn(dt26, sy, __fmaf_rn(dt, vy, y));
-    vx = __fmaf_rn(dt6, __fmaf_rn(2.0f, __fadd_rn(l2x, l3x), __fadd_rn(l1x, l4x)), vx);
-    vy = __fmaf_rn(dt6, __fmaf_rn(2.0f, __fadd_rn(l2y, l3y), __fadd_rn(l1y, l4y)), vy);
+    // increments are formed in full precision, then added once with the
+    // carried rounding error (the lens defocuses, so uncompensated rounding of
+    // x and v grows to micrometres at the detector)
+    accumulate(x, cx, __fmaf_rn(dt26, sx, __fmul_rn(dt, vx)));
+    accumulate(y, cy, __fmaf_rn(dt26, sy, __fmul_rn(dt, vy)));
+    accumulate(vx, cvx, __fmul_rn(dt6, __fmaf_rn(2.0f, __fadd_rn(l2x, l3x), __fadd_rn(l1x, l4x))));
+    accumulate(vy, cvy, __fmul_rn(dt6, __fmaf_rn(2.0f, __fadd_rn(l2y, l3y), __fadd_rn(l1y, l4y))));
     ax = l1x;
     ay = l1y;
     const float r2 = __fmaf_rn(y, y, __fmul_rn(x, x));
@@ -535,7 +550,10 @@ struct Mol32 {
 
   // Inside the lens t and z follow from the step count (t0 + n dt, z0 + n dz)
   // instead of being accumulated in float.
-  __device__ void lens_begin(const Plan&, int, const LensStep&) { t0 = double(t); }
+  __device__ void lens_begin(const Plan&, int, const LensStep&) {
+    t0 = double(t);
+    cx = cy = cvx = cvy = 0.0f;
+  }
   __device__ void lens_row(const Plan& P, int i, const LensStep& s) {
     if (kRec) {
       zc = P.el[i].z0 + double(s.n_done) * s.dz;
@@ -547,6 +565,10 @@ struct Mol32 {
   __device__ void lens_end(const Plan& P, int i, const LensStep& s, bool lost) {
     t = float(t0 + double(s.n_done) * s.dt);
     rows += int(s.n_done);
+    x = __fadd_rn(x, cx);
+    y = __fadd_rn(y, cy);
+    vx = __fadd_rn(vx, cvx);
+    vy = __fadd_rn(vy, cvy);
     if (kOut || kRec) zc = P.el[i].z0 + double(s.n_done) * s.dz;
     if (lost) return;
     flight(float(s.snap), P);
