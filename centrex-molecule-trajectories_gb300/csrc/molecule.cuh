@@ -216,9 +216,9 @@ struct Mol64 {
     if (R.ic_mode == CTRAJ_IC_DEVICE_DRAW) {
       const Words8 w = molecule_words(R.offset + uint64_t(i), R.seed);
       double n0, n1, n2, n3, n4, n5;
-      box_muller(u01d(w.w[0]), u01d(w.w[1]), n0, n1);
-      box_muller(u01d(w.w[2]), u01d(w.w[3]), n2, n3);
-      box_muller(u01d(w.w[4]), u01d(w.w[5]), n4, n5);
+      box_muller(w.w[0], w.w[1], n0, n1);
+      box_muller(w.w[2], w.w[3], n2, n3);
+      box_muller(w.w[4], w.w[5], n4, n5);
       const double* vp = R.vd.p;
       v[0] = __fma_rn(vp[1], n0, vp[0]);
       v[1] = __fma_rn(vp[3], n1, vp[2]);
@@ -417,9 +417,9 @@ struct Mol32 {
     if (R.ic_mode == CTRAJ_IC_DEVICE_DRAW) {
       const Words8 w = molecule_words(R.offset + uint64_t(i), R.seed);
       float n0, n1, n2, n3, n4, n5;
-      box_muller(u01f(w.w[0]), u01f(w.w[1]), n0, n1);
-      box_muller(u01f(w.w[2]), u01f(w.w[3]), n2, n3);
-      box_muller(u01f(w.w[4]), u01f(w.w[5]), n4, n5);
+      box_muller(w.w[0], w.w[1], n0, n1);
+      box_muller(w.w[2], w.w[3], n2, n3);
+      box_muller(w.w[4], w.w[5], n4, n5);
       const double* vp = R.vd.p;
       vx = __fmaf_rn(float(vp[1]), n0, float(vp[0]));
       vy = __fmaf_rn(float(vp[3]), n1, float(vp[2]));

@@ -56,20 +56,32 @@ __device__ __forceinline__ double u01d(uint32_t w) {
   return __fma_rn(double(w), 2.3283064365386963e-10, 1.1641532182693481e-10);
 }
 
-__device__ __forceinline__ void box_muller(float u1, float u2, float& a, float& b) {
-  const float r = sqrtf(-2.0f * logf(u1));
-  float s, c;
-  sincospif(2.0f * u2, &s, &c);
-  a = r * c;
-  b = r * s;
+// ln U for U = (w + 1/2) 2^-32.  Above one half, U is close to 1 and a float
+// holds it only to 2^-25 absolute, which would make the Box-Muller radius
+// sqrt(-2 ln U) inaccurate near zero; there ln U = log1p(-V) with
+// V = 1 - U = (~w + 1/2) 2^-32 formed exactly from the integer.
+__device__ __forceinline__ float log_u01f(uint32_t w) {
+  return (w < 0x80000000u) ? logf(u01f(w)) : log1pf(-u01f(~w));
 }
 
-__device__ __forceinline__ void box_muller(double u1, double u2, double& a, double& b) {
-  const double r = sqrt(-2.0 * log(u1));
+__device__ __forceinline__ double log_u01d(uint32_t w) {
+  return (w < 0x80000000u) ? log(u01d(w)) : log1p(-u01d(~w));
+}
+
+__device__ __forceinline__ void box_muller(uint32_t w1, uint32_t w2, float& a, float& b) {
+  const float r = sqrtf(__fmul_rn(-2.0f, log_u01f(w1)));
+  float s, c;
+  sincospif(__fmul_rn(2.0f, u01f(w2)), &s, &c);
+  a = __fmul_rn(r, c);
+  b = __fmul_rn(r, s);
+}
+
+__device__ __forceinline__ void box_muller(uint32_t w1, uint32_t w2, double& a, double& b) {
+  const double r = sqrt(__dmul_rn(-2.0, log_u01d(w1)));
   double s, c;
-  sincospi(2.0 * u2, &s, &c);
-  a = r * c;
-  b = r * s;
+  sincospi(__dmul_rn(2.0, u01d(w2)), &s, &c);
+  a = __dmul_rn(r, c);
+  b = __dmul_rn(r, s);
 }
 
 // The eight words of two Philox calls and how they are used:

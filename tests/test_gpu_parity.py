@@ -62,7 +62,14 @@ def test_fp32_within_tolerance(engine, case):
     # molecules of the lens beamline travel ~3 m; positions within 1 um
     dpos = np.abs(r.final[0:2, same] - o["final"][0:2, same])
     assert dpos.max(initial=0) < POS_TOL, dpos.max(initial=0)
-    np.testing.assert_allclose(r.final[2, same], o["final"][2, same], atol=POS_TOL, rtol=0)
+    # z of a field-plate hit is (x_plate - x) / vx * vz: an error dx in x
+    # becomes dx * |vz / vx| in z at grazing incidence, so z is checked to
+    # POS_TOL there scaled by that factor
+    plates = np.array([cb.label_of(s) in {e.name for e in fixtures.build_beamline(fx).elements
+                                           if type(e).__name__ == "FieldPlates"} for s in o["label"]])
+    ztol = np.where(plates, POS_TOL * np.maximum(1.0, np.abs(o["final"][5] / o["final"][3])), POS_TOL)
+    dz = np.abs(r.final[2] - o["final"][2])
+    assert np.all(dz[same] <= ztol[same]), dz[same].max()
     dvel = np.abs(r.final[3:6, same] - o["final"][3:6, same])
     assert dvel.max(initial=0) < VEL_TOL, dvel.max(initial=0)
     np.testing.assert_allclose(r.final[9, same], o["final"][9, same], atol=TIME_TOL, rtol=0)
@@ -93,8 +100,11 @@ def test_record_stride_keeps_last_row(engine):
     fx = fixtures.load("config1")
     cb = compile_beamline(fixtures.build_beamline(fx))
     n = fx["ics"].shape[1]
-    j = max(fixtures.traces(fx), key=lambda k: fixtures.traces(fx)[k][2])
+    j = int(np.argmax(fx["rows"]))  # the longest-lived molecule (a lens survivor)
+    assert fx["rows"][j] > 3000
     full = engine.record(cb, n, [j], stride=1, max_rows=5000, precision=64, ics=fx["ics"])[0]
+    assert full.shape[0] == fx["rows"][j] + 1
+    np.testing.assert_array_equal(full[-1], fx["final"][:, j])
     sub = engine.record(cb, n, [j], stride=50, max_rows=200, precision=64, ics=fx["ics"])[0]
     expect = list(range(0, full.shape[0], 50))
     if expect[-1] != full.shape[0] - 1:
@@ -106,7 +116,7 @@ def test_record_overflow_is_reported(engine):
     fx = fixtures.load("config1")
     cb = compile_beamline(fixtures.build_beamline(fx))
     n = fx["ics"].shape[1]
-    j = max(fixtures.traces(fx), key=lambda k: fixtures.traces(fx)[k][2])
+    j = int(np.argmax(fx["rows"]))
     from ctraj._abi import CtrajError
 
     with pytest.raises(CtrajError):
