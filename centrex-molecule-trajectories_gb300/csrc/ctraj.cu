@@ -2,10 +2,10 @@
 //
 // A context owns one CUDA stream (or borrows the caller's), the device copies
 // of the beamline's force tables, the FP32 lens tables derived from them, and
-// grow-only work buffers (survivor queues, injected initial conditions,
-// per-molecule outputs).  ctraj_run enqueues k_front and one k_lens per lens
-// and copies the per-label counts back; nothing is allocated on a repeated
-// run of the same or a smaller size.
+// grow-only work buffers (lens queues, injected initial conditions,
+// per-molecule outputs).  ctraj_run enqueues k_front and the chunked lens
+// kernels and copies the per-label counts back; nothing is allocated on a
+// repeated run of the same or a smaller size.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -94,14 +94,16 @@ struct ctraj_context {
   bool lens_tables_dirty = true;
   std::vector<size_t> lens_offset;
   std::vector<int> lens_n_int, lens_n_smem;
-  DevBuf queue[2];
-  DevBuf qctl;                  // queue counters (4 x unsigned) + counts + stats
+  DevBuf queue[3];              // lens queues: current chunk, continuation, next lens
+  DevBuf qctl;                  // queue counters (2 x unsigned per queue) + counts + stats
   DevBuf ics;
   DevBuf outs;
   DevBuf rec_rows, rec_ids, rec_count;
-  int refill = 16;
+  unsigned* host_max = nullptr; // pinned: largest remaining lens step count of a queue
+  int chunk = 128;              // RK4 steps per lens chunk (compaction interval)
   bool timing = false;
-  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // before front, after front, after lenses
+  // before front, after front, before the first lens chunk, after the last one
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 namespace ctraj {
@@ -109,42 +111,37 @@ namespace {
 
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
-// Queue layout inside one buffer of capacity cap.
-Queue make_queue(const DevBuf& b, size_t cap, int precision, unsigned* ctl) {
-  Queue q{};
+// Queue layout inside one buffer of capacity cap (SoA, each array 256-byte
+// aligned so a warp's 32 consecutive entries are whole 128-byte lines).
+// Returns the bytes used; with b == nullptr only sizes the layout.
+size_t layout_queue(const DevBuf* b, size_t cap, int precision, unsigned* ctl, Queue* q) {
+  Queue tmp{};
   size_t off = 0;
   auto take = [&](size_t bytes) {
     size_t o = off;
     off += align256(bytes);
     return o;
   };
+  auto f = [&](float** p) { size_t o = take(cap * 4); if (b) *p = b->as<float>(o); };
+  auto d = [&](double** p) { size_t o = take(cap * 8); if (b) *p = b->as<double>(o); };
+  auto i = [&](int32_t** p) { size_t o = take(cap * 4); if (b) *p = b->as<int32_t>(o); };
   if (precision == 32) {
-    q.x = b.as<float>(take(cap * 4));
-    q.y = b.as<float>(take(cap * 4));
-    q.vx = b.as<float>(take(cap * 4));
-    q.vy = b.as<float>(take(cap * 4));
-    q.vz = b.as<float>(take(cap * 4));
-    q.t = b.as<float>(take(cap * 4));
+    f(&tmp.x); f(&tmp.y); f(&tmp.vx); f(&tmp.vy); f(&tmp.vz); f(&tmp.t);
+    f(&tmp.cx); f(&tmp.cy); f(&tmp.cvx); f(&tmp.cvy); f(&tmp.snap);
   } else {
-    q.dx = b.as<double>(take(cap * 8));
-    q.dy = b.as<double>(take(cap * 8));
-    q.dz = b.as<double>(take(cap * 8));
-    q.dvx = b.as<double>(take(cap * 8));
-    q.dvy = b.as<double>(take(cap * 8));
-    q.dvz = b.as<double>(take(cap * 8));
-    q.dt = b.as<double>(take(cap * 8));
+    d(&tmp.dx); d(&tmp.dy); d(&tmp.dz); d(&tmp.dvx); d(&tmp.dvy); d(&tmp.dvz); d(&tmp.dt);
   }
-  q.margin = b.as<double>(take(cap * 8));
-  q.rows = b.as<int32_t>(take(cap * 4));
-  q.id = b.as<int32_t>(take(cap * 4));
-  q.count = ctl;
-  q.head = ctl + 1;
-  return q;
+  d(&tmp.lens_dt);
+  d(&tmp.margin);
+  i(&tmp.rows); i(&tmp.id); i(&tmp.n_done); i(&tmp.n_total);
+  tmp.count = ctl;
+  tmp.max_steps = ctl ? ctl + 1 : nullptr;
+  if (q) *q = tmp;
+  return off;
 }
 
 size_t queue_bytes(size_t cap, int precision) {
-  size_t per = precision == 32 ? 6 * align256(cap * 4) : 7 * align256(cap * 8);
-  return per + align256(cap * 8) + 2 * align256(cap * 4);
+  return layout_queue(nullptr, cap, precision, nullptr, nullptr);
 }
 
 int lens_force_kind(const ctraj_context* c, const ctraj_element& e) {
@@ -288,19 +285,24 @@ int blocks_per_sm(KernelT k, int threads, size_t smem) {
 
 // The lens kernel for lens element i: FP32 is specialised on the force law,
 // FP64 evaluates the reference's force code for every table kind.
-template <bool k64, bool kOut>
-using LensKernel = void (*)(const Plan, const RunDev, const int, const Queue, const Queue, const int);
+using LensKernel = void (*)(const Plan, const RunDev, const int, const Queue, const Queue,
+                            const Queue, const int);
 
 template <bool k64, bool kOut>
-LensKernel<k64, kOut> lens_kernel(int force) {
-  if (k64) return k_lens<Mol64<false>, kOut, 0, true>;
+LensKernel lens_kernel(int force) {
+  if (k64) return k_lens_chunk<Mol64<false>, kOut, 0, true>;
   switch (force) {
-    case kForceStark2: return k_lens<Mol32<kOut, false>, kOut, kForceStark2, false>;
-    case kForceStark1: return k_lens<Mol32<kOut, false>, kOut, kForceStark1, false>;
-    default: return k_lens<Mol32<kOut, false>, kOut, kForceRadial, false>;
+    case kForceStark2: return k_lens_chunk<Mol32<kOut, false>, kOut, kForceStark2, false>;
+    case kForceStark1: return k_lens_chunk<Mol32<kOut, false>, kOut, kForceStark1, false>;
+    default: return k_lens_chunk<Mol32<kOut, false>, kOut, kForceRadial, false>;
   }
 }
 
+// k_front, then for each lens: read the lens queue's size and largest
+// remaining step count (one small device-to-host copy), and launch
+// ceil(max / chunk) chunk kernels that ping-pong between two queues while
+// molecules leaving the lens collect in a third for the next lens.
+// *left receives the molecules still in a lens afterwards (always 0).
 template <bool k64, bool kOut>
 int launch_all(ctraj_context* c, const Plan& P, const RunDev& R, Queue* q, int* launches) {
   using MolT = typename std::conditional<k64, Mol64<false>, Mol32<kOut, false>>::type;
@@ -317,23 +319,38 @@ int launch_all(ctraj_context* c, const Plan& P, const RunDev& R, Queue* q, int* 
     ++*launches;
   }
   if (c->timing) CT_CUDA(cudaEventRecord(c->ev[1], s));
-  int cur = 0;
-  for (int i = 0; i < P.n_el; ++i) {
+  bool started = false;
+  int cur = 0, alt = 1, nxt = 2;
+  for (int i = 0; i < P.n_el && n > 0; ++i) {
     if (P.el[i].type != CTRAJ_ELECTROSTATIC_LENS) continue;
-    const int nxt = cur ^ 1;
+    CT_CUDA(cudaMemcpyAsync(c->host_max, q[cur].count, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    CT_CUDA(cudaStreamSynchronize(s));
+    const unsigned count = c->host_max[0], max_steps = c->host_max[1];
+    if (count == 0) break;  // no molecule reaches this lens, hence none reaches a later one
+    if (c->timing && !started) CT_CUDA(cudaEventRecord(c->ev[2], s));
+    started = true;
     CT_CUDA(cudaMemsetAsync(q[nxt].count, 0, 2 * sizeof(unsigned), s));
     const size_t smem = k64 ? 0 : size_t(P.lf[i].n_smem) * sizeof(float4);
-    LensKernel<k64, kOut> kl = lens_kernel<k64, kOut>(P.lf[i].force);
+    LensKernel kl = lens_kernel<k64, kOut>(P.lf[i].force);
     CT_CUDA(cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    const int grid = blocks_per_sm(kl, kThreads, smem) * c->sm_count;
-    if (n > 0) {
-      kl<<<grid, kThreads, smem, s>>>(P, R, i, q[cur], q[nxt], c->refill);
+    const int64_t per_launch = int64_t(blocks_per_sm(kl, kThreads, smem)) * c->sm_count;
+    const int grid = int(std::max<int64_t>(1, std::min<int64_t>(per_launch, (count + kThreads - 1) / kThreads)));
+    const int64_t n_chunks = std::max<int64_t>(1, (int64_t(max_steps) + c->chunk - 1) / c->chunk);
+    for (int64_t k = 0; k < n_chunks; ++k) {
+      CT_CUDA(cudaMemsetAsync(q[alt].count, 0, 2 * sizeof(unsigned), s));
+      kl<<<grid, kThreads, smem, s>>>(P, R, i, q[cur], q[alt], q[nxt], c->chunk);
       CT_CUDA(cudaGetLastError());
       ++*launches;
+      std::swap(cur, alt);
     }
-    cur = nxt;
+    std::swap(cur, nxt);  // the next lens starts from the molecules queued at its entrance
   }
-  if (c->timing) CT_CUDA(cudaEventRecord(c->ev[2], s));
+  if (c->timing) {
+    if (!started) CT_CUDA(cudaEventRecord(c->ev[2], s));
+    CT_CUDA(cudaEventRecord(c->ev[3], s));
+  }
+  // the queue that would feed one more chunk must be empty
+  CT_CUDA(cudaMemcpyAsync(c->host_max + 2, q[alt].count, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   return CTRAJ_OK;
 }
 
@@ -420,7 +437,8 @@ int ctraj_create(int device, ctraj_context** out) {
   c->device = device;
   cudaError_t e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
-  for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
+  for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
+  if (e == cudaSuccess) e = cudaMallocHost(&c->host_max, 4 * sizeof(unsigned));
   if (e != cudaSuccess) {
     delete c;
     return fail(CTRAJ_ECUDA, "context setup: %s", cudaGetErrorString(e));
@@ -442,8 +460,7 @@ int ctraj_destroy(ctraj_context* c) {
   cudaStreamSynchronize(c->stream);
   for (auto& t : c->tables) t.dev.release();
   c->lens_tables.release();
-  c->queue[0].release();
-  c->queue[1].release();
+  for (auto& q : c->queue) q.release();
   c->qctl.release();
   c->ics.release();
   c->outs.release();
@@ -452,6 +469,7 @@ int ctraj_destroy(ctraj_context* c) {
   c->rec_count.release();
   for (auto& ev : c->ev)
     if (ev) cudaEventDestroy(ev);
+  if (c->host_max) cudaFreeHost(c->host_max);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
   return CTRAJ_OK;
@@ -529,13 +547,18 @@ int ctraj_run(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* stats)
   const size_t cap = size_t(std::max<int64_t>(n, 1));
   int n_lens = 0;
   for (int i = 0; i < P.n_el; ++i) n_lens += P.el[i].type == CTRAJ_ELECTROSTATIC_LENS;
-  if ((st = c->queue[0].ensure(queue_bytes(cap, a->precision)))) return st;
-  if (n_lens > 1 && (st = c->queue[1].ensure(queue_bytes(cap, a->precision)))) return st;
+  // two queues per lens (chunk ping-pong) plus one collecting the next lens's entrants
+  const int n_queues = n_lens == 0 ? 1 : (n_lens == 1 ? 2 : 3);
+  for (int k = 0; k < n_queues; ++k)
+    if ((st = c->queue[k].ensure(queue_bytes(cap, a->precision)))) return st;
   unsigned* ctl = c->qctl.as<unsigned>();
   unsigned long long* counts = c->qctl.as<unsigned long long>(256);
   unsigned long long* dstats = c->qctl.as<unsigned long long>(256 + 8 * (CTRAJ_MAX_LABELS + 1));
-  Queue q[2] = {make_queue(c->queue[0], cap, a->precision, ctl),
-                make_queue(n_lens > 1 ? c->queue[1] : c->queue[0], cap, a->precision, ctl + 2)};
+  // without a third buffer the next-lens queue aliases queue 1's storage: it is
+  // never written, because nothing follows the last lens
+  Queue q[3];
+  for (int k = 0; k < 3; ++k)
+    layout_queue(&c->queue[std::min(k, n_queues - 1)], cap, a->precision, ctl + 2 * k, &q[k]);
   CT_CUDA(cudaMemsetAsync(c->qctl.p, 0, 4096, c->stream));
   R.counts = counts;
   R.stats = dstats;
@@ -570,6 +593,8 @@ int ctraj_run(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* stats)
     if (a->out_final) CT_CUDA(cudaMemcpyAsync(a->out_final, R.out_final, n * 80, cudaMemcpyDeviceToHost, c->stream));
   }
   CT_CUDA(cudaStreamSynchronize(c->stream));
+  if (c->host_max[2] != 0)
+    return fail(CTRAJ_ECUDA, "internal error: %u molecules left inside a lens", c->host_max[2]);
   for (int k = 0; k <= c->n_labels; ++k) a->counts[k] = int64_t(hc[k]);
   if (stats) {
     std::memset(stats, 0, sizeof *stats);
@@ -583,7 +608,7 @@ int ctraj_run(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* stats)
     if (c->timing) {
       stats->timed = 1;
       CT_CUDA(cudaEventElapsedTime(&stats->front_ms, c->ev[0], c->ev[1]));
-      CT_CUDA(cudaEventElapsedTime(&stats->lens_ms, c->ev[1], c->ev[2]));
+      CT_CUDA(cudaEventElapsedTime(&stats->lens_ms, c->ev[2], c->ev[3]));
     }
   }
   if (hs[kStatRangeError])

@@ -1,21 +1,22 @@
 // Propagation kernels.
 //
-// One run = k_front over all molecules, then one k_lens per electrostatic
-// lens in beamline order.
+// One run = k_front over all molecules, then, for each electrostatic lens in
+// beamline order, k_lens_chunk launched until the lens is empty.
 //
 // k_front (one thread per molecule, grid-stride): draws or loads the initial
 //   conditions, walks the ballistic elements in closed form and stops at the
 //   first lens entrance.  Molecules lost on the way (98 % on the lens-beamline
-//   workload) are tallied at once; survivors are appended to a queue with one
-//   atomic per warp (ballot + prefix popcount), which is the stream compaction
-//   between element segments.
-// k_lens (persistent, one table copy in shared memory per CTA): each warp
-//   takes molecules from the queue and integrates the lens interior with RK4.
-//   A lane whose molecule is lost or reaches the lens exit is refilled from the
-//   queue at the next refill point (every `refill` steps), so warps stay full
-//   while molecules die at different steps.  Finished molecules do the exit
-//   snap and the ballistic elements after the lens, then are tallied or queued
-//   for the next lens.
+//   workload) are tallied at once; molecules inside the lens bore get their
+//   step count, step size and exit-snap time (in double) and are appended to
+//   a queue with one atomic per warp (ballot + prefix popcount): the stream
+//   compaction between element segments.
+// k_lens_chunk (one thread per queued molecule, the lens's table staged in
+//   shared memory per CTA): at most `chunk` RK4 steps per molecule, then the
+//   molecules still inside the lens are compacted into the next chunk's
+//   queue.  Every chunk therefore starts with full warps although molecules
+//   are lost at very different steps.  Molecules that leave the lens do the
+//   exit snap and the ballistic elements after it here, then are tallied or
+//   queued at the next lens.
 // k_record: replays chosen molecules one thread each and writes their
 //   trajectory rows (trajectory recording for apertures of interest).
 //
@@ -26,6 +27,7 @@
 #include "molecule.cuh"
 
 namespace ctraj {
+
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kThreads = 256;
@@ -93,6 +95,26 @@ __device__ __forceinline__ void write_outputs(const RunDev& R, const M& m, int l
   if (R.out_final) m.final_row(R.out_final, i, R.n);
 }
 
+
+// Step parameters of a molecule that passed the entrance of lens `li`; false
+// when rint(L/dz) is not finite or too large (the reference raises there).
+template <class M>
+__device__ __forceinline__ bool enter_lens(M& m, const Plan& P, int li, LensStep& st) {
+  if (!lens_setup(P.el[li], m.vel_z(), st)) return false;
+  m.lens_begin(P, li, st);
+  return true;
+}
+
+// Append the lanes with push == true to Q and raise Q's largest remaining
+// step count (all lanes call).
+template <class M>
+__device__ __forceinline__ void push_lens(const Queue& Q, bool push, const M& m, const LensStep& st) {
+  const unsigned slot = queue_slot(push, Q.count);
+  if (push) m.store(Q, slot, st);
+  const unsigned rem = __reduce_max_sync(kFull, push ? unsigned(st.n_total - st.n_done) : 0u);
+  if ((threadIdx.x & 31) == 0 && rem) atomicMax(Q.max_steps, rem);
+}
+
 // ---------------------------------------------------------------------------
 template <class M, bool kOut>
 __global__ void __launch_bounds__(kThreads) k_front(const __grid_constant__ Plan P, const RunDev R,
@@ -101,40 +123,48 @@ __global__ void __launch_bounds__(kThreads) k_front(const __grid_constant__ Plan
   tally_init(S);
   __syncthreads();
   const int lane = threadIdx.x & 31;
-  unsigned long long steps = 0, band = 0;
+  unsigned long long steps = 0, band = 0, bad = 0;
   const int64_t stride = int64_t(gridDim.x) * blockDim.x;
   for (int64_t base = int64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31); base < R.n; base += stride) {
     const int64_t i = base + lane;
     int label = kNone;
     M m;
+    LensStep st;
     if (i < R.n) {
       m.init(P, R, i);
       int lens_at = -1;
       label = walk(m, P, 0, &lens_at);
+      if (label == kQueued && !enter_lens(m, P, lens_at, st)) {
+        label = P.el[lens_at].label_inside;
+        ++bad;
+      }
       if (label != kQueued) {
         steps += unsigned(m.rows);
         band += (m.margin < double(kEdgeBand)) ? 1 : 0;
         write_outputs<M, kOut>(R, m, label);
       }
     }
-    const unsigned slot = queue_slot(label == kQueued, Q.count);
-    if (label == kQueued) m.store(Q, slot);
+    push_lens(Q, label == kQueued, m, st);
     tally_warp(S, label, P.n_labels);
   }
   stat_add(S, kStatSteps, steps);
   stat_add(S, kStatEdgeBand, band);
+  stat_add(S, kStatBadSteps, bad);
   tally_flush(S, R, P.n_labels);
 }
 
 // ---------------------------------------------------------------------------
-enum : int { kFree = 0, kRun = 1, kLost = 2, kExit = 3, kExhausted = 4 };
+enum : int { kIdle = 0, kRun = 1, kLost = 2, kExit = 3 };
 
 template <class M, bool kOut, int F, bool k64>
-__global__ void __launch_bounds__(kThreads) k_lens(const __grid_constant__ Plan P, const RunDev R,
-                                                   const int li, const Queue Qin, const Queue Qout,
-                                                   const int refill) {
+__global__ void __launch_bounds__(kThreads) k_lens_chunk(const __grid_constant__ Plan P, const RunDev R,
+                                                         const int li, const Queue Qin,
+                                                         const Queue Qcont, const Queue Qnext,
+                                                         const int chunk) {
   extern __shared__ float4 s_tab[];
   __shared__ BlockTally S;
+  const unsigned n_in = *(volatile unsigned*)Qin.count;
+  if (int64_t(blockIdx.x) * blockDim.x >= n_in) return;  // nothing for this CTA (uniform)
   tally_init(S);
   const LensF& L = P.lf[li];
   if (!k64)
@@ -142,57 +172,30 @@ __global__ void __launch_bounds__(kThreads) k_lens(const __grid_constant__ Plan 
   __syncthreads();
 
   const ctraj_element& e = P.el[li];
-  const unsigned n_in = *(volatile unsigned*)Qin.count;
+  const bool classic = e.scheme == CTRAJ_RK4_CLASSIC;
   const int lane = threadIdx.x & 31;
   unsigned long long steps = 0, lsteps = 0, band = 0, bad = 0, range = 0, rerr = 0;
-
-  M m;
-  LensStep st;
-  float dt = 0.f, hdt = 0.f, c2 = 0.f, dt6 = 0.f, dt26 = 0.f;
-  int phase = kFree;
-  unsigned flags = 0;
-  const bool classic = e.scheme == CTRAJ_RK4_CLASSIC;
-
-  for (;;) {
-    // refill lanes without a molecule
-    for (;;) {
-      const unsigned need = __ballot_sync(kFull, phase == kFree);
-      if (!need) break;
-      const int leader = __ffs(need) - 1;
-      unsigned base = 0;
-      if (lane == leader) base = atomicAdd(Qin.head, unsigned(__popc(need)));
-      base = __shfl_sync(kFull, base, leader);
-      int label = kNone;
-      if (phase == kFree) {
-        const unsigned idx = base + unsigned(__popc(need & ((1u << lane) - 1u)));
-        if (idx >= n_in) {
-          phase = kExhausted;
-        } else {
-          m.load(Qin, idx, P);
-          flags = 0;
-          if (!lens_setup(e, m.vel_z(), st)) {
-            // rint(L/dz) not finite or too large: the reference raises here
-            ++bad;
-            label = e.label_inside;
-            steps += unsigned(m.rows);
-            write_outputs<M, kOut>(R, m, label);
-          } else {
-            m.lens_begin(P, li, st);
-            dt = float(st.dt);
-            hdt = 0.5f * dt;
-            c2 = classic ? hdt : dt;
-            dt6 = dt * (1.0f / 6.0f);
-            dt26 = float(st.dt * st.dt / 6.0);
-            phase = st.n_total > 0 ? kRun : kExit;
-          }
-        }
-      }
-      tally_warp(S, label, P.n_labels);
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t base = int64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31); base < n_in; base += stride) {
+    const int64_t idx = base + lane;
+    M m;
+    LensStep st, nst;
+    st.n_done = 0;
+    int phase = kIdle;
+    unsigned flags = 0;
+    float dt = 0.f, hdt = 0.f, c2 = 0.f, dt6 = 0.f, dt26 = 0.f;
+    int64_t n0 = 0;
+    if (idx < n_in) {
+      m.load(Qin, unsigned(idx), P, st);
+      n0 = st.n_done;
+      dt = float(st.dt);
+      hdt = 0.5f * dt;
+      c2 = classic ? hdt : dt;
+      dt6 = dt * (1.0f / 6.0f);
+      dt26 = float(st.dt * st.dt / 6.0);
+      phase = st.n_done < st.n_total ? kRun : kExit;
     }
-    if (__all_sync(kFull, phase == kExhausted)) break;
-
-    // integrate
-    for (int k = 0; k < refill; ++k) {
+    for (int k = 0; k < chunk; ++k) {
       if (phase == kRun) {
         bool lost;
         if constexpr (k64) {
@@ -208,13 +211,12 @@ __global__ void __launch_bounds__(kThreads) k_lens(const __grid_constant__ Plan 
         if (lost) phase = kLost;
         else if (st.n_done == st.n_total) phase = kExit;
       }
+      if ((k & 15) == 15 && !__any_sync(kFull, phase == kRun)) break;
     }
-
-    // finish molecules that left the lens or were lost in it
+    lsteps += unsigned(st.n_done - n0);
     int label = kNone;
-    const bool done = phase == kLost || phase == kExit;
-    if (done) {
-      lsteps += unsigned(st.n_done);
+    bool enter = false;
+    if (phase == kLost || phase == kExit) {
       range += (flags & 1u) ? 1 : 0;
       rerr += (flags & 2u) ? 1 : 0;
       m.lens_end(P, li, st, phase == kLost);
@@ -223,6 +225,13 @@ __global__ void __launch_bounds__(kThreads) k_lens(const __grid_constant__ Plan 
       } else {
         int lens_at = -1;
         label = walk(m, P, li + 1, &lens_at);
+        if (label == kQueued) {
+          enter = enter_lens(m, P, lens_at, nst);
+          if (!enter) {
+            label = P.el[lens_at].label_inside;
+            ++bad;
+          }
+        }
       }
       if (label != kQueued) {
         steps += unsigned(m.rows);
@@ -230,10 +239,9 @@ __global__ void __launch_bounds__(kThreads) k_lens(const __grid_constant__ Plan 
         write_outputs<M, kOut>(R, m, label);
       }
     }
-    const unsigned slot = queue_slot(label == kQueued, Qout.count);
-    if (label == kQueued) m.store(Qout, slot);
+    push_lens(Qcont, phase == kRun, m, st);
+    push_lens(Qnext, enter, m, nst);
     tally_warp(S, label, P.n_labels);
-    if (done) phase = kFree;
   }
   stat_add(S, kStatSteps, steps);
   stat_add(S, kStatLensSteps, lsteps);

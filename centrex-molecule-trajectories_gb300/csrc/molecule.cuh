@@ -367,16 +367,19 @@ struct Mol64 {
     if (kRec && !sink->last_written) sink->write(x[0], x[1], x[2], v[0], v[1], v[2], a[0], a[1], a[2], t);
   }
 
-  __device__ void store(const Queue& Q, unsigned s) const {
+  __device__ void store(const Queue& Q, unsigned s, const LensStep& st) const {
     Q.dx[s] = x[0]; Q.dy[s] = x[1]; Q.dz[s] = x[2];
     Q.dvx[s] = v[0]; Q.dvy[s] = v[1]; Q.dvz[s] = v[2];
     Q.dt[s] = t; Q.margin[s] = margin; Q.rows[s] = rows; Q.id[s] = id;
+    Q.lens_dt[s] = st.dt; Q.n_done[s] = int32_t(st.n_done); Q.n_total[s] = int32_t(st.n_total);
   }
-  __device__ void load(const Queue& Q, unsigned s, const Plan& P) {
+  // The stored acceleration is not carried: the next RK4 step recomputes it.
+  __device__ void load(const Queue& Q, unsigned s, const Plan& P, LensStep& st) {
     x[0] = Q.dx[s]; x[1] = Q.dy[s]; x[2] = Q.dz[s];
     v[0] = Q.dvx[s]; v[1] = Q.dvy[s]; v[2] = Q.dvz[s];
     t = Q.dt[s]; margin = Q.margin[s]; rows = Q.rows[s]; id = Q.id[s];
     a[0] = 0.0; a[1] = -P.g; a[2] = 0.0;
+    st.dt = Q.lens_dt[s]; st.n_done = Q.n_done[s]; st.n_total = Q.n_total[s];
   }
 };
 
@@ -393,7 +396,6 @@ struct Mol32 {
   double zc;      // current z, kept only for outputs / recording
   float ax, ay;   // stored acceleration (recording)
   float cx, cy, cvx, cvy;  // rounding errors carried by the lens integration
-  double t0;      // time at the lens entrance
   RowSink* sink;
 
   // s += inc with the rounding error carried in c (Fast2Sum: |s| >= |inc + c|
@@ -548,28 +550,29 @@ struct Mol32 {
     return r2 > P.ef[i].c[0];
   }
 
-  // Inside the lens t and z follow from the step count (t0 + n dt, z0 + n dz)
-  // instead of being accumulated in float.
-  __device__ void lens_begin(const Plan&, int, const LensStep&) {
-    t0 = double(t);
-    cx = cy = cvx = cvy = 0.0f;
+  // Inside the lens t keeps the entrance time and z is not tracked: both
+  // follow from the step count (t + n dt, z0 + n dz) instead of being
+  // accumulated in float.
+  __device__ void lens_begin(const Plan&, int, const LensStep&) { cx = cy = cvx = cvy = 0.0f; }
+  __device__ double lens_dz(const ctraj_element& e) const {
+    return e.step_mode == CTRAJ_STEP_DT ? dmul(double(vz), e.p[2]) : e.p[1];
   }
   __device__ void lens_row(const Plan& P, int i, const LensStep& s) {
     if (kRec) {
-      zc = P.el[i].z0 + double(s.n_done) * s.dz;
-      sink->put(x, y, zc, vx, vy, vz, ax, ay, 0.0, t0 + double(s.n_done) * s.dt);
+      zc = P.el[i].z0 + double(s.n_done) * lens_dz(P.el[i]);
+      sink->put(x, y, zc, vx, vy, vz, ax, ay, 0.0, double(t) + double(s.n_done) * s.dt);
     }
   }
   // After the last step: t from the step count, then the exit snap of
   // (z1 - z0 - N dz) / vz with the stored acceleration l1 unless lost inside.
   __device__ void lens_end(const Plan& P, int i, const LensStep& s, bool lost) {
-    t = float(t0 + double(s.n_done) * s.dt);
+    t = float(double(t) + double(s.n_done) * s.dt);
     rows += int(s.n_done);
     x = __fadd_rn(x, cx);
     y = __fadd_rn(y, cy);
     vx = __fadd_rn(vx, cvx);
     vy = __fadd_rn(vy, cvy);
-    if (kOut || kRec) zc = P.el[i].z0 + double(s.n_done) * s.dz;
+    if (kOut || kRec) zc = P.el[i].z0 + double(s.n_done) * lens_dz(P.el[i]);
     if (lost) return;
     flight(float(s.snap), P);
     if (kOut || kRec) zc = P.el[i].z1;
@@ -584,13 +587,20 @@ struct Mol32 {
     if (kRec && !sink->last_written) sink->write(x, y, zc, vx, vy, vz, ax, ay, 0.0, t);
   }
 
-  __device__ void store(const Queue& Q, unsigned s) const {
+  __device__ void store(const Queue& Q, unsigned s, const LensStep& st) const {
     Q.x[s] = x; Q.y[s] = y; Q.vx[s] = vx; Q.vy[s] = vy; Q.vz[s] = vz; Q.t[s] = t;
+    Q.cx[s] = cx; Q.cy[s] = cy; Q.cvx[s] = cvx; Q.cvy[s] = cvy;
+    Q.lens_dt[s] = st.dt; Q.snap[s] = float(st.snap);
+    Q.n_done[s] = int32_t(st.n_done); Q.n_total[s] = int32_t(st.n_total);
     Q.rows[s] = rows; Q.id[s] = id;
     if (kOut) Q.margin[s] = margin;
   }
-  __device__ void load(const Queue& Q, unsigned s, const Plan& P) {
+  // The stored acceleration is not carried: the next RK4 step recomputes it.
+  __device__ void load(const Queue& Q, unsigned s, const Plan& P, LensStep& st) {
     x = Q.x[s]; y = Q.y[s]; vx = Q.vx[s]; vy = Q.vy[s]; vz = Q.vz[s]; t = Q.t[s];
+    cx = Q.cx[s]; cy = Q.cy[s]; cvx = Q.cvx[s]; cvy = Q.cvy[s];
+    st.dt = Q.lens_dt[s]; st.snap = double(Q.snap[s]);
+    st.n_done = Q.n_done[s]; st.n_total = Q.n_total[s];
     rows = Q.rows[s]; id = Q.id[s];
     inv_vz = __frcp_rn(vz);
     ax = 0.0f;

@@ -89,16 +89,23 @@ enum : int {
   kStatCount = 8,
 };
 
-// Molecules waiting at a lens entrance (SoA, capacity n).  FP32 queues use the
-// float arrays, FP64 queues the double ones.
+// Molecules inside a lens between two chunks of RK4 steps (SoA, capacity n):
+// the state, the carried rounding errors of the FP32 integration, and the
+// per-molecule step parameters computed once at the lens entrance.  FP32
+// queues use the float arrays, FP64 queues the double ones.
 struct Queue {
-  float *x, *y, *vx, *vy, *vz, *t;
+  float *x, *y, *vx, *vy, *vz, *t;     // t: time at the lens entrance
+  float *cx, *cy, *cvx, *cvy;
+  float* snap;                          // exit-snap time
   double *dx, *dy, *dz, *dvx, *dvy, *dvz, *dt;
+  double* lens_dt;                      // dz / vz
   double* margin;
   int32_t* rows;
   int32_t* id;
+  int32_t* n_done;
+  int32_t* n_total;
   unsigned int* count;  // entries written
-  unsigned int* head;   // entries taken
+  unsigned int* max_steps;  // largest n_total - n_done written (sizes the chunk loop)
 };
 
 constexpr int kLabelDetected = -1;  // counts[n_labels]
