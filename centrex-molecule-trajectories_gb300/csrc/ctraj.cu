@@ -111,6 +111,8 @@ namespace {
 
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
+constexpr int kMaxStagedIntervals = 6144;  // 96 KiB of float4 per CTA
+
 // Queue layout inside one buffer of capacity cap (SoA, each array 256-byte
 // aligned so a warp's 32 consecutive entries are whole 128-byte lines).
 // Returns the bytes used; with b == nullptr only sizes the layout.
@@ -166,12 +168,10 @@ int build_lens_tables(ctraj_context* c) {
     const int n_int = t.n - 1;
     c->lens_offset[i] = host.size();
     c->lens_n_int[i] = n_int;
-    const double bore = e.p[0] * 0.5;
-    int n_cover;
+    (void)x0;
     if (t.kind == CTRAJ_TABLE_RADIAL_LINEAR) {
       for (int j = 0; j < n_int; ++j)
         host.push_back(make_float4(float(t.values[j]), float(t.values[j + 1] - t.values[j]), 0.f, 0.f));
-      n_cover = n_int;
     } else {
       const double alpha = e.p[6], mass = e.p[5];
       const double kappa = e.field_order == 1 ? alpha / mass : 2.0 * alpha / mass;
@@ -180,12 +180,9 @@ int build_lens_tables(ctraj_context* c) {
         host.push_back(make_float4(float(-kappa * cj[2]), float(-kappa * 2.0 * cj[1] * h),
                                    float(-kappa * 3.0 * cj[0] * h * h), 0.f));
       }
-      const double rcap = 1.1 * bore;
-      const double ecap = e.field_order == 1 ? alpha * rcap : alpha * rcap * rcap;
-      n_cover = int(std::min<double>(n_int, std::ceil((ecap - x0) / h) + 2.0));
     }
-    // at most 96 KiB of shared memory per CTA for the staged part
-    c->lens_n_smem[i] = std::max(0, std::min(n_cover, 6144));
+    // the whole table goes to shared memory when it takes at most 96 KiB
+    c->lens_n_smem[i] = n_int <= kMaxStagedIntervals ? n_int : 0;
   }
   if (!host.empty()) {
     int st = c->lens_tables.ensure(host.size() * sizeof(float4));
@@ -286,16 +283,21 @@ int blocks_per_sm(KernelT k, int threads, size_t smem) {
 // The lens kernel for lens element i: FP32 is specialised on the force law,
 // FP64 evaluates the reference's force code for every table kind.
 using LensKernel = void (*)(const Plan, const RunDev, const int, const Queue, const Queue,
-                            const Queue, const int);
+                            const Queue, const int, const LensArgs);
+
+template <bool kOut, bool kStaged>
+LensKernel lens_kernel32(int force) {
+  switch (force) {
+    case kForceStark2: return k_lens_chunk<Mol32<kOut, false>, kOut, kForceStark2, false, kStaged>;
+    case kForceStark1: return k_lens_chunk<Mol32<kOut, false>, kOut, kForceStark1, false, kStaged>;
+    default: return k_lens_chunk<Mol32<kOut, false>, kOut, kForceRadial, false, kStaged>;
+  }
+}
 
 template <bool k64, bool kOut>
-LensKernel lens_kernel(int force) {
-  if (k64) return k_lens_chunk<Mol64<false>, kOut, 0, true>;
-  switch (force) {
-    case kForceStark2: return k_lens_chunk<Mol32<kOut, false>, kOut, kForceStark2, false>;
-    case kForceStark1: return k_lens_chunk<Mol32<kOut, false>, kOut, kForceStark1, false>;
-    default: return k_lens_chunk<Mol32<kOut, false>, kOut, kForceRadial, false>;
-  }
+LensKernel lens_kernel(int force, bool staged) {
+  if (k64) return k_lens_chunk<Mol64<false>, kOut, 0, true, false>;
+  return staged ? lens_kernel32<kOut, true>(force) : lens_kernel32<kOut, false>(force);
 }
 
 // k_front, then for each lens: read the lens queue's size and largest
@@ -330,27 +332,29 @@ int launch_all(ctraj_context* c, const Plan& P, const RunDev& R, Queue* q, int* 
     if (c->timing && !started) CT_CUDA(cudaEventRecord(c->ev[2], s));
     started = true;
     CT_CUDA(cudaMemsetAsync(q[nxt].count, 0, 2 * sizeof(unsigned), s));
-    const size_t smem = k64 ? 0 : size_t(P.lf[i].n_smem) * sizeof(float4);
-    LensKernel kl = lens_kernel<k64, kOut>(P.lf[i].force);
+    const bool staged = !k64 && P.lf[i].n_smem > 0;
+    const size_t smem = staged ? size_t(P.lf[i].n_int) * sizeof(float4) : 0;
+    LensKernel kl = lens_kernel<k64, kOut>(P.lf[i].force, staged);
     CT_CUDA(cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     const int64_t per_launch = int64_t(blocks_per_sm(kl, kThreads, smem)) * c->sm_count;
     const int grid = int(std::max<int64_t>(1, std::min<int64_t>(per_launch, (count + kThreads - 1) / kThreads)));
     const int64_t n_chunks = std::max<int64_t>(1, (int64_t(max_steps) + c->chunk - 1) / c->chunk);
+    const LensArgs la = lens_args(P, i, !k64);
     for (int64_t k = 0; k < n_chunks; ++k) {
       CT_CUDA(cudaMemsetAsync(q[alt].count, 0, 2 * sizeof(unsigned), s));
-      kl<<<grid, kThreads, smem, s>>>(P, R, i, q[cur], q[alt], q[nxt], c->chunk);
+      kl<<<grid, kThreads, smem, s>>>(P, R, i, q[cur], q[alt], q[nxt], c->chunk, la);
       CT_CUDA(cudaGetLastError());
       ++*launches;
       std::swap(cur, alt);
     }
+    // q[cur] now holds what would feed one more chunk: it must be empty
+    CT_CUDA(cudaMemcpyAsync(c->host_max + 2 + i, q[cur].count, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     std::swap(cur, nxt);  // the next lens starts from the molecules queued at its entrance
   }
   if (c->timing) {
     if (!started) CT_CUDA(cudaEventRecord(c->ev[2], s));
     CT_CUDA(cudaEventRecord(c->ev[3], s));
   }
-  // the queue that would feed one more chunk must be empty
-  CT_CUDA(cudaMemcpyAsync(c->host_max + 2, q[alt].count, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   return CTRAJ_OK;
 }
 
@@ -438,7 +442,7 @@ int ctraj_create(int device, ctraj_context** out) {
   cudaError_t e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
   for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
-  if (e == cudaSuccess) e = cudaMallocHost(&c->host_max, 4 * sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMallocHost(&c->host_max, (2 + CTRAJ_MAX_ELEMENTS) * sizeof(unsigned));
   if (e != cudaSuccess) {
     delete c;
     return fail(CTRAJ_ECUDA, "context setup: %s", cudaGetErrorString(e));
@@ -577,6 +581,7 @@ int ctraj_run(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* stats)
     R.out_final = a->out_final;
   }
   int launches = 0;
+  std::memset(c->host_max, 0, (2 + CTRAJ_MAX_ELEMENTS) * sizeof(unsigned));
   c->timing = a->timing != 0;
   if (a->precision == 32)
     st = out ? launch_all<false, true>(c, P, R, q, &launches) : launch_all<false, false>(c, P, R, q, &launches);
@@ -593,8 +598,10 @@ int ctraj_run(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* stats)
     if (a->out_final) CT_CUDA(cudaMemcpyAsync(a->out_final, R.out_final, n * 80, cudaMemcpyDeviceToHost, c->stream));
   }
   CT_CUDA(cudaStreamSynchronize(c->stream));
-  if (c->host_max[2] != 0)
-    return fail(CTRAJ_ECUDA, "internal error: %u molecules left inside a lens", c->host_max[2]);
+  for (int i = 0; i < P.n_el; ++i)
+    if (c->host_max[2 + i] != 0)
+      return fail(CTRAJ_ECUDA, "internal error: %u molecules left inside lens element %d",
+                  c->host_max[2 + i], i);
   for (int k = 0; k <= c->n_labels; ++k) a->counts[k] = int64_t(hc[k]);
   if (stats) {
     std::memset(stats, 0, sizeof *stats);

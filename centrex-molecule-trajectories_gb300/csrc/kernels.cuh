@@ -156,19 +156,18 @@ __global__ void __launch_bounds__(kThreads) k_front(const __grid_constant__ Plan
 // ---------------------------------------------------------------------------
 enum : int { kIdle = 0, kRun = 1, kLost = 2, kExit = 3 };
 
-template <class M, bool kOut, int F, bool k64>
+template <class M, bool kOut, int F, bool k64, bool kStaged>
 __global__ void __launch_bounds__(kThreads) k_lens_chunk(const __grid_constant__ Plan P, const RunDev R,
                                                          const int li, const Queue Qin,
                                                          const Queue Qcont, const Queue Qnext,
-                                                         const int chunk) {
+                                                         const int chunk, const LensArgs L) {
   extern __shared__ float4 s_tab[];
   __shared__ BlockTally S;
   const unsigned n_in = *(volatile unsigned*)Qin.count;
   if (int64_t(blockIdx.x) * blockDim.x >= n_in) return;  // nothing for this CTA (uniform)
   tally_init(S);
-  const LensF& L = P.lf[li];
-  if (!k64)
-    for (int k = threadIdx.x; k < L.n_smem; k += blockDim.x) s_tab[k] = __ldg(L.q + k);
+  if (!k64 && kStaged)
+    for (int k = threadIdx.x; k < L.n_int; k += blockDim.x) s_tab[k] = __ldg(L.q + k);
   __syncthreads();
 
   const ctraj_element& e = P.el[li];
@@ -203,7 +202,7 @@ __global__ void __launch_bounds__(kThreads) k_lens_chunk(const __grid_constant__
           lost = m.lens_step(P, li, st, rg, er);
           flags |= (rg ? 1u : 0u) | (er ? 2u : 0u);
         } else {
-          lost = m.template lens_step<F>(P, li, dt, hdt, c2, dt6, dt26, s_tab, flags);
+          lost = m.template lens_step<F, kStaged>(L, dt, hdt, c2, dt6, dt26, s_tab, flags);
           if (F == kForceRadial && (flags & 2u)) lost = true;
         }
         ++st.n_done;
@@ -258,18 +257,18 @@ template <class M>
 __device__ __forceinline__ bool step_any(M& m, const Plan& P, int li, const float dt, const float hdt,
                                          const float c2, const float dt6, const float dt26,
                                          unsigned& flags) {
+  const LensArgs L = lens_args(P, li, false);  // no shared-memory copy: tables from global memory
   switch (P.lf[li].force) {
     case kForceStark2:
-      return m.template lens_step<kForceStark2>(P, li, dt, hdt, c2, dt6, dt26, nullptr, flags);
+      return m.template lens_step<kForceStark2, false>(L, dt, hdt, c2, dt6, dt26, nullptr, flags);
     case kForceStark1:
-      return m.template lens_step<kForceStark1>(P, li, dt, hdt, c2, dt6, dt26, nullptr, flags);
+      return m.template lens_step<kForceStark1, false>(L, dt, hdt, c2, dt6, dt26, nullptr, flags);
     default:
-      return m.template lens_step<kForceRadial>(P, li, dt, hdt, c2, dt6, dt26, nullptr, flags) ||
+      return m.template lens_step<kForceRadial, false>(L, dt, hdt, c2, dt6, dt26, nullptr, flags) ||
              (flags & 2u);
   }
 }
 
-// The replay plan has n_smem = 0 for every lens, so table reads go to global memory.
 template <class M, bool k64>
 __global__ void __launch_bounds__(128) k_record(const __grid_constant__ Plan P, const RunDev R,
                                                 const int64_t* ids, int64_t n_ids, int stride,

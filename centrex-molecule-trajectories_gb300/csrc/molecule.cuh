@@ -115,8 +115,11 @@ __device__ inline void lens_force64(const Plan& P, const ctraj_element& e, doubl
 // ---------------------------------------------------------------------------
 // FP32 force: w such that a_perp = w * (x, y)
 // ---------------------------------------------------------------------------
-template <int F, bool kFirst = false>
-__device__ __forceinline__ float wforce(float px, float py, const LensF& L, const float4* s_tab,
+// kStaged: the whole table is in shared memory (s_tab); otherwise it is read
+// from global memory through the read-only cache.  Lookups past the last
+// interval extrapolate it (as scipy CubicSpline does); s < 0 uses interval 0.
+template <int F, bool kStaged>
+__device__ __forceinline__ float wforce(float px, float py, const LensArgs& L, const float4* s_tab,
                                         unsigned& flags) {
   const float r2 = __fmaf_rn(py, py, __fmul_rn(px, px));
   float s, r = 0.0f;
@@ -127,11 +130,9 @@ __device__ __forceinline__ float wforce(float px, float py, const LensF& L, cons
     s = __fmaf_rn(L.beta, r, -L.s0);
     if (F == kForceRadial) flags |= (r > L.r_max) ? 2u : 0u;
   }
-  if (kFirst && F != kForceRadial) flags |= (s > float(L.n_int) || s < 0.0f) ? 1u : 0u;
-  int i = __float2int_rz(s);
-  i = max(0, min(i, L.n_int - 1));
-  const float u = __fadd_rn(s, -__int2float_rn(i));
-  const float4 q = (i < L.n_smem) ? s_tab[i] : __ldg(L.q + i);
+  const unsigned i = min(__float2uint_rz(s), unsigned(L.n_int - 1));  // negative s -> 0
+  const float u = __fadd_rn(s, -__uint2float_rn(i));
+  const float4 q = kStaged ? s_tab[i] : __ldg(L.q + i);
   if (F == kForceRadial) {
     const float a_r = __fmaf_rn(u, q.y, q.x);
     return r > 0.0f ? __fdividef(a_r, r) : 0.0f;
@@ -143,8 +144,8 @@ __device__ __forceinline__ float wforce(float px, float py, const LensF& L, cons
 
 // Per-molecule lens integration parameters (both precisions).
 struct LensStep {
-  int64_t n_total;  // rint(L/dz)
-  int64_t n_done;
+  int n_total;  // rint(L/dz), at most CTRAJ_MAX_LENS_STEPS
+  int n_done;
   double dt;        // dz / vz
   double snap;      // FP32: exit-snap time (z1 - z0 - N dz) / vz
   double dz;
@@ -162,7 +163,7 @@ __device__ __forceinline__ bool lens_setup(const ctraj_element& e, double vz, Le
     s.snap = 0.0;
     return false;
   }
-  s.n_total = nf < 0.0 ? 0 : int64_t(nf);
+  s.n_total = nf < 0.0 ? 0 : int(nf);
   s.dt = dz / vz;
   s.snap = ((e.z1 - e.z0) - double(s.n_total) * dz) / vz;
   return true;
@@ -516,23 +517,22 @@ struct Mol32 {
 
   __device__ double vel_z() const { return double(vz); }
 
-  template <int F>
-  __device__ bool lens_step(const Plan& P, int i, const float dt, const float hdt, const float c2,
+  template <int F, bool kStaged>
+  __device__ bool lens_step(const LensArgs& L, const float dt, const float hdt, const float c2,
                             const float dt6, const float dt26, const float4* s_tab, unsigned& flags) {
-    const LensF& L = P.lf[i];
-    const float g = P.gf;
-    const float w1 = wforce<F, true>(x, y, L, s_tab, flags);
+    const float g = L.g;
+    const float w1 = wforce<F, kStaged>(x, y, L, s_tab, flags);
     const float l1x = __fmul_rn(w1, x), l1y = __fmaf_rn(w1, y, -g);
     const float k2x = __fmaf_rn(hdt, l1x, vx), k2y = __fmaf_rn(hdt, l1y, vy);
     const float p2x = __fmaf_rn(c2, vx, x), p2y = __fmaf_rn(c2, vy, y);
-    const float w2 = wforce<F>(p2x, p2y, L, s_tab, flags);
+    const float w2 = wforce<F, kStaged>(p2x, p2y, L, s_tab, flags);
     const float l2x = __fmul_rn(w2, p2x), l2y = __fmaf_rn(w2, p2y, -g);
     const float k3x = __fmaf_rn(hdt, l2x, vx), k3y = __fmaf_rn(hdt, l2y, vy);
     const float p3x = __fmaf_rn(hdt, k2x, x), p3y = __fmaf_rn(hdt, k2y, y);
-    const float w3 = wforce<F>(p3x, p3y, L, s_tab, flags);
+    const float w3 = wforce<F, kStaged>(p3x, p3y, L, s_tab, flags);
     const float l3x = __fmul_rn(w3, p3x), l3y = __fmaf_rn(w3, p3y, -g);
     const float p4x = __fmaf_rn(dt, k3x, x), p4y = __fmaf_rn(dt, k3y, y);
-    const float w4 = wforce<F>(p4x, p4y, L, s_tab, flags);
+    const float w4 = wforce<F, kStaged>(p4x, p4y, L, s_tab, flags);
     const float l4x = __fmul_rn(w4, p4x), l4y = __fmaf_rn(w4, p4y, -g);
     const float sx = __fadd_rn(__fadd_rn(l1x, l2x), l3x);
     const float sy = __fadd_rn(__fadd_rn(l1y, l2y), l3y);
@@ -546,8 +546,8 @@ struct Mol32 {
     ax = l1x;
     ay = l1y;
     const float r2 = __fmaf_rn(y, y, __fmul_rn(x, x));
-    if (kOut) note(__fadd_rn(sqrtf(r2), -P.ef[i].c[1]));
-    return r2 > P.ef[i].c[0];
+    if (kOut) note(__fadd_rn(sqrtf(r2), -L.bore));
+    return r2 > L.bore2;
   }
 
   // Inside the lens t keeps the entrance time and z is not tracked: both

@@ -36,6 +36,19 @@ struct LensF {
   int force;        // kForce*
 };
 
+// The FP32 constants of the one lens a k_lens_chunk launch integrates, passed
+// as their own kernel parameter so every use is a fixed-offset constant-bank
+// operand (the Plan's per-element arrays need an indexed load per use).
+struct LensArgs {
+  const float4* q;
+  float beta, s0, r_max;
+  int n_int, n_smem;
+  float g;
+  float bore2;  // (d/2)^2
+  float bore;   // d/2
+  int classic;
+};
+
 // FP64 view of a force table (device pointers).
 struct TableD {
   const double* knots;
@@ -59,6 +72,24 @@ struct Plan {
   LensF lf[CTRAJ_MAX_ELEMENTS];
   TableD td[CTRAJ_MAX_TABLES];
 };
+
+// LensArgs of lens element li; staged = false reads the whole table from
+// global memory (no shared-memory copy).
+__host__ __device__ inline LensArgs lens_args(const Plan& P, int li, bool staged) {
+  const LensF& f = P.lf[li];
+  LensArgs a;
+  a.q = f.q;
+  a.beta = f.beta;
+  a.s0 = f.s0;
+  a.r_max = f.r_max;
+  a.n_int = f.n_int;
+  a.n_smem = staged ? f.n_smem : 0;
+  a.g = P.gf;
+  a.bore2 = P.ef[li].c[0];
+  a.bore = P.ef[li].c[1];
+  a.classic = P.el[li].scheme == CTRAJ_RK4_CLASSIC;
+  return a;
+}
 
 // Per-run device pointers and scalars.
 struct RunDev {
