@@ -100,7 +100,9 @@ struct ctraj_context {
   DevBuf outs;
   DevBuf rec_rows, rec_ids, rec_count;
   unsigned* host_max = nullptr; // pinned: largest remaining lens step count of a queue
-  int chunk = 128;              // RK4 steps per lens chunk (compaction interval)
+  DevBuf chunk_ctl;             // (count, max_steps) of the queue each lens chunk writes
+  int chunk = 64;               // RK4 steps of the first lens chunk (compaction interval)
+  int chunk_max = 1024;         // chunks double in length up to this
   bool timing = false;
   // before front, after front, before the first lens chunk, after the last one
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -112,6 +114,7 @@ namespace {
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 constexpr int kMaxStagedIntervals = 6144;  // 96 KiB of float4 per CTA
+constexpr int kMaxChunks = 16384;          // lens chunks per lens (CTRAJ_MAX_LENS_STEPS / 1024 < this)
 
 // Queue layout inside one buffer of capacity cap (SoA, each array 256-byte
 // aligned so a warp's 32 consecutive entries are whole 128-byte lines).
@@ -338,17 +341,32 @@ int launch_all(ctraj_context* c, const Plan& P, const RunDev& R, Queue* q, int* 
     CT_CUDA(cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     const int64_t per_launch = int64_t(blocks_per_sm(kl, kThreads, smem)) * c->sm_count;
     const int grid = int(std::max<int64_t>(1, std::min<int64_t>(per_launch, (count + kThreads - 1) / kThreads)));
-    const int64_t n_chunks = std::max<int64_t>(1, (int64_t(max_steps) + c->chunk - 1) / c->chunk);
+    // chunk lengths double from c->chunk up to c->chunk_max: molecules are
+    // lost fastest right after the entrance, so compaction is frequent there
+    // and launches are few in the long tail of survivors
+    std::vector<int> lens_chunks;
+    for (int64_t done = 0, len = c->chunk; done < int64_t(max_steps) || lens_chunks.empty();) {
+      lens_chunks.push_back(int(len));
+      done += len;
+      len = std::min<int64_t>(2 * len, c->chunk_max);
+    }
+    const size_t nc = lens_chunks.size();
+    if (nc > kMaxChunks) return fail(CTRAJ_ESTEPS, "lens element %d needs %zu chunks (max %d)", i, nc, kMaxChunks);
+    CT_CUDA(cudaMemsetAsync(c->chunk_ctl.p, 0, nc * 2 * sizeof(unsigned), s));
     const LensArgs la = lens_args(P, i, !k64);
-    for (int64_t k = 0; k < n_chunks; ++k) {
-      CT_CUDA(cudaMemsetAsync(q[alt].count, 0, 2 * sizeof(unsigned), s));
-      kl<<<grid, kThreads, smem, s>>>(P, R, i, q[cur], q[alt], q[nxt], c->chunk, la);
+    Queue in = q[cur];
+    for (size_t k = 0; k < nc; ++k) {
+      Queue out = q[alt];  // each chunk counts its output in its own slot: no reset in between
+      out.count = c->chunk_ctl.as<unsigned>(k * 2 * sizeof(unsigned));
+      out.max_steps = out.count + 1;
+      kl<<<grid, kThreads, smem, s>>>(P, R, i, in, out, q[nxt], lens_chunks[k], la);
       CT_CUDA(cudaGetLastError());
       ++*launches;
+      in = out;
       std::swap(cur, alt);
     }
-    // q[cur] now holds what would feed one more chunk: it must be empty
-    CT_CUDA(cudaMemcpyAsync(c->host_max + 2 + i, q[cur].count, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    // the last chunk's continuation queue must be empty
+    CT_CUDA(cudaMemcpyAsync(c->host_max + 2 + i, in.count, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     std::swap(cur, nxt);  // the next lens starts from the molecules queued at its entrance
   }
   if (c->timing) {
@@ -443,15 +461,17 @@ int ctraj_create(int device, ctraj_context** out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
   for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
   if (e == cudaSuccess) e = cudaMallocHost(&c->host_max, (2 + CTRAJ_MAX_ELEMENTS) * sizeof(unsigned));
+  c->stream = c->own_stream;
   if (e != cudaSuccess) {
-    delete c;
+    ctraj_destroy(c);
     return fail(CTRAJ_ECUDA, "context setup: %s", cudaGetErrorString(e));
   }
-  c->stream = c->own_stream;
   int st = c->qctl.ensure(4096);
+  if (!st) st = c->chunk_ctl.ensure(size_t(kMaxChunks) * 2 * sizeof(unsigned));
   if (st) {
-    cudaStreamDestroy(c->own_stream);
-    delete c;
+    std::string msg = g_error;
+    ctraj_destroy(c);  // releases whatever was set up
+    g_error = msg;
     return st;
   }
   *out = c;
@@ -471,6 +491,7 @@ int ctraj_destroy(ctraj_context* c) {
   c->rec_rows.release();
   c->rec_ids.release();
   c->rec_count.release();
+  c->chunk_ctl.release();
   for (auto& ev : c->ev)
     if (ev) cudaEventDestroy(ev);
   if (c->host_max) cudaFreeHost(c->host_max);

@@ -72,7 +72,10 @@ def test_fp32_within_tolerance(engine, case):
     assert np.all(dz[same] <= ztol[same]), dz[same].max()
     dvel = np.abs(r.final[3:6, same] - o["final"][3:6, same])
     assert dvel.max(initial=0) < VEL_TOL, dvel.max(initial=0)
-    np.testing.assert_allclose(r.final[9, same], o["final"][9, same], atol=TIME_TOL, rtol=0)
+    # time of a plate hit is (x_plate - x) / vx: an error dx in x is dx / |vx| in t
+    ttol = TIME_TOL + np.where(plates, POS_TOL / np.abs(o["final"][3]), 0.0)
+    dtime = np.abs(r.final[9] - o["final"][9])
+    assert np.all(dtime[same] <= ttol[same]), dtime[same].max()
     # row counts agree except where rint(L/dz) sits on a rounding tie of vz
     assert np.mean(r.rows[same] == o["rows"][same]) > 0.999
 
