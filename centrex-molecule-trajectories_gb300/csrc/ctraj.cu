@@ -141,6 +141,7 @@ size_t layout_queue(const DevBuf* b, size_t cap, int precision, unsigned* ctl, Q
   i(&tmp.rows); i(&tmp.id); i(&tmp.n_done); i(&tmp.n_total);
   tmp.count = ctl;
   tmp.max_steps = ctl ? ctl + 1 : nullptr;
+  tmp.head = ctl ? ctl + 2 : nullptr;
   if (q) *q = tmp;
   return off;
 }
@@ -334,13 +335,14 @@ int launch_all(ctraj_context* c, const Plan& P, const RunDev& R, Queue* q, int* 
     if (count == 0) break;  // no molecule reaches this lens, hence none reaches a later one
     if (c->timing && !started) CT_CUDA(cudaEventRecord(c->ev[2], s));
     started = true;
-    CT_CUDA(cudaMemsetAsync(q[nxt].count, 0, 2 * sizeof(unsigned), s));
+    CT_CUDA(cudaMemsetAsync(q[nxt].count, 0, kCtlWords * sizeof(unsigned), s));
     const bool staged = !k64 && P.lf[i].n_smem > 0;
     const size_t smem = staged ? size_t(P.lf[i].n_int) * sizeof(float4) : 0;
     LensKernel kl = lens_kernel<k64, kOut>(P.lf[i].force, staged);
     CT_CUDA(cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    const int64_t per_launch = int64_t(blocks_per_sm(kl, kThreads, smem)) * c->sm_count;
-    const int grid = int(std::max<int64_t>(1, std::min<int64_t>(per_launch, (count + kThreads - 1) / kThreads)));
+    const int64_t per_launch = int64_t(blocks_per_sm(kl, kLensThreads, smem)) * c->sm_count;
+    const int grid =
+        int(std::max<int64_t>(1, std::min<int64_t>(per_launch, (count + kLensThreads - 1) / kLensThreads)));
     // chunk lengths double from c->chunk up to c->chunk_max: molecules are
     // lost fastest right after the entrance, so compaction is frequent there
     // and launches are few in the long tail of survivors
@@ -352,14 +354,15 @@ int launch_all(ctraj_context* c, const Plan& P, const RunDev& R, Queue* q, int* 
     }
     const size_t nc = lens_chunks.size();
     if (nc > kMaxChunks) return fail(CTRAJ_ESTEPS, "lens element %d needs %zu chunks (max %d)", i, nc, kMaxChunks);
-    CT_CUDA(cudaMemsetAsync(c->chunk_ctl.p, 0, nc * 2 * sizeof(unsigned), s));
+    CT_CUDA(cudaMemsetAsync(c->chunk_ctl.p, 0, nc * kCtlWords * sizeof(unsigned), s));
     const LensArgs la = lens_args(P, i, !k64);
     Queue in = q[cur];
     for (size_t k = 0; k < nc; ++k) {
-      Queue out = q[alt];  // each chunk counts its output in its own slot: no reset in between
-      out.count = c->chunk_ctl.as<unsigned>(k * 2 * sizeof(unsigned));
+      Queue out = q[alt];  // each chunk counts its output in its own slots: no reset in between
+      out.count = c->chunk_ctl.as<unsigned>(k * kCtlWords * sizeof(unsigned));
       out.max_steps = out.count + 1;
-      kl<<<grid, kThreads, smem, s>>>(P, R, i, in, out, q[nxt], lens_chunks[k], la);
+      out.head = out.count + 2;
+      kl<<<grid, kLensThreads, smem, s>>>(P, R, i, in, out, q[nxt], lens_chunks[k], la);
       CT_CUDA(cudaGetLastError());
       ++*launches;
       in = out;
@@ -467,7 +470,7 @@ int ctraj_create(int device, ctraj_context** out) {
     return fail(CTRAJ_ECUDA, "context setup: %s", cudaGetErrorString(e));
   }
   int st = c->qctl.ensure(4096);
-  if (!st) st = c->chunk_ctl.ensure(size_t(kMaxChunks) * 2 * sizeof(unsigned));
+  if (!st) st = c->chunk_ctl.ensure(size_t(kMaxChunks) * kCtlWords * sizeof(unsigned));
   if (st) {
     std::string msg = g_error;
     ctraj_destroy(c);  // releases whatever was set up
@@ -583,7 +586,7 @@ int ctraj_run(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* stats)
   // never written, because nothing follows the last lens
   Queue q[3];
   for (int k = 0; k < 3; ++k)
-    layout_queue(&c->queue[std::min(k, n_queues - 1)], cap, a->precision, ctl + 2 * k, &q[k]);
+    layout_queue(&c->queue[std::min(k, n_queues - 1)], cap, a->precision, ctl + kCtlWords * k, &q[k]);
   CT_CUDA(cudaMemsetAsync(c->qctl.p, 0, 4096, c->stream));
   R.counts = counts;
   R.stats = dstats;

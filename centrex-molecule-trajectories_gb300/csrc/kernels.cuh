@@ -31,6 +31,9 @@ namespace ctraj {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kThreads = 256;
+// Lens chunks: 512 threads, 2 CTAs per SM (<= 64 registers): 32 warps share
+// two copies of the staged table (2 x 64 KiB for 4096 knots).
+constexpr int kLensThreads = 512;
 
 struct BlockTally {
   unsigned long long cnt[CTRAJ_MAX_LABELS + 1];
@@ -157,26 +160,35 @@ __global__ void __launch_bounds__(kThreads) k_front(const __grid_constant__ Plan
 enum : int { kIdle = 0, kRun = 1, kLost = 2, kExit = 3 };
 
 template <class M, bool kOut, int F, bool k64, bool kStaged>
-__global__ void __launch_bounds__(kThreads) k_lens_chunk(const __grid_constant__ Plan P, const RunDev R,
+__global__ void __launch_bounds__(kLensThreads, 2) k_lens_chunk(const __grid_constant__ Plan P, const RunDev R,
                                                          const int li, const Queue Qin,
                                                          const Queue Qcont, const Queue Qnext,
                                                          const int chunk, const LensArgs L) {
   extern __shared__ float4 s_tab[];
   __shared__ BlockTally S;
   const unsigned n_in = *(volatile unsigned*)Qin.count;
-  if (int64_t(blockIdx.x) * blockDim.x >= n_in) return;  // nothing for this CTA (uniform)
+  if (n_in == 0) return;
+  const int lane = threadIdx.x & 31;
+  // Warps take 32 queue entries at a time from a shared counter, so warps
+  // whose molecules are lost early take more and no CTA waits on a partial
+  // second wave.  A CTA that gets nothing leaves before staging the table.
+  auto fetch = [&]() {
+    unsigned b = 0;
+    if (lane == 0) b = atomicAdd(Qin.head, 32u);
+    return __shfl_sync(kFull, b, 0);
+  };
+  unsigned base = fetch();
   tally_init(S);
+  if (!__syncthreads_or(base < n_in)) return;
   if (!k64 && kStaged)
     for (int k = threadIdx.x; k < L.n_int; k += blockDim.x) s_tab[k] = __ldg(L.q + k);
   __syncthreads();
 
   const ctraj_element& e = P.el[li];
   const bool classic = e.scheme == CTRAJ_RK4_CLASSIC;
-  const int lane = threadIdx.x & 31;
   unsigned long long steps = 0, lsteps = 0, band = 0, bad = 0, range = 0, rerr = 0;
-  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
-  for (int64_t base = int64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31); base < n_in; base += stride) {
-    const int64_t idx = base + lane;
+  for (; base < n_in; base = fetch()) {
+    const unsigned idx = base + lane;
     M m;
     LensStep st, nst;
     st.n_done = 0;
@@ -185,7 +197,7 @@ __global__ void __launch_bounds__(kThreads) k_lens_chunk(const __grid_constant__
     float dt = 0.f, hdt = 0.f, c2 = 0.f, dt6 = 0.f, dt26 = 0.f;
     int64_t n0 = 0;
     if (idx < n_in) {
-      m.load(Qin, unsigned(idx), P, st);
+      m.load_state(Qin, idx, P, st);
       n0 = st.n_done;
       dt = float(st.dt);
       hdt = 0.5f * dt;
@@ -212,6 +224,8 @@ __global__ void __launch_bounds__(kThreads) k_lens_chunk(const __grid_constant__
       }
       if ((k & 15) == 15 && !__any_sync(kFull, phase == kRun)) break;
     }
+    asm volatile("" ::: "memory");  // keep the loads below after the loop (register pressure)
+    if (idx < n_in) m.load_rest(Qin, idx, st);
     lsteps += unsigned(st.n_done - n0);
     int label = kNone;
     bool enter = false;

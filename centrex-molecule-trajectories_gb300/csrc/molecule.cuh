@@ -375,13 +375,14 @@ struct Mol64 {
     Q.lens_dt[s] = st.dt; Q.n_done[s] = int32_t(st.n_done); Q.n_total[s] = int32_t(st.n_total);
   }
   // The stored acceleration is not carried: the next RK4 step recomputes it.
-  __device__ void load(const Queue& Q, unsigned s, const Plan& P, LensStep& st) {
+  __device__ void load_state(const Queue& Q, unsigned s, const Plan& P, LensStep& st) {
     x[0] = Q.dx[s]; x[1] = Q.dy[s]; x[2] = Q.dz[s];
     v[0] = Q.dvx[s]; v[1] = Q.dvy[s]; v[2] = Q.dvz[s];
     t = Q.dt[s]; margin = Q.margin[s]; rows = Q.rows[s]; id = Q.id[s];
     a[0] = 0.0; a[1] = -P.g; a[2] = 0.0;
     st.dt = Q.lens_dt[s]; st.n_done = Q.n_done[s]; st.n_total = Q.n_total[s];
   }
+  __device__ void load_rest(const Queue&, unsigned, LensStep&) {}
 };
 
 // ===========================================================================
@@ -595,17 +596,26 @@ struct Mol32 {
     Q.rows[s] = rows; Q.id[s] = id;
     if (kOut) Q.margin[s] = margin;
   }
-  // The stored acceleration is not carried: the next RK4 step recomputes it.
-  __device__ void load(const Queue& Q, unsigned s, const Plan& P, LensStep& st) {
-    x = Q.x[s]; y = Q.y[s]; vx = Q.vx[s]; vy = Q.vy[s]; vz = Q.vz[s]; t = Q.t[s];
+  // What the RK4 loop needs; the stored acceleration is not carried (the next
+  // RK4 step recomputes it).
+  __device__ void load_state(const Queue& Q, unsigned s, const Plan& P, LensStep& st) {
+    x = Q.x[s]; y = Q.y[s]; vx = Q.vx[s]; vy = Q.vy[s];
     cx = Q.cx[s]; cy = Q.cy[s]; cvx = Q.cvx[s]; cvy = Q.cvy[s];
-    st.dt = Q.lens_dt[s]; st.snap = double(Q.snap[s]);
+    st.dt = Q.lens_dt[s];
     st.n_done = Q.n_done[s]; st.n_total = Q.n_total[s];
-    rows = Q.rows[s]; id = Q.id[s];
-    inv_vz = __frcp_rn(vz);
     ax = 0.0f;
     ay = -P.gf;
-    margin = kOut ? float(Q.margin[s]) : INFINITY;
+    margin = INFINITY;  // edges seen during this chunk; merged with the queued value below
+  }
+  // The rest, read after the RK4 loop so it does not occupy registers during it.
+  __device__ void load_rest(const Queue& Q, unsigned s, LensStep& st) {
+    vz = Q.vz[s];
+    t = Q.t[s];
+    st.snap = double(Q.snap[s]);
+    rows = Q.rows[s];
+    id = Q.id[s];
+    inv_vz = __frcp_rn(vz);
+    if (kOut) margin = fminf(margin, float(Q.margin[s]));
   }
 };
 

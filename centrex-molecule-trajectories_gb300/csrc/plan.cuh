@@ -135,9 +135,13 @@ struct Queue {
   int32_t* id;
   int32_t* n_done;
   int32_t* n_total;
-  unsigned int* count;  // entries written
+  unsigned int* count;      // entries written
   unsigned int* max_steps;  // largest n_total - n_done written (sizes the chunk loop)
+  unsigned int* head;       // entries taken by the warps of the kernel reading the queue
 };
+
+// Queue control words: count, max_steps, head, (unused) -- 16 bytes per queue.
+constexpr int kCtlWords = 4;
 
 constexpr int kLabelDetected = -1;  // counts[n_labels]
 constexpr int kQueued = -2;         // waiting at a lens entrance
