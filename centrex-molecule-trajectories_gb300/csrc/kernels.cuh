@@ -169,15 +169,18 @@ __global__ void __launch_bounds__(kLensThreads, 2) k_lens_chunk(const __grid_con
   const unsigned n_in = *(volatile unsigned*)Qin.count;
   if (n_in == 0) return;
   const int lane = threadIdx.x & 31;
-  // Warps take 32 queue entries at a time from a shared counter, so warps
-  // whose molecules are lost early take more and no CTA waits on a partial
-  // second wave.  A CTA that gets nothing leaves before staging the table.
+  // Each warp's first batch of 32 entries is fixed, interleaved across CTAs
+  // (batch k -> CTA k mod grid) so that a short queue spreads over all SMs;
+  // later batches come from a shared counter, so warps whose molecules are
+  // lost early take more and no CTA waits on a partial second wave.  A CTA
+  // that gets nothing leaves before staging the table.
+  const unsigned static_entries = gridDim.x * (blockDim.x / 32) * 32u;
   auto fetch = [&]() {
     unsigned b = 0;
     if (lane == 0) b = atomicAdd(Qin.head, 32u);
-    return __shfl_sync(kFull, b, 0);
+    return static_entries + __shfl_sync(kFull, b, 0);
   };
-  unsigned base = fetch();
+  unsigned base = ((threadIdx.x >> 5) * gridDim.x + blockIdx.x) * 32u;
   tally_init(S);
   if (!__syncthreads_or(base < n_in)) return;
   if (!k64 && kStaged)
