@@ -13,6 +13,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -693,3 +694,307 @@ int ctraj_record(ctraj_context* c, const ctraj_run_args* a, const int64_t* ids, 
 }
 
 }  // extern "C"
+
+// ============================================================================
+// Allocation-free run (ctraj_run_noalloc): the same kernels as ctraj_run, with
+// every piece of scratch in one statically sized device array.
+// ============================================================================
+namespace ctraj {
+namespace {
+
+// The scratch array.  Each GPU that loads this library holds it until exit.
+// Host code must not use the name as a device address: it is a host-side
+// stand-in; noalloc_scratch() looks up the real address per device.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[CTRAJ_NOALLOC_SCRATCH_BYTES];
+
+// Layout: control words (queue counters, tallies, stats) | per-chunk queue
+// counters | FP32 lens tables | three lens queues.
+constexpr size_t kNaCtl = 0;
+constexpr size_t kNaChunk = 4096;
+constexpr size_t kNaTables = kNaChunk + size_t(kMaxChunks) * kCtlWords * sizeof(unsigned);
+constexpr size_t kNaQueues = kNaTables + size_t(CTRAJ_NOALLOC_MAX_INTERVALS) * sizeof(float4);
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[64] = {};
+
+// Device address of the scratch array on the current device, looked up once
+// per device with that device current (cudaGetSymbolAddress).
+int noalloc_scratch(char** out) {
+  int dev = 0;
+  CT_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(CTRAJ_EINVAL, "device %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(CTRAJ_ECUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = static_cast<char*>(g_noalloc_ptr[dev]);
+  return CTRAJ_OK;
+}
+
+int noalloc_check_table(const ctraj_force_table& t, int k) {
+  if (t.n_knots < 2 || !t.knots) return fail(CTRAJ_EINVAL, "table %d needs at least 2 knots", k);
+  if (t.kind == CTRAJ_TABLE_STARK_SPLINE && !t.coef) return fail(CTRAJ_EINVAL, "table %d: no coef", k);
+  if (t.kind == CTRAJ_TABLE_RADIAL_LINEAR && !t.values) return fail(CTRAJ_EINVAL, "table %d: no values", k);
+  if (t.kind != CTRAJ_TABLE_STARK_SPLINE && t.kind != CTRAJ_TABLE_RADIAL_LINEAR)
+    return fail(CTRAJ_EINVAL, "table %d: unknown kind %d", k, t.kind);
+  const double h = (t.knots[t.n_knots - 1] - t.knots[0]) / double(t.n_knots - 1);
+  if (!(h > 0)) return fail(CTRAJ_EINVAL, "table %d: knots must ascend", k);
+  for (int j = 1; j < t.n_knots; ++j)
+    if (std::fabs((t.knots[j] - t.knots[j - 1]) - h) > 1e-6 * h)
+      return fail(CTRAJ_EINVAL, "table %d: knots must be uniformly spaced", k);
+  return CTRAJ_OK;
+}
+
+// Plan and FP32 lens tables (written into the scratch through a small stack
+// buffer: nothing is allocated on the host heap either).
+int noalloc_plan(const ctraj_element* el, int n_el, int n_labels, const ctraj_force_table* tabs,
+                 int n_tab, const ctraj_run_args* a, float4* dev_tables, cudaStream_t s, Plan& P) {
+  std::memset(&P, 0, sizeof P);
+  P.n_el = n_el;
+  P.n_labels = n_labels;
+  P.first_lens = n_el;
+  P.g = a->g;
+  P.gf = float(a->g);
+  size_t offset = 0;
+  float4 buf[256];
+  for (int i = 0; i < n_el; ++i) {
+    const ctraj_element& e = el[i];
+    P.el[i] = e;
+    ElemF& f = P.ef[i];
+    f.gap = i > 0 ? float(e.z0 - el[i - 1].z1) : 0.f;
+    f.len = float(e.z1 - e.z0);
+    if (e.type == CTRAJ_CIRCULAR_APERTURE || e.type == CTRAJ_ELECTROSTATIC_LENS) {
+      const double h = e.p[0] * 0.5;
+      f.c[0] = float(h * h);
+      f.c[1] = float(h);
+    } else if (e.type == CTRAJ_RECTANGULAR_APERTURE) {
+      for (int k = 0; k < 4; ++k) f.c[k] = float(e.p[k]);
+    } else if (e.type == CTRAJ_FIELD_PLATES) {
+      f.c[0] = float(e.p[0]);
+      f.c[1] = float(e.p[1]);
+    }
+    if (e.type != CTRAJ_ELECTROSTATIC_LENS) continue;
+    if (e.table < 0 || e.table >= n_tab) return fail(CTRAJ_ESTATE, "lens element %d uses table %d, not given", i, e.table);
+    const ctraj_force_table& t = tabs[e.table];
+    if (t.kind == CTRAJ_TABLE_STARK_SPLINE && e.field_order != 1 && e.field_order != 2)
+      return fail(CTRAJ_EINVAL, "lens element %d: field_order must be 1 or 2", i);
+    if (P.first_lens == n_el) P.first_lens = i;
+    const int n_int = t.n_knots - 1;
+    if (offset + size_t(n_int) > size_t(CTRAJ_NOALLOC_MAX_INTERVALS))
+      return fail(CTRAJ_EINVAL, "lens tables exceed %d intervals", CTRAJ_NOALLOC_MAX_INTERVALS);
+    const double x0 = t.knots[0], h = (t.knots[t.n_knots - 1] - t.knots[0]) / double(n_int);
+    const double alpha = e.p[6], mass = e.p[5];
+    const double kappa = e.field_order == 1 ? alpha / mass : 2.0 * alpha / mass;
+    for (int j0 = 0; j0 < n_int; j0 += 256) {
+      const int m = std::min(256, n_int - j0);
+      for (int j = 0; j < m; ++j) {
+        const int k = j0 + j;
+        if (t.kind == CTRAJ_TABLE_RADIAL_LINEAR) {
+          buf[j] = make_float4(float(t.values[k]), float(t.values[k + 1] - t.values[k]), 0.f, 0.f);
+        } else {
+          const double* ck = &t.coef[size_t(k) * 4];
+          buf[j] = make_float4(float(-kappa * ck[2]), float(-kappa * 2.0 * ck[1] * h),
+                               float(-kappa * 3.0 * ck[0] * h * h), 0.f);
+        }
+      }
+      // pageable source: the call returns once buf has been staged, so buf can be refilled
+      CT_CUDA(cudaMemcpyAsync(dev_tables + offset + j0, buf, m * sizeof(float4), cudaMemcpyHostToDevice, s));
+    }
+    LensF& L = P.lf[i];
+    L.q = dev_tables + offset;
+    L.n_int = n_int;
+    L.n_smem = n_int <= kMaxStagedIntervals ? n_int : 0;
+    if (t.kind == CTRAJ_TABLE_RADIAL_LINEAR) {
+      L.force = kForceRadial;
+      L.beta = float(1.0 / h);
+      L.s0 = float(x0 / h);
+      L.r_max = float(t.knots[t.n_knots - 1]);
+    } else {
+      L.force = e.field_order == 1 ? kForceStark1 : kForceStark2;
+      L.beta = float(alpha / h);
+      L.s0 = float(x0 / h);
+      L.r_max = INFINITY;
+    }
+    offset += size_t(n_int);
+  }
+  return CTRAJ_OK;
+}
+
+// The launch sequence of launch_all (FP32), on the scratch's queues.
+template <bool kOut>
+int noalloc_launch(const Plan& P, const RunDev& R, Queue* q, unsigned* chunk_ctl, cudaStream_t s,
+                   int* launches, unsigned* leftover) {
+  int dev = 0, sms = 0;
+  CT_CUDA(cudaGetDevice(&dev));
+  CT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int64_t n = R.n;
+  if (n > 0) {
+    auto kf = k_front<Mol32<kOut, false>, kOut>;
+    const int bps = blocks_per_sm(kf, kThreads, 0);
+    const int grid = int(std::min<int64_t>((n + kThreads - 1) / kThreads, int64_t(bps) * sms * 4));
+    kf<<<grid, kThreads, 0, s>>>(P, R, q[0]);
+    CT_CUDA(cudaGetLastError());
+    ++*launches;
+  }
+  int cur = 0, alt = 1, nxt = 2;
+  for (int i = 0; i < P.n_el && n > 0; ++i) {
+    if (P.el[i].type != CTRAJ_ELECTROSTATIC_LENS) continue;
+    unsigned head[2] = {0, 0};  // count, largest remaining step count
+    CT_CUDA(cudaMemcpyAsync(head, q[cur].count, sizeof head, cudaMemcpyDeviceToHost, s));
+    CT_CUDA(cudaStreamSynchronize(s));
+    if (head[0] == 0) break;
+    CT_CUDA(cudaMemsetAsync(q[nxt].count, 0, kCtlWords * sizeof(unsigned), s));
+    const bool staged = P.lf[i].n_smem > 0;
+    const size_t smem = staged ? size_t(P.lf[i].n_int) * sizeof(float4) : 0;
+    LensKernel kl = lens_kernel<false, kOut>(P.lf[i].force, staged);
+    CT_CUDA(cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    const int64_t per_launch = int64_t(blocks_per_sm(kl, kLensThreads, smem)) * sms;
+    const int grid =
+        int(std::max<int64_t>(1, std::min<int64_t>(per_launch, (head[0] + kLensThreads - 1) / kLensThreads)));
+    int lens_chunks[kMaxChunks];
+    int nc = 0;
+    for (int64_t done = 0, len = 64; done < int64_t(head[1]) || nc == 0; len = std::min<int64_t>(2 * len, 1024)) {
+      if (nc == kMaxChunks) return fail(CTRAJ_ESTEPS, "lens element %d needs more than %d chunks", i, kMaxChunks);
+      lens_chunks[nc++] = int(len);
+      done += len;
+    }
+    CT_CUDA(cudaMemsetAsync(chunk_ctl, 0, size_t(nc) * kCtlWords * sizeof(unsigned), s));
+    const LensArgs la = lens_args(P, i, true);
+    Queue in = q[cur];
+    for (int k = 0; k < nc; ++k) {
+      Queue out = q[alt];
+      out.count = chunk_ctl + size_t(k) * kCtlWords;
+      out.max_steps = out.count + 1;
+      out.head = out.count + 2;
+      kl<<<grid, kLensThreads, smem, s>>>(P, R, i, in, out, q[nxt], lens_chunks[k], la);
+      CT_CUDA(cudaGetLastError());
+      ++*launches;
+      in = out;
+      std::swap(cur, alt);
+    }
+    unsigned left = 0;
+    CT_CUDA(cudaMemcpyAsync(&left, in.count, sizeof left, cudaMemcpyDeviceToHost, s));
+    CT_CUDA(cudaStreamSynchronize(s));
+    *leftover += left;
+    std::swap(cur, nxt);
+  }
+  return CTRAJ_OK;
+}
+
+}  // namespace
+}  // namespace ctraj
+
+extern "C" int ctraj_run_noalloc(const ctraj_element* el, int32_t n_el, int32_t n_labels,
+                                 const ctraj_force_table* tabs, int32_t n_tab,
+                                 const ctraj_run_args* a, void* stream, ctraj_run_stats* stats) {
+  if (!a) return fail(CTRAJ_EINVAL, "args is NULL");
+  if (a->precision != 32) return fail(CTRAJ_EINVAL, "ctraj_run_noalloc supports precision 32 only");
+  if (a->n < 0 || a->n > CTRAJ_NOALLOC_MAX_MOLECULES)
+    return fail(CTRAJ_EINVAL, "n = %lld: ctraj_run_noalloc takes at most %d molecules per call",
+                (long long)a->n, CTRAJ_NOALLOC_MAX_MOLECULES);
+  if (a->ic_mode == CTRAJ_IC_HOST) return fail(CTRAJ_EINVAL, "ctraj_run_noalloc needs device-memory initial conditions");
+  if (a->ic_mode == CTRAJ_IC_DEVICE_DRAW) {
+    if (a->xdist.kind != CTRAJ_DIST_GAUSSIAN_POSITION && a->xdist.kind != CTRAJ_DIST_DISC_POSITION)
+      return fail(CTRAJ_EINVAL, "unknown position distribution kind %d", a->xdist.kind);
+    if (a->vdist.kind != CTRAJ_DIST_GAUSSIAN_VELOCITY)
+      return fail(CTRAJ_EINVAL, "unknown velocity distribution kind %d", a->vdist.kind);
+  } else if (a->ic_mode == CTRAJ_IC_DEVICE) {
+    if (!a->ics && a->n > 0) return fail(CTRAJ_EINVAL, "ics is NULL");
+  } else {
+    return fail(CTRAJ_EINVAL, "unknown ic_mode %d", a->ic_mode);
+  }
+  if (a->out_mode == CTRAJ_OUT_HOST) return fail(CTRAJ_EINVAL, "ctraj_run_noalloc writes per-molecule outputs to device memory only");
+  if (a->out_mode != CTRAJ_OUT_NONE && a->out_mode != CTRAJ_OUT_DEVICE) return fail(CTRAJ_EINVAL, "bad out_mode");
+  if (!a->counts) return fail(CTRAJ_EINVAL, "counts is NULL");
+  if (n_el < 0 || n_el > CTRAJ_MAX_ELEMENTS || (n_el > 0 && !el)) return fail(CTRAJ_EINVAL, "bad elements");
+  if (n_labels < 0 || n_labels > CTRAJ_MAX_LABELS) return fail(CTRAJ_EINVAL, "n_labels %d out of range", n_labels);
+  if (n_tab < 0 || n_tab > CTRAJ_MAX_TABLES || (n_tab > 0 && !tabs)) return fail(CTRAJ_EINVAL, "bad tables");
+  for (int i = 0; i < n_el; ++i) {
+    const ctraj_element& e = el[i];
+    if (e.type < CTRAJ_CIRCULAR_APERTURE || e.type > CTRAJ_ELECTROSTATIC_LENS)
+      return fail(CTRAJ_EINVAL, "element %d: unknown type %d", i, e.type);
+    if (e.label < -1 || e.label >= n_labels || e.label_inside < -1 || e.label_inside >= n_labels)
+      return fail(CTRAJ_EINVAL, "element %d: label out of range", i);
+    if (i > 0 && e.z0 < el[i - 1].z0) return fail(CTRAJ_EINVAL, "elements are not sorted by z0 (element %d)", i);
+  }
+  for (int k = 0; k < n_tab; ++k) {
+    int st = noalloc_check_table(tabs[k], k);
+    if (st) return st;
+  }
+  char* scratch = nullptr;
+  int st = noalloc_scratch(&scratch);
+  if (st) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t cap = CTRAJ_NOALLOC_MAX_MOLECULES;
+  const size_t qb = queue_bytes(cap, 32);
+  if (kNaQueues + 3 * qb > CTRAJ_NOALLOC_SCRATCH_BYTES) return fail(CTRAJ_ENOMEM, "scratch layout too large");
+  Plan P;
+  if ((st = noalloc_plan(el, n_el, n_labels, tabs, n_tab, a, reinterpret_cast<float4*>(scratch + kNaTables), s, P)))
+    return st;
+  unsigned* ctl = reinterpret_cast<unsigned*>(scratch + kNaCtl);
+  unsigned long long* counts = reinterpret_cast<unsigned long long*>(scratch + kNaCtl + 256);
+  unsigned long long* dstats = reinterpret_cast<unsigned long long*>(scratch + kNaCtl + 256 + 8 * (CTRAJ_MAX_LABELS + 1));
+  // queues are handed over in DevBuf form so the same layout code places the arrays
+  Queue q[3];
+  for (int k = 0; k < 3; ++k) {
+    DevBuf view;
+    view.p = scratch + kNaQueues + size_t(k) * qb;
+    view.bytes = qb;
+    layout_queue(&view, cap, 32, ctl + kCtlWords * k, &q[k]);
+    view.p = nullptr;  // a view: nothing to free
+  }
+  CT_CUDA(cudaMemsetAsync(scratch + kNaCtl, 0, 4096, s));  // counters, tallies and stats start at zero
+  RunDev R;
+  std::memset(&R, 0, sizeof R);
+  R.n = a->n;
+  R.seed = a->seed;
+  R.offset = a->offset;
+  R.ic_mode = a->ic_mode;
+  R.xd = a->xdist;
+  R.vd = a->vdist;
+  R.ics = a->ics;
+  if (a->ic_mode == CTRAJ_IC_DEVICE_DRAW) {
+    const double zd = a->xdist.kind == CTRAJ_DIST_DISC_POSITION ? a->xdist.p[1] : a->xdist.p[2];
+    R.gap0f = P.n_el > 0 ? float(P.el[0].z0 - zd) : 0.f;
+  }
+  R.counts = counts;
+  R.stats = dstats;
+  const bool out = a->out_mode == CTRAJ_OUT_DEVICE;
+  if (out) {
+    R.out_label = a->out_label;
+    R.out_rows = a->out_rows;
+    R.out_margin = a->out_margin;
+    R.out_final = a->out_final;
+  }
+  int launches = 0;
+  unsigned leftover = 0;
+  unsigned* chunk_ctl = reinterpret_cast<unsigned*>(scratch + kNaChunk);
+  st = out ? noalloc_launch<true>(P, R, q, chunk_ctl, s, &launches, &leftover)
+           : noalloc_launch<false>(P, R, q, chunk_ctl, s, &launches, &leftover);
+  if (st) return st;
+  unsigned long long hc[CTRAJ_MAX_LABELS + 1], hs[kStatCount];
+  CT_CUDA(cudaMemcpyAsync(hc, counts, sizeof hc, cudaMemcpyDeviceToHost, s));
+  CT_CUDA(cudaMemcpyAsync(hs, dstats, sizeof hs, cudaMemcpyDeviceToHost, s));
+  CT_CUDA(cudaStreamSynchronize(s));
+  if (leftover) return fail(CTRAJ_ECUDA, "internal error: %u molecules left inside a lens", leftover);
+  for (int k = 0; k <= n_labels; ++k) a->counts[k] = int64_t(hc[k]);
+  if (stats) {
+    std::memset(stats, 0, sizeof *stats);
+    stats->molecules = a->n;
+    stats->molecule_steps = int64_t(hs[kStatSteps]);
+    stats->lens_steps = int64_t(hs[kStatLensSteps]);
+    stats->edge_band = out ? int64_t(hs[kStatEdgeBand]) : -1;
+    stats->table_range = int64_t(hs[kStatTableRange]);
+    stats->bad_steps = int64_t(hs[kStatBadSteps]);
+    stats->kernels = launches;
+  }
+  if (hs[kStatRangeError])
+    return fail(CTRAJ_ERANGE, "%llu molecules looked up the lens table above its last knot", hs[kStatRangeError]);
+  if (hs[kStatBadSteps])
+    return fail(CTRAJ_ESTEPS, "%llu molecules have a non-finite or oversize lens step count", hs[kStatBadSteps]);
+  return CTRAJ_OK;
+}

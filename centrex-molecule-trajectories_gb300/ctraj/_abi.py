@@ -148,7 +148,14 @@ SIGNATURES = {
     "ctraj_run": (ctypes.c_int, [_P, ctypes.POINTER(RunArgs), ctypes.POINTER(RunStats)]),
     "ctraj_record": (ctypes.c_int, [_P, ctypes.POINTER(RunArgs), _P, ctypes.c_int64, ctypes.c_int32,
                                     ctypes.c_int32, _P, _P]),
+    "ctraj_run_noalloc": (ctypes.c_int, [ctypes.POINTER(Element), ctypes.c_int32, ctypes.c_int32,
+                                         ctypes.POINTER(ForceTable), ctypes.c_int32,
+                                         ctypes.POINTER(RunArgs), _P, ctypes.POINTER(RunStats)]),
 }
+
+# ctraj_run_noalloc limits (include/ctraj.h)
+NOALLOC_MAX_MOLECULES = 131072
+NOALLOC_SCRATCH_BYTES = 32 << 20
 
 
 class CtrajError(RuntimeError):

@@ -240,6 +240,41 @@ int ctraj_record(ctraj_context* ctx, const ctraj_run_args* args,
                  const int64_t* ids, int64_t n_ids, int32_t stride,
                  int32_t max_rows, double* rows, int32_t* row_count);
 
+/*
+ * Allocation-free run.  This entry point has no counterpart in the reference.
+ *
+ * ctraj_run_noalloc propagates molecules exactly as ctraj_run does (same
+ * kernels, same results molecule by molecule) but needs no context and
+ * allocates no device memory: its scratch (lens queues, queue counters,
+ * tallies, the FP32 lens tables) lives in one file-scope __device__ array of
+ * CTRAJ_NOALLOC_SCRATCH_BYTES that every GPU which loads libctraj.so holds
+ * until the process exits.  It is for callers that cannot allocate device
+ * memory while they run: an application that hands this library a fixed
+ * device-memory budget at start-up and owns every allocation itself, or a
+ * service that must not call cudaMalloc/cudaFree on its request path because
+ * those calls synchronize the whole device and stall the other work on it.
+ *
+ * Limits: precision 32 only; at most CTRAJ_NOALLOC_MAX_MOLECULES molecules per
+ * call (larger n is rejected with CTRAJ_EINVAL); initial conditions drawn on
+ * the device or given in device memory (CTRAJ_IC_DEVICE); per-molecule outputs,
+ * if any, in device memory (CTRAJ_OUT_DEVICE); counts are written to the host
+ * array args->counts.  Runs on the calling thread's current device and on
+ * `cuda_stream` (NULL = the legacy default stream), and returns after the
+ * counts are on the host.
+ *
+ * The first call on a device looks up the array's device address with that
+ * device current; make that first call before capturing any stream.  All
+ * calls share the one array and each overwrites it, so calls that overlap on
+ * the GPU (from two host threads, or on two streams) race: serialize them.
+ */
+#define CTRAJ_NOALLOC_MAX_MOLECULES 131072
+#define CTRAJ_NOALLOC_MAX_INTERVALS 16384 /* FP32 table intervals over all lenses */
+#define CTRAJ_NOALLOC_SCRATCH_BYTES (32u << 20)
+int ctraj_run_noalloc(const ctraj_element* elements, int32_t n_elements,
+                      int32_t n_labels, const ctraj_force_table* tables,
+                      int32_t n_tables, const ctraj_run_args* args,
+                      void* cuda_stream, ctraj_run_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif
