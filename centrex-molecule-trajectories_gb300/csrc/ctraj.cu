@@ -103,7 +103,9 @@ struct ctraj_context {
   unsigned* host_max = nullptr; // pinned: largest remaining lens step count of a queue
   DevBuf chunk_ctl;             // (count, max_steps) of the queue each lens chunk writes
   int chunk = 64;               // RK4 steps of the first lens chunk (compaction interval)
-  int chunk_max = 1024;         // chunks double in length up to this
+  int chunk_growth = 200;       // percent: each chunk's length relative to the previous
+  int chunk_max = 1024;         // longest chunk
+  int front_waves = 4;          // k_front grid in units of resident CTAs
   bool timing = false;
   // before front, after front, before the first lens chunk, after the last one
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -320,7 +322,7 @@ int launch_all(ctraj_context* c, const Plan& P, const RunDev& R, Queue* q, int* 
     auto kf = k_front<MolT, kOut>;
     int bps = blocks_per_sm(kf, kThreads, 0);
     int64_t want = (n + kThreads - 1) / kThreads;
-    int grid = int(std::min<int64_t>(want, int64_t(bps) * c->sm_count * 4));
+    int grid = int(std::min<int64_t>(want, int64_t(bps) * c->sm_count * c->front_waves));
     kf<<<grid, kThreads, 0, s>>>(P, R, q[0]);
     CT_CUDA(cudaGetLastError());
     ++*launches;
@@ -349,12 +351,13 @@ int launch_all(ctraj_context* c, const Plan& P, const RunDev& R, Queue* q, int* 
     // and launches are few in the long tail of survivors
     std::vector<int> lens_chunks;
     for (int64_t done = 0, len = c->chunk; done < int64_t(max_steps) || lens_chunks.empty();) {
+      if (lens_chunks.size() == size_t(kMaxChunks))
+        return fail(CTRAJ_ESTEPS, "lens element %d needs more than %d chunks", i, kMaxChunks);
       lens_chunks.push_back(int(len));
       done += len;
-      len = std::min<int64_t>(2 * len, c->chunk_max);
+      len = std::min<int64_t>(std::max<int64_t>(len + 1, len * c->chunk_growth / 100), c->chunk_max);
     }
     const size_t nc = lens_chunks.size();
-    if (nc > kMaxChunks) return fail(CTRAJ_ESTEPS, "lens element %d needs %zu chunks (max %d)", i, nc, kMaxChunks);
     CT_CUDA(cudaMemsetAsync(c->chunk_ctl.p, 0, nc * kCtlWords * sizeof(unsigned), s));
     const LensArgs la = lens_args(P, i, !k64);
     Queue in = q[cur];
@@ -501,6 +504,28 @@ int ctraj_destroy(ctraj_context* c) {
   if (c->host_max) cudaFreeHost(c->host_max);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
+  return CTRAJ_OK;
+}
+
+int ctraj_set_tuning(ctraj_context* c, const ctraj_tuning* t) {
+  if (!c || !t) return fail(CTRAJ_EINVAL, "NULL argument");
+  if (t->chunk_first < 1 || t->chunk_max < t->chunk_first || t->chunk_max > 1000000 ||
+      t->chunk_growth < 100 || t->chunk_growth > 1000 || t->front_waves < 1 || t->front_waves > 64)
+    return fail(CTRAJ_EINVAL, "tuning out of range (chunk_first %d, chunk_growth %d, chunk_max %d, front_waves %d)",
+                t->chunk_first, t->chunk_growth, t->chunk_max, t->front_waves);
+  c->chunk = t->chunk_first;
+  c->chunk_growth = t->chunk_growth;
+  c->chunk_max = t->chunk_max;
+  c->front_waves = t->front_waves;
+  return CTRAJ_OK;
+}
+
+int ctraj_get_tuning(ctraj_context* c, ctraj_tuning* t) {
+  if (!c || !t) return fail(CTRAJ_EINVAL, "NULL argument");
+  t->chunk_first = c->chunk;
+  t->chunk_growth = c->chunk_growth;
+  t->chunk_max = c->chunk_max;
+  t->front_waves = c->front_waves;
   return CTRAJ_OK;
 }
 

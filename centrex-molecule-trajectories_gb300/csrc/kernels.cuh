@@ -108,14 +108,32 @@ __device__ __forceinline__ bool enter_lens(M& m, const Plan& P, int li, LensStep
   return true;
 }
 
+// FP32 runs leave the exact step setup (three double divisions) of a molecule
+// entering the first lens to the first lens chunk, whose warps are full; here
+// only n_total = -1 ("pending") and a float upper bound on the step count,
+// which sizes the chunk loop.
+template <class M>
+__device__ __forceinline__ bool enter_lens_front(M& m, const Plan& P, int li, LensStep& st) {
+  if (!M::kDeferLensSetup) return enter_lens(m, P, li, st);
+  const ctraj_element& e = P.el[li];
+  const float dz = e.step_mode == CTRAJ_STEP_DT ? float(m.vel_z()) * float(e.p[2]) : float(e.p[1]);
+  const float bound = fabsf(float(e.p[7]) / dz);
+  st.n_done = 0;
+  st.n_total = -1;
+  // NaN / inf / oversize: the exact setup in the first chunk rejects the molecule
+  st.bound = bound < float(CTRAJ_MAX_LENS_STEPS) ? int(bound) + 2 : int(CTRAJ_MAX_LENS_STEPS) + 1;
+  return true;
+}
+
 // Append the lanes with push == true to Q and raise Q's largest remaining
 // step count (all lanes call).
 template <class M>
 __device__ __forceinline__ void push_lens(const Queue& Q, bool push, const M& m, const LensStep& st) {
   const unsigned slot = queue_slot(push, Q.count);
   if (push) m.store(Q, slot, st);
-  const unsigned rem = __reduce_max_sync(kFull, push ? unsigned(st.n_total - st.n_done) : 0u);
-  if ((threadIdx.x & 31) == 0 && rem) atomicMax(Q.max_steps, rem);
+  const unsigned rem = push ? unsigned(st.n_total < 0 ? st.bound : st.n_total - st.n_done) : 0u;
+  const unsigned wmax = __reduce_max_sync(kFull, rem);
+  if ((threadIdx.x & 31) == 0 && wmax) atomicMax(Q.max_steps, wmax);
 }
 
 // ---------------------------------------------------------------------------
@@ -137,7 +155,7 @@ __global__ void __launch_bounds__(kThreads) k_front(const __grid_constant__ Plan
       m.init(P, R, i);
       int lens_at = -1;
       label = walk(m, P, 0, &lens_at);
-      if (label == kQueued && !enter_lens(m, P, lens_at, st)) {
+      if (label == kQueued && !enter_lens_front(m, P, lens_at, st)) {
         label = P.el[lens_at].label_inside;
         ++bad;
       }
@@ -157,7 +175,7 @@ __global__ void __launch_bounds__(kThreads) k_front(const __grid_constant__ Plan
 }
 
 // ---------------------------------------------------------------------------
-enum : int { kIdle = 0, kRun = 1, kLost = 2, kExit = 3 };
+enum : int { kIdle = 0, kRun = 1, kLost = 2, kExit = 3, kBad = 4 };
 
 template <class M, bool kOut, int F, bool k64, bool kStaged>
 __global__ void __launch_bounds__(kLensThreads, 2) k_lens_chunk(const __grid_constant__ Plan P, const RunDev R,
@@ -198,16 +216,23 @@ __global__ void __launch_bounds__(kLensThreads, 2) k_lens_chunk(const __grid_con
     int phase = kIdle;
     unsigned flags = 0;
     float dt = 0.f, hdt = 0.f, c2 = 0.f, dt6 = 0.f, dt26 = 0.f;
-    int64_t n0 = 0;
+    int n0 = 0;
+    bool fresh = false;
     if (idx < n_in) {
       m.load_state(Qin, idx, P, st);
+      bool ok = true;
+      fresh = st.n_total < 0;
+      if (fresh) {  // step setup deferred by the front kernel
+        m.load_vz(Qin, idx);
+        ok = enter_lens(m, P, li, st);
+      }
       n0 = st.n_done;
       dt = float(st.dt);
       hdt = 0.5f * dt;
       c2 = classic ? hdt : dt;
       dt6 = dt * (1.0f / 6.0f);
       dt26 = float(st.dt * st.dt / 6.0);
-      phase = st.n_done < st.n_total ? kRun : kExit;
+      phase = !ok ? kBad : (st.n_done < st.n_total ? kRun : kExit);
     }
     for (int k = 0; k < chunk; ++k) {
       if (phase == kRun) {
@@ -228,11 +253,16 @@ __global__ void __launch_bounds__(kLensThreads, 2) k_lens_chunk(const __grid_con
       if ((k & 15) == 15 && !__any_sync(kFull, phase == kRun)) break;
     }
     asm volatile("" ::: "memory");  // keep the loads below after the loop (register pressure)
-    if (idx < n_in) m.load_rest(Qin, idx, st);
+    if (idx < n_in) m.load_rest(Qin, idx, st, !fresh);
     lsteps += unsigned(st.n_done - n0);
     int label = kNone;
     bool enter = false;
-    if (phase == kLost || phase == kExit) {
+    if (phase == kBad) {  // rint(L/dz) not usable: the reference raises here
+      label = e.label_inside;
+      ++bad;
+      steps += unsigned(m.rows);
+      write_outputs<M, kOut>(R, m, label);
+    } else if (phase == kLost || phase == kExit) {
       range += (flags & 1u) ? 1 : 0;
       rerr += (flags & 2u) ? 1 : 0;
       m.lens_end(P, li, st, phase == kLost);

@@ -144,8 +144,9 @@ __device__ __forceinline__ float wforce(float px, float py, const LensArgs& L, c
 
 // Per-molecule lens integration parameters (both precisions).
 struct LensStep {
-  int n_total;  // rint(L/dz), at most CTRAJ_MAX_LENS_STEPS
+  int n_total;  // rint(L/dz), at most CTRAJ_MAX_LENS_STEPS; -1 while the setup is pending
   int n_done;
+  int bound;    // upper bound on n_total while the setup is pending
   double dt;        // dz / vz
   double snap;      // FP32: exit-snap time (z1 - z0 - N dz) / vz
   double dz;
@@ -382,7 +383,9 @@ struct Mol64 {
     a[0] = 0.0; a[1] = -P.g; a[2] = 0.0;
     st.dt = Q.lens_dt[s]; st.n_done = Q.n_done[s]; st.n_total = Q.n_total[s];
   }
-  __device__ void load_rest(const Queue&, unsigned, LensStep&) {}
+  __device__ void load_vz(const Queue&, unsigned) {}
+  __device__ void load_rest(const Queue&, unsigned, LensStep&, bool) {}
+  static constexpr bool kDeferLensSetup = false;
 };
 
 // ===========================================================================
@@ -607,11 +610,14 @@ struct Mol32 {
     ay = -P.gf;
     margin = INFINITY;  // edges seen during this chunk; merged with the queued value below
   }
-  // The rest, read after the RK4 loop so it does not occupy registers during it.
-  __device__ void load_rest(const Queue& Q, unsigned s, LensStep& st) {
+  __device__ void load_vz(const Queue& Q, unsigned s) { vz = Q.vz[s]; }
+  static constexpr bool kDeferLensSetup = true;
+  // The rest, read after the RK4 loop so it does not occupy registers during
+  // it (the exit-snap time too, unless the setup was just done in this chunk).
+  __device__ void load_rest(const Queue& Q, unsigned s, LensStep& st, bool snap_from_queue) {
     vz = Q.vz[s];
     t = Q.t[s];
-    st.snap = double(Q.snap[s]);
+    if (snap_from_queue) st.snap = double(Q.snap[s]);
     rows = Q.rows[s];
     id = Q.id[s];
     inv_vz = __frcp_rn(vz);

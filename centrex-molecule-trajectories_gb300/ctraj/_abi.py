@@ -134,6 +134,15 @@ class RunStats(ctypes.Structure):
     ]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [
+        ("chunk_first", ctypes.c_int32),
+        ("chunk_growth", ctypes.c_int32),
+        ("chunk_max", ctypes.c_int32),
+        ("front_waves", ctypes.c_int32),
+    ]
+
+
 # Entry points declared in include/ctraj.h: name -> (restype, argtypes)
 _P = ctypes.c_void_p
 SIGNATURES = {
@@ -142,6 +151,8 @@ SIGNATURES = {
     "ctraj_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_P)]),
     "ctraj_destroy": (ctypes.c_int, [_P]),
     "ctraj_set_stream": (ctypes.c_int, [_P, _P]),
+    "ctraj_set_tuning": (ctypes.c_int, [_P, ctypes.POINTER(Tuning)]),
+    "ctraj_get_tuning": (ctypes.c_int, [_P, ctypes.POINTER(Tuning)]),
     "ctraj_synchronize": (ctypes.c_int, [_P]),
     "ctraj_set_beamline": (ctypes.c_int, [_P, ctypes.POINTER(Element), ctypes.c_int32, ctypes.c_int32]),
     "ctraj_set_force_table": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(ForceTable)]),

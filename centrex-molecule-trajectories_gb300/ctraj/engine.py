@@ -77,6 +77,16 @@ class Engine:
     def synchronize(self):
         _abi.check(self.lib.ctraj_synchronize(self.ctx), self.lib)
 
+    def set_tuning(self, chunk_first: int = 64, chunk_growth: int = 200, chunk_max: int = 1024,
+                   front_waves: int = 4):
+        t = _abi.Tuning(int(chunk_first), int(chunk_growth), int(chunk_max), int(front_waves))
+        _abi.check(self.lib.ctraj_set_tuning(self.ctx, ctypes.byref(t)), self.lib)
+
+    def get_tuning(self) -> dict:
+        t = _abi.Tuning()
+        _abi.check(self.lib.ctraj_get_tuning(self.ctx, ctypes.byref(t)), self.lib)
+        return {k: int(getattr(t, k)) for k, _ in _abi.Tuning._fields_}
+
     def load(self, cb: CompiledBeamline):
         """Upload a compiled beamline and its force tables (skipped when already loaded)."""
         if self._loaded is cb:

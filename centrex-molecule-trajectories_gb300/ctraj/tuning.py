@@ -1,0 +1,92 @@
+"""Autotuner for the engine's launch knobs.
+
+The knobs (``ctraj_set_tuning``): the length of the first lens chunk, the
+growth of later chunks and their maximum (how often molecules still inside a
+lens are compacted into full warps), and the size of the front kernel's grid.
+The best setting depends on the beamline: how fast molecules are lost inside
+the lens and how long the survivors stay.  ``autotune`` times every candidate
+on the actual workload with CUDA events (kernel time of the front and lens
+passes), keeps the fastest, applies it to the engine and caches it per
+(beamline, molecule count, GPU) in a JSON file.
+"""
+from __future__ import annotations
+
+import hashlib
+import itertools
+import json
+import os
+from pathlib import Path
+
+DEFAULT = dict(chunk_first=64, chunk_growth=200, chunk_max=1024, front_waves=4)
+
+
+def candidates():
+    out = []
+    for cf, g, cm in itertools.product((32, 64, 128), (150, 200, 300), (256, 512, 1024, 2048)):
+        if cm >= cf:
+            out.append(dict(chunk_first=cf, chunk_growth=g, chunk_max=cm, front_waves=4))
+    for fw in (1, 2, 8):
+        out.append(dict(DEFAULT, front_waves=fw))
+    return out
+
+
+def _cache_path() -> Path:
+    base = os.environ.get("CTRAJ_CACHE_DIR") or os.path.join(os.path.expanduser("~"), ".cache", "ctraj")
+    return Path(base) / "tuning.json"
+
+
+def workload_key(cb, n: int, device_name: str) -> str:
+    h = hashlib.sha256(bytes(cb.elements))
+    for t in cb.tables:
+        h.update(t.knots.tobytes())
+        if t.coef is not None:
+            h.update(t.coef.tobytes())
+        if t.values is not None:
+            h.update(t.values.tobytes())
+    # molecule counts within a factor of two share a setting
+    return f"{device_name}|{h.hexdigest()[:16]}|{max(0, int(n)).bit_length()}"
+
+
+def _load_cache() -> dict:
+    try:
+        return json.loads(_cache_path().read_text())
+    except (OSError, ValueError):
+        return {}
+
+
+def _store_cache(cache: dict) -> None:
+    try:
+        p = _cache_path()
+        p.parent.mkdir(parents=True, exist_ok=True)
+        tmp = p.with_suffix(".tmp")
+        tmp.write_text(json.dumps(cache, indent=1, sort_keys=True))
+        tmp.replace(p)
+    except OSError:
+        pass  # read-only home: tune again next time
+
+
+def autotune(engine, cb, n: int, run_kwargs: dict, device_name: str = "gpu", repeats: int = 2,
+             use_cache: bool = True, cands=None) -> dict:
+    """Pick the fastest knob setting for this workload; returns {"tuning", "ms", "trials"}."""
+    key = workload_key(cb, n, device_name)
+    cache = _load_cache() if use_cache else {}
+    if use_cache and key in cache:
+        engine.set_tuning(**cache[key]["tuning"])
+        return dict(cache[key], cached=True)
+    trials = []
+    for cand in (cands or candidates()):
+        engine.set_tuning(**cand)
+        best = float("inf")
+        for _ in range(repeats):
+            r = engine.run(cb, n, timing=True, **run_kwargs)
+            best = min(best, r.extra["front_ms"] + r.extra["lens_ms"])
+        trials.append((best, cand))
+    trials.sort(key=lambda x: x[0])
+    ms, tuning = trials[0]
+    engine.set_tuning(**tuning)
+    result = {"tuning": tuning, "ms": ms, "trials": len(trials),
+              "default_ms": next((t for t, c in trials if c == DEFAULT), None)}
+    if use_cache:
+        cache[key] = result
+        _store_cache(cache)
+    return dict(result, cached=False)

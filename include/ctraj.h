@@ -217,6 +217,23 @@ int ctraj_synchronize(ctraj_context* ctx);
 int ctraj_set_beamline(ctraj_context* ctx, const ctraj_element* elements,
                        int32_t n_elements, int32_t n_labels);
 
+/* Launch tuning of a context.  No reference counterpart: these are the knobs
+ * of this engine's kernels, set by the Python autotuner (ctraj.tuning).
+ *   chunk_first   RK4 steps of the first lens chunk (molecules still inside the
+ *                 lens are compacted between chunks)            default 64
+ *   chunk_growth  each chunk is this many percent of the previous  default 200
+ *   chunk_max     upper limit of a chunk's steps                  default 1024
+ *   front_waves   k_front grid = front_waves x resident CTAs     default 4 */
+typedef struct ctraj_tuning {
+  int32_t chunk_first;
+  int32_t chunk_growth;
+  int32_t chunk_max;
+  int32_t front_waves;
+} ctraj_tuning;
+
+int ctraj_set_tuning(ctraj_context* ctx, const ctraj_tuning* tuning);
+int ctraj_get_tuning(ctraj_context* ctx, ctraj_tuning* tuning);
+
 /* ElectrostaticLens.a_interp / lens_acceleration table (electrostatic_lens.py:174-213). */
 int ctraj_set_force_table(ctraj_context* ctx, int32_t table_id,
                           const ctraj_force_table* table);

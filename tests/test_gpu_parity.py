@@ -236,3 +236,27 @@ def test_empty_and_tiny_runs(engine):
         ics = np.ascontiguousarray(fx["ics"][:, :n])
         r = engine.run(cb, n, precision=64, ics=ics, outputs=True)
         assert r.label_names() == fixtures.expected_labels(fx)[:n]
+
+
+def test_results_do_not_depend_on_tuning(engine):
+    """The launch knobs change speed only: counts and per-molecule results are identical."""
+    import ctraj
+    from ctraj.distributions import device_spec
+    from ctraj.workloads import lens_beamline, source
+
+    cb = compile_beamline(lens_beamline())
+    xd, vd = (device_spec(d, r) for d, r in zip(source(), ("position", "velocity")))
+    ref = engine.run(cb, 200_000, xdist=xd, vdist=vd, seed=9, outputs=True)
+    try:
+        for t in (dict(chunk_first=16, chunk_growth=100, chunk_max=16, front_waves=1),
+                  dict(chunk_first=2048, chunk_growth=150, chunk_max=8192, front_waves=8)):
+            engine.set_tuning(**t)
+            r = engine.run(cb, 200_000, xdist=xd, vdist=vd, seed=9, outputs=True)
+            np.testing.assert_array_equal(r.counts, ref.counts)
+            np.testing.assert_array_equal(r.label, ref.label)
+            np.testing.assert_array_equal(r.final, ref.final)
+            assert r.molecule_steps == ref.molecule_steps
+        with pytest.raises(ValueError):
+            engine.set_tuning(chunk_first=0)
+    finally:
+        engine.set_tuning()
