@@ -58,7 +58,31 @@ def parse():
     p.add_argument("--cpu-sample", type=float, default=2e6, help="molecules per CPU sample")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--profile", action="store_true",
+                   help="only run the workload --steps times with the default launch knobs "
+                        "(the command the ncu captures under profiles/ use)")
     return p.parse_args()
+
+
+def run_profile(args):
+    """Plain runs of the workload: no autotuning, probes, flushes or CPU leg."""
+    from __graft_entry__ import build
+    from ctraj.compiler import compile_beamline
+    from ctraj.distributions import device_spec
+    from ctraj.engine import Engine
+    from ctraj.workloads import lens_beamline, source
+
+    build()
+    cb = compile_beamline(lens_beamline())
+    xd, vd = source()
+    xs, vs = device_spec(xd, "position"), device_spec(vd, "velocity")
+    eng = Engine(0)
+    for k in range(args.steps):
+        r = eng.run(cb, int(args.molecules), xdist=xs, vdist=vs, seed=k, timing=True)
+        print(json.dumps({"run": k, "kernels": r.kernels, "front_ms": r.extra["front_ms"],
+                          "lens_ms": r.extra["lens_ms"], "molecule_steps": r.molecule_steps,
+                          "lens_steps": r.lens_steps, "counts": r.counter_dict()}), flush=True)
+    eng.close()
 
 
 # ---------------------------------------------------------------------------
@@ -182,6 +206,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile:
+        return run_profile(args)
 
     import numpy as np
     import torch
