@@ -43,6 +43,10 @@ UNIT = "molecule-steps/s"
 # four table-driven force evaluations, stage points, RK4 combination, bore test).
 FLOP_PER_RK4_STEP = 114
 FLOP_PER_BALLISTIC_STEP = 12
+# dram__bytes_read.sum + dram__bytes_write.sum of all k_lens_chunk launches of
+# one run of this workload, from the ncu capture summarised in
+# profiles/k_lens_chunk_lens_beamline_1e7.md (the queues stay in L2)
+LENS_DRAM_BYTES_PER_RUN = 35.1e6
 WORKLOAD = ("lens beamline: aperture r=6mm@0.30m, hexapole lens z0=0.80m L=0.60m R=17.5mm V=30kV "
             "(4096-knot Stark spline, a=h*6.7GHz, d=4.2D), RK4 dt=1us, detection@3.0m; "
             "x,y~N(0,1.5mm) vx,vy~N(0,20m/s) vz~N(184,16m/s)")
@@ -202,6 +206,40 @@ def fp32_peak(device: int):
     return best
 
 
+def step_probe(device: int, bl):
+    """The production FP32 lens step in a loop: cycles per step of a lone warp
+    (latency floor) and lane-steps/s at 2 x 512 threads per SM (throughput
+    without queue, compaction or loss effects)."""
+    import numpy as np
+    import torch
+
+    from ctraj.build import PEAK_OUT
+
+    lens = [e for e in bl.elements if type(e).__name__ == "ElectrostaticLens"][0]
+    F = lens.a_interp
+    h = (F.knots[-1] - F.knots[0]) / (len(F.knots) - 1)
+    kappa = 2.0 * F.alpha / F.mass
+    q = np.zeros((len(F.coef), 4), np.float32)
+    q[:, 0] = -kappa * F.coef[:, 2]
+    q[:, 1] = -kappa * 2.0 * F.coef[:, 1] * h
+    q[:, 2] = -kappa * 3.0 * F.coef[:, 0] * h * h
+    qd = torch.from_numpy(q).to(f"cuda:{device}")
+    lib = ctypes.CDLL(str(PEAK_OUT))
+    lib.ctraj_peak_step.restype = ctypes.c_int
+    lib.ctraj_peak_step.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    out = {}
+    for key, blocks, threads in (("one_warp", 1, 32), ("full", 2 * sms, 512)):
+        cyc, lps = ctypes.c_double(), ctypes.c_double()
+        rc = lib.ctraj_peak_step(ctypes.c_void_p(qd.data_ptr()), len(q), ctypes.c_float(F.alpha / h), 4096,
+                                 blocks, threads, ctypes.byref(cyc), ctypes.byref(lps))
+        out[key] = (cyc.value, lps.value) if rc == 0 else (None, None)
+    return {"one_warp_cycles_per_step": out["one_warp"][0],
+            "isolated_lane_steps_per_s": out["full"][1],
+            "isolated_tflops": None if out["full"][1] is None else out["full"][1] * FLOP_PER_RK4_STEP / 1e12}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -253,6 +291,7 @@ def main():
     for k in range(args.warmup):
         step(seed=k)
     peak = fp32_peak(local)
+    probe = step_probe(local, bl)
 
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
@@ -326,7 +365,8 @@ def main():
                                "MEASURED_PEAKS.json has no FP32 CUDA-core figure",
                 "flop_per_step": FLOP_PER_RK4_STEP, "lens_steps_per_launch": lens_steps / args.steps,
                 "lens_ms_per_launch": lens_ms / args.steps, "front_ms_per_launch": front_ms / args.steps,
-                "traffic": None}
+                "traffic": LENS_DRAM_BYTES_PER_RUN, "traffic_unit": "bytes per lens pass (ncu, summed over its chunk launches)",
+                "step_probe": probe}
     cpu = None if args.no_cpu or world > 1 else cpu_baseline(int(args.cpu_sample))
     r0 = results[-1]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

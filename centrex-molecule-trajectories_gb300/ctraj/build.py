@@ -59,18 +59,20 @@ def build_library(force: bool = False, verbose: bool = False, extra: list[str] |
     return OUT
 
 
-PEAK_SRC = CSRC / "peak" / "fp32_peak.cu"
+PEAK_SRC = sorted((CSRC / "peak").glob("*.cu"))
 PEAK_OUT = PKG / "_lib" / "libctraj_peak.so"
 
 
 def build_peak_library(force: bool = False) -> Path:
-    """The FP32-throughput probe used by bench.py for the roofline denominator."""
-    if not force and PEAK_OUT.exists() and PEAK_OUT.stat().st_mtime >= PEAK_SRC.stat().st_mtime:
+    """Measurement probes used by bench.py: FP32 peak (roofline denominator)
+    and the lens RK4 step's latency and throughput."""
+    deps = PEAK_SRC + headers()
+    if not force and PEAK_OUT.exists() and all(p.stat().st_mtime <= PEAK_OUT.stat().st_mtime for p in deps):
         return PEAK_OUT
     PEAK_OUT.parent.mkdir(parents=True, exist_ok=True)
     tmp = PEAK_OUT.with_name(PEAK_OUT.name + f".tmp{os.getpid()}")
-    subprocess.run([nvcc(), *ARCH, "-O3", "-Xcompiler", "-fPIC", "-shared", str(PEAK_SRC), "-o", str(tmp)],
-                   check=True)
+    subprocess.run([nvcc(), *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", f"-I{INCLUDE}",
+                    f"-I{CSRC}", *map(str, PEAK_SRC), "-o", str(tmp)], check=True)
     tmp.replace(PEAK_OUT)
     return PEAK_OUT
 
