@@ -67,6 +67,27 @@ __device__ __forceinline__ void stat_add(BlockTally& S, int k, unsigned long lon
   if ((threadIdx.x & 31) == 0 && v) atomicAdd(&S.stat[k], v);
 }
 
+// Per-configuration tallies of a batched sweep (all 32 lanes call): lanes with
+// equal (configuration, label) are combined, one global atomic per group.
+__device__ __forceinline__ void tally_cfg(const RunDev& R, int cfg, int label, int n_labels) {
+  const bool counted = label != kNone && label != kQueued;
+  const int key = counted ? cfg * (n_labels + 1) + (label < 0 ? n_labels : label) : -1;
+  const unsigned peers = __match_any_sync(kFull, key);
+  if (counted && (threadIdx.x & 31) == __ffs(peers) - 1)
+    atomicAdd(&R.cfg_counts[key], (unsigned long long)__popc(peers));
+}
+
+// Configuration of sweep molecule i: the last c with cfg_start[c] <= i.
+__device__ __forceinline__ int find_cfg(const RunDev& R, int64_t i) {
+  int lo = 0, hi = R.n_cfg - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(R.cfg_start + mid) <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
 __device__ __forceinline__ void tally_flush(BlockTally& S, const RunDev& R, int n_labels) {
   __syncthreads();
   for (int k = threadIdx.x; k <= n_labels; k += blockDim.x)
@@ -127,10 +148,14 @@ __device__ __forceinline__ bool enter_lens_front(M& m, const Plan& P, int li, Le
 
 // Append the lanes with push == true to Q and raise Q's largest remaining
 // step count (all lanes call).
-template <class M>
-__device__ __forceinline__ void push_lens(const Queue& Q, bool push, const M& m, const LensStep& st) {
+template <bool kSweep = false, class M>
+__device__ __forceinline__ void push_lens(const Queue& Q, bool push, const M& m, const LensStep& st,
+                                          int cfg = 0) {
   const unsigned slot = queue_slot(push, Q.count);
-  if (push) m.store(Q, slot, st);
+  if (push) {
+    m.store(Q, slot, st);
+    if (kSweep) Q.cfg[slot] = cfg;
+  }
   const unsigned rem = push ? unsigned(st.n_total < 0 ? st.bound : st.n_total - st.n_done) : 0u;
   const unsigned wmax = __reduce_max_sync(kFull, rem);
   if ((threadIdx.x & 31) == 0 && wmax) atomicMax(Q.max_steps, wmax);
@@ -174,10 +199,53 @@ __global__ void __launch_bounds__(kThreads) k_front(const __grid_constant__ Plan
   tally_flush(S, R, P.n_labels);
 }
 
+// Batched sweep front: k_front over the molecules of all configurations; the
+// lens entrants of configuration c go to the queue of its Stark table
+// (cfg_table[c]), and every tally is also kept per configuration.  The sweep
+// beamline has one lens, so a molecule queued here is at that lens.
+template <class M>
+__global__ void __launch_bounds__(kThreads) k_sweep_front(const __grid_constant__ Plan P, const RunDev R,
+                                                          const __grid_constant__ SweepQueues Qs,
+                                                          const int n_tables) {
+  __shared__ BlockTally S;
+  tally_init(S);
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  unsigned long long steps = 0, bad = 0;
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t base = int64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31); base < R.n; base += stride) {
+    const int64_t i = base + lane;
+    int label = kNone, cfg = 0, tab = -1;
+    M m;
+    LensStep st;
+    if (i < R.n) {
+      cfg = find_cfg(R, i);
+      tab = __ldg(R.cfg_table + cfg);
+      m.init(P, R, i);
+      int lens_at = -1;
+      label = walk(m, P, 0, &lens_at);
+      if (label == kQueued && !enter_lens_front(m, P, lens_at, st)) {
+        label = P.el[lens_at].label_inside;
+        ++bad;
+      }
+      if (label != kQueued) steps += unsigned(m.rows);
+    }
+    for (int t = 0; t < n_tables; ++t) push_lens<true>(Qs.q[t], label == kQueued && tab == t, m, st, cfg);
+    tally_warp(S, label, P.n_labels);
+    tally_cfg(R, cfg, label, P.n_labels);
+  }
+  stat_add(S, kStatSteps, steps);
+  stat_add(S, kStatBadSteps, bad);
+  tally_flush(S, R, P.n_labels);
+}
+
 // ---------------------------------------------------------------------------
 enum : int { kIdle = 0, kRun = 1, kLost = 2, kExit = 3, kBad = 4 };
 
-template <class M, bool kOut, int F, bool k64, bool kStaged>
+// kSweep (batched sweeps, FP32 only): every molecule carries its configuration;
+// the staged table is unscaled and the configuration's beta and kappa scale it;
+// tallies are also kept per configuration.
+template <class M, bool kOut, int F, bool k64, bool kStaged, bool kSweep = false>
 __global__ void __launch_bounds__(kLensThreads, 2) k_lens_chunk(const __grid_constant__ Plan P, const RunDev R,
                                                          const int li, const Queue Qin,
                                                          const Queue Qcont, const Queue Qnext,
@@ -216,10 +284,16 @@ __global__ void __launch_bounds__(kLensThreads, 2) k_lens_chunk(const __grid_con
     int phase = kIdle;
     unsigned flags = 0;
     float dt = 0.f, hdt = 0.f, c2 = 0.f, dt6 = 0.f, dt26 = 0.f;
-    int n0 = 0;
+    int n0 = 0, cfg = 0;
+    float beta = 0.f, kappa = 0.f;
     bool fresh = false;
     if (idx < n_in) {
       m.load_state(Qin, idx, P, st);
+      if (kSweep) {
+        const int c = Qin.cfg[idx];
+        beta = __ldg(R.cfg_beta + c);
+        kappa = __ldg(R.cfg_kappa + c);
+      }
       bool ok = true;
       fresh = st.n_total < 0;
       if (fresh) {  // step setup deferred by the front kernel
@@ -242,7 +316,8 @@ __global__ void __launch_bounds__(kLensThreads, 2) k_lens_chunk(const __grid_con
           lost = m.lens_step(P, li, st, rg, er);
           flags |= (rg ? 1u : 0u) | (er ? 2u : 0u);
         } else {
-          lost = m.template lens_step<F, kStaged>(L, dt, hdt, c2, dt6, dt26, s_tab, flags);
+          lost = m.template lens_step<F, kStaged, kSweep>(L, dt, hdt, c2, dt6, dt26, s_tab, flags, beta,
+                                                          kappa);
           if (F == kForceRadial && (flags & 2u)) lost = true;
         }
         ++st.n_done;
@@ -253,7 +328,10 @@ __global__ void __launch_bounds__(kLensThreads, 2) k_lens_chunk(const __grid_con
       if ((k & 15) == 15 && !__any_sync(kFull, phase == kRun)) break;
     }
     asm volatile("" ::: "memory");  // keep the loads below after the loop (register pressure)
-    if (idx < n_in) m.load_rest(Qin, idx, st, !fresh);
+    if (idx < n_in) {
+      m.load_rest(Qin, idx, st, !fresh);
+      if (kSweep) cfg = Qin.cfg[idx];
+    }
     lsteps += unsigned(st.n_done - n0);
     int label = kNone;
     bool enter = false;
@@ -285,9 +363,10 @@ __global__ void __launch_bounds__(kLensThreads, 2) k_lens_chunk(const __grid_con
         write_outputs<M, kOut>(R, m, label);
       }
     }
-    push_lens(Qcont, phase == kRun, m, st);
-    push_lens(Qnext, enter, m, nst);
+    push_lens<kSweep>(Qcont, phase == kRun, m, st, cfg);
+    push_lens<kSweep>(Qnext, enter, m, nst, cfg);
     tally_warp(S, label, P.n_labels);
+    if (kSweep) tally_cfg(R, cfg, label, P.n_labels);
   }
   stat_add(S, kStatSteps, steps);
   stat_add(S, kStatLensSteps, lsteps);

@@ -118,16 +118,18 @@ __device__ inline void lens_force64(const Plan& P, const ctraj_element& e, doubl
 // kStaged: the whole table is in shared memory (s_tab); otherwise it is read
 // from global memory through the read-only cache.  Lookups past the last
 // interval extrapolate it (as scipy CubicSpline does); s < 0 uses interval 0.
+// `beta` is the table-coordinate scale (L.beta, or a molecule's own in a
+// batched sweep where each configuration has its lens voltage).
 template <int F, bool kStaged>
 __device__ __forceinline__ float wforce(float px, float py, const LensArgs& L, const float4* s_tab,
-                                        unsigned& flags) {
+                                        unsigned& flags, const float beta) {
   const float r2 = __fmaf_rn(py, py, __fmul_rn(px, px));
   float s, r = 0.0f;
   if (F == kForceStark2) {
-    s = __fmaf_rn(L.beta, r2, -L.s0);
+    s = __fmaf_rn(beta, r2, -L.s0);
   } else {
     r = sqrtf(r2);
-    s = __fmaf_rn(L.beta, r, -L.s0);
+    s = __fmaf_rn(beta, r, -L.s0);
     if (F == kForceRadial) flags |= (r > L.r_max) ? 2u : 0u;
   }
   const unsigned i = min(__float2uint_rz(s), unsigned(L.n_int - 1));  // negative s -> 0
@@ -521,22 +523,31 @@ struct Mol32 {
 
   __device__ double vel_z() const { return double(vz); }
 
-  template <int F, bool kStaged>
+  // kScaled (batched sweeps): the table holds the unscaled polynomial and each
+  // molecule brings its configuration's coordinate scale beta and force scale
+  // kappa; otherwise both come from L (kappa folded into the table).
+  template <int F, bool kStaged, bool kScaled = false>
   __device__ bool lens_step(const LensArgs& L, const float dt, const float hdt, const float c2,
-                            const float dt6, const float dt26, const float4* s_tab, unsigned& flags) {
+                            const float dt6, const float dt26, const float4* s_tab, unsigned& flags,
+                            const float beta = 0.0f, const float kappa = 1.0f) {
     const float g = L.g;
-    const float w1 = wforce<F, kStaged>(x, y, L, s_tab, flags);
+    const float b = kScaled ? beta : L.beta;
+    auto force = [&](float px, float py) {
+      const float w = wforce<F, kStaged>(px, py, L, s_tab, flags, b);
+      return kScaled ? __fmul_rn(kappa, w) : w;
+    };
+    const float w1 = force(x, y);
     const float l1x = __fmul_rn(w1, x), l1y = __fmaf_rn(w1, y, -g);
     const float k2x = __fmaf_rn(hdt, l1x, vx), k2y = __fmaf_rn(hdt, l1y, vy);
     const float p2x = __fmaf_rn(c2, vx, x), p2y = __fmaf_rn(c2, vy, y);
-    const float w2 = wforce<F, kStaged>(p2x, p2y, L, s_tab, flags);
+    const float w2 = force(p2x, p2y);
     const float l2x = __fmul_rn(w2, p2x), l2y = __fmaf_rn(w2, p2y, -g);
     const float k3x = __fmaf_rn(hdt, l2x, vx), k3y = __fmaf_rn(hdt, l2y, vy);
     const float p3x = __fmaf_rn(hdt, k2x, x), p3y = __fmaf_rn(hdt, k2y, y);
-    const float w3 = wforce<F, kStaged>(p3x, p3y, L, s_tab, flags);
+    const float w3 = force(p3x, p3y);
     const float l3x = __fmul_rn(w3, p3x), l3y = __fmaf_rn(w3, p3y, -g);
     const float p4x = __fmaf_rn(dt, k3x, x), p4y = __fmaf_rn(dt, k3y, y);
-    const float w4 = wforce<F, kStaged>(p4x, p4y, L, s_tab, flags);
+    const float w4 = force(p4x, p4y);
     const float l4x = __fmul_rn(w4, p4x), l4y = __fmaf_rn(w4, p4y, -g);
     const float sx = __fadd_rn(__fadd_rn(l1x, l2x), l3x);
     const float sy = __fadd_rn(__fadd_rn(l1y, l2y), l3y);

@@ -108,6 +108,17 @@ struct RunDev {
   double* out_margin;
   unsigned long long* counts;  // n_labels + 1
   unsigned long long* stats;   // kStat*
+  // batched sweep: molecule i belongs to configuration c with
+  // cfg_start[c] <= i < cfg_start[c + 1]; each configuration has its own
+  // lens voltage (table coordinate scale beta and force scale kappa) and
+  // Stark table; counts are kept per configuration in cfg_counts.
+  int n_cfg;
+  int pad4;
+  const int64_t* cfg_start;   // n_cfg + 1
+  const float* cfg_beta;      // n_cfg
+  const float* cfg_kappa;     // n_cfg
+  const int32_t* cfg_table;   // n_cfg: which lens queue / table
+  unsigned long long* cfg_counts;  // n_cfg x (n_labels + 1)
 };
 
 enum : int {
@@ -135,6 +146,7 @@ struct Queue {
   int32_t* id;
   int32_t* n_done;
   int32_t* n_total;
+  int32_t* cfg;         // configuration of the molecule (batched sweeps only)
   unsigned int* count;      // entries written
   unsigned int* max_steps;  // largest n_total - n_done written (sizes the chunk loop)
   unsigned int* head;       // entries taken by the warps of the kernel reading the queue
@@ -142,6 +154,11 @@ struct Queue {
 
 // Queue control words: count, max_steps, head, (unused) -- 16 bytes per queue.
 constexpr int kCtlWords = 4;
+
+// Batched sweeps: the lens-entrance queue of each Stark table.
+struct SweepQueues {
+  Queue q[CTRAJ_MAX_TABLES];
+};
 
 constexpr int kLabelDetected = -1;  // counts[n_labels]
 constexpr int kQueued = -2;         // waiting at a lens entrance

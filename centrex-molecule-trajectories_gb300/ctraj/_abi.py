@@ -143,6 +143,18 @@ class Tuning(ctypes.Structure):
     ]
 
 
+class Sweep(ctypes.Structure):
+    _fields_ = [
+        ("n_configs", ctypes.c_int32),
+        ("use_graph", ctypes.c_int32),
+        ("n_molecules", ctypes.c_void_p),  # int64[n_configs]
+        ("alpha", ctypes.c_void_p),        # double[n_configs]
+        ("table", ctypes.c_void_p),        # int32[n_configs]
+    ]
+
+
+MAX_SWEEP_CONFIGS = 65536
+
 # Entry points declared in include/ctraj.h: name -> (restype, argtypes)
 _P = ctypes.c_void_p
 SIGNATURES = {
@@ -159,6 +171,8 @@ SIGNATURES = {
     "ctraj_run": (ctypes.c_int, [_P, ctypes.POINTER(RunArgs), ctypes.POINTER(RunStats)]),
     "ctraj_record": (ctypes.c_int, [_P, ctypes.POINTER(RunArgs), _P, ctypes.c_int64, ctypes.c_int32,
                                     ctypes.c_int32, _P, _P]),
+    "ctraj_run_sweep": (ctypes.c_int, [_P, ctypes.POINTER(Sweep), ctypes.POINTER(RunArgs), _P,
+                                       ctypes.POINTER(RunStats)]),
     "ctraj_run_noalloc": (ctypes.c_int, [ctypes.POINTER(Element), ctypes.c_int32, ctypes.c_int32,
                                          ctypes.POINTER(ForceTable), ctypes.c_int32,
                                          ctypes.POINTER(RunArgs), _P, ctypes.POINTER(RunStats)]),

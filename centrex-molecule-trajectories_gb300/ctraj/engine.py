@@ -97,6 +97,59 @@ class Engine:
         _abi.check(self.lib.ctraj_set_beamline(self.ctx, cb.elements, cb.n_elements, len(cb.labels)),
                    self.lib)
         self._loaded = cb
+        self._sweep_tables = None
+
+    def load_sweep_tables(self, cb: CompiledBeamline, tables) -> list:
+        """Upload a sweep's Stark tables after the beamline's own; returns their table ids
+        (skipped when the same tables are already loaded for this beamline)."""
+        self.load(cb)
+        tables = list(tables)
+        base = len(cb.tables)
+        if base + len(tables) > _abi.MAX_TABLES:
+            raise ValueError(f"at most {_abi.MAX_TABLES} force tables (beamline {base} + sweep {len(tables)})")
+        key = tuple(id(t) for t in tables)
+        if getattr(self, "_sweep_tables", None) != key:
+            for k, t in enumerate(tables):
+                st = t.as_struct()
+                _abi.check(self.lib.ctraj_set_force_table(self.ctx, base + k, ctypes.byref(st)), self.lib)
+            self._sweep_tables = key
+            self._sweep_keep = tables
+        return [base + k for k in range(len(tables))]
+
+    def run_sweep(self, cb: CompiledBeamline, tables, alpha, table_index, n_molecules, ics=None,
+                  xdist=None, vdist=None, seed: int = 0, offset: int = 0, g: float = G,
+                  use_graph: bool = True, timing: bool = False) -> dict:
+        """ctraj_run_sweep: configuration c uses Stark table tables[table_index[c]] with
+        field coefficient alpha[c] and n_molecules[c] molecules.  Returns
+        {"counts": (n_configs, n_labels + 1), "totals", "stats", "extra"}."""
+        ids = self.load_sweep_tables(cb, tables)
+        alpha = np.ascontiguousarray(alpha, dtype=np.float64)
+        n_mol = np.ascontiguousarray(n_molecules, dtype=np.int64)
+        tid = np.ascontiguousarray(np.asarray(ids, np.int32)[np.asarray(table_index, np.int64)],
+                                   dtype=np.int32)
+        if not (alpha.shape == n_mol.shape == tid.shape) or alpha.ndim != 1:
+            raise ValueError("alpha, table_index and n_molecules must be 1-D of equal length")
+        n = int(n_mol.sum())
+        a, keep = self._args(n, 32, ics, xdist, vdist, seed, offset, g)
+        a.timing = 1 if timing else 0
+        nl = len(cb.labels)
+        totals = np.zeros(nl + 1, np.int64)
+        a.counts = totals.ctypes.data
+        counts = np.zeros((alpha.size, nl + 1), np.int64)
+        sw = _abi.Sweep(int(alpha.size), 1 if use_graph else 0, n_mol.ctypes.data, alpha.ctypes.data,
+                        tid.ctypes.data)
+        st = _abi.RunStats()
+        status = self.lib.ctraj_run_sweep(self.ctx, ctypes.byref(sw), ctypes.byref(a),
+                                          counts.ctypes.data, ctypes.byref(st))
+        del keep
+        _abi.check(status, self.lib)
+        extra = {}
+        if st.timed:
+            extra.update(front_ms=float(st.front_ms), lens_ms=float(st.lens_ms))
+        stats = dict(molecules=int(st.molecules), molecule_steps=int(st.molecule_steps),
+                     lens_steps=int(st.lens_steps), table_range=int(st.table_range),
+                     kernels=int(st.kernels))
+        return {"counts": counts, "totals": totals, "stats": stats, "extra": extra}
 
     def _args(self, n, precision, ics, xdist, vdist, seed, offset, g):
         a = _abi.RunArgs()

@@ -66,9 +66,14 @@ def _store_cache(cache: dict) -> None:
 
 
 def autotune(engine, cb, n: int, run_kwargs: dict, device_name: str = "gpu", repeats: int = 2,
-             use_cache: bool = True, cands=None) -> dict:
-    """Pick the fastest knob setting for this workload; returns {"tuning", "ms", "trials"}."""
-    key = workload_key(cb, n, device_name)
+             use_cache: bool = True, cands=None, measure=None, key_extra: str = "") -> dict:
+    """Pick the fastest knob setting for this workload; returns {"tuning", "ms", "trials"}.
+
+    By default a candidate is timed as ``engine.run(cb, n, **run_kwargs)``;
+    ``measure`` (a callable returning milliseconds under the engine's current
+    tuning) times something else, e.g. a batched sweep, and ``key_extra``
+    keeps its cache entry apart."""
+    key = workload_key(cb, n, device_name) + key_extra
     cache = _load_cache() if use_cache else {}
     if use_cache and key in cache:
         engine.set_tuning(**cache[key]["tuning"])
@@ -78,8 +83,11 @@ def autotune(engine, cb, n: int, run_kwargs: dict, device_name: str = "gpu", rep
         engine.set_tuning(**cand)
         best = float("inf")
         for _ in range(repeats):
-            r = engine.run(cb, n, timing=True, **run_kwargs)
-            best = min(best, r.extra["front_ms"] + r.extra["lens_ms"])
+            if measure is None:
+                r = engine.run(cb, n, timing=True, **run_kwargs)
+                best = min(best, r.extra["front_ms"] + r.extra["lens_ms"])
+            else:
+                best = min(best, float(measure()))
         trials.append((best, cand))
     trials.sort(key=lambda x: x[0])
     ms, tuning = trials[0]

@@ -1,4 +1,4 @@
-"""The benchmark beamlines, built from this package's reference-mirror classes.
+"""The benchmark beamlines and the lens sweep, built from this package's reference-mirror classes.
 
 * ballistic_beamline(): plain ballistic beamline -- circular aperture
   r = 6 mm at 0.30 m (L = 1 mm), rectangular 10 x 8 mm at 1.00 m (L = 1 mm),
@@ -46,3 +46,25 @@ def lens_beamline(V: float = 30e3, splitting_hz: float = 6.7e9, z0: float = 0.80
         ElectrostaticLens(name="ES lens", z0=z0, L=0.60, d=35e-3, V=V, dt=1e-6, a_interp=force),
         CircularAperture(name="Detection plane", z0=3.00, L=0.0, d=INF),
     ])
+
+
+SWEEP_SPLITTINGS_HZ = (6.7e9, 13.3e9, 20.0e9, 26.6e9)
+
+
+def sweep_configs(n_voltages: int = 256, splittings_hz=SWEEP_SPLITTINGS_HZ, n_min: float = 1e4,
+                  n_max: float = 1e6, v_max: float = 30e3, seed: int = 0, n_knots: int = 4096):
+    """The batched lens sweep: n_voltages lens voltages drawn uniformly in
+    [0, v_max] x one two-level Stark table per splitting (4096 knots over
+    0-100 kV/cm, d = 4.2 D), molecules per configuration log-uniform in
+    [n_min, n_max].  One numpy default_rng(seed) draws the voltages, then the
+    counts (table-major: configuration (t, j) is splitting t at voltage j)."""
+    import numpy as np
+
+    from .stark import hexapole_force
+    from .sweep import SweepConfigs
+
+    rng = np.random.default_rng(seed)
+    voltages = rng.uniform(0.0, v_max, n_voltages)
+    n = np.exp(rng.uniform(np.log(n_min), np.log(n_max), (len(splittings_hz), n_voltages)))
+    forces = [hexapole_force(V=v_max, R=17.5e-3, splitting_hz=a, n_knots=n_knots) for a in splittings_hz]
+    return SweepConfigs(voltages=voltages, forces=forces, n_molecules=np.rint(n).astype(np.int64))

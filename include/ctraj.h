@@ -258,6 +258,49 @@ int ctraj_record(ctraj_context* ctx, const ctraj_run_args* args,
                  int32_t max_rows, double* rows, int32_t* row_count);
 
 /*
+ * Batched sweep: many lens configurations in one launch sequence.  Replaces
+ * the caller's loop of one run_simulation per configuration (the per-state
+ * sweep of examples/lens_simulation_different_states.py:136-156 builds one
+ * beamline per Stark state and voltage and calls run_simulation on each).
+ *
+ * The beamline (ctraj_set_beamline) must hold exactly one electrostatic lens
+ * with a Stark-spline force law (field_order 1 or 2).  Configuration c differs
+ * from it only in the lens: field coefficient alpha[c] (|E| = alpha r^n; the
+ * element's p[6]) and Stark table table[c] (a table id set with
+ * ctraj_set_force_table, kind CTRAJ_TABLE_STARK_SPLINE).  It propagates
+ * n_molecules[c] molecules: molecule j of configuration c is molecule
+ * start_c + j of the whole sweep (start_c = sum of the earlier n_molecules),
+ * so with device draws it gets Philox counter base->offset + start_c + j,
+ * exactly as a ctraj_run of that configuration alone with offset
+ * base->offset + start_c.
+ *
+ * base: precision 32; base->n = the sum of n_molecules; ic_mode as in
+ * ctraj_run ((6, base->n) arrays hold the configurations one after another);
+ * out_mode CTRAJ_OUT_NONE; base->counts receives the totals over all
+ * configurations (n_labels + 1).  counts receives n_configs x (n_labels + 1)
+ * int64, row-major.
+ *
+ * With use_graph != 0 the launch sequence (one ballistic front kernel over all
+ * configurations, then per Stark table a fixed sequence of lens chunks on its
+ * own stream) is captured once as a CUDA graph and replayed by later calls
+ * with the same configurations, initial-condition source and context state.
+ * The chunk sequence is sized without a device-to-host read: its last chunk
+ * runs every molecule still inside the lens to the end.
+ */
+#define CTRAJ_MAX_SWEEP_CONFIGS 65536
+typedef struct ctraj_sweep {
+  int32_t n_configs;
+  int32_t use_graph;
+  const int64_t* n_molecules;  /* n_configs */
+  const double* alpha;         /* n_configs: lens field coefficient */
+  const int32_t* table;        /* n_configs: Stark table id */
+} ctraj_sweep;
+
+int ctraj_run_sweep(ctraj_context* ctx, const ctraj_sweep* sweep,
+                    const ctraj_run_args* base, int64_t* counts,
+                    ctraj_run_stats* stats);
+
+/*
  * Allocation-free run.  This entry point has no counterpart in the reference.
  *
  * ctraj_run_noalloc propagates molecules exactly as ctraj_run does (same
