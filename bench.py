@@ -19,6 +19,10 @@ steps).  `e2e` times the public drop-in TrajectorySimulator.run_simulation
 reference (oracle/) on the host cores on a bounded sample of the same workload.
 For N > 1 (torchrun) every rank propagates its own 1e7 molecules on disjoint
 Philox counters (replicas, weak scaling); time is the max over ranks.
+
+`sweep` (rank 0) times the batched lens sweep -- 256 voltages x 4 Stark
+tables, 2.1e8 molecules -- as one graph-replayed ctraj_run_sweep and as the
+loop of one plain run per configuration, and checks their counts agree.
 """
 from __future__ import annotations
 
@@ -62,6 +66,7 @@ def parse():
     p.add_argument("--cpu-sample", type=float, default=2e6, help="molecules per CPU sample")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-sweep", action="store_true", help="skip the batched-sweep measurement")
     p.add_argument("--profile", action="store_true",
                    help="only run the workload --steps times with the default launch knobs "
                         "(the command the ncu captures under profiles/ use)")
@@ -240,6 +245,71 @@ def step_probe(device: int, bl):
             "isolated_tflops": None if out["full"][1] is None else out["full"][1] * FLOP_PER_RK4_STEP / 1e12}
 
 
+def bench_sweep(eng, stream, flush, steps: int, warmup: int, device_name: str):
+    """The batched lens sweep (256 voltages x 4 Stark tables, log-uniform
+    molecules per configuration) as one graph-replayed ctraj_run_sweep, against
+    the same configurations looped through the plain path (ctraj_run each)."""
+    import numpy as np
+    import torch
+
+    from ctraj.distributions import device_spec
+    from ctraj.sweep import config_beamlines, loop_sweep, run_sweep, sweep_beamline
+    from ctraj.tuning import autotune
+    from ctraj.workloads import lens_beamline, source, sweep_configs
+
+    cfg = sweep_configs()
+    bl = lens_beamline()
+    cb = sweep_beamline(bl)
+    xd, vd = source()
+    xs, vs = device_spec(xd, "position"), device_spec(vd, "velocity")
+    plain_tuning = eng.get_tuning()
+
+    def sweep(seed, timing=False):
+        return run_sweep(cb, cfg, xdist=xs, vdist=vs, seed=seed, use_graph=True, timing=timing, engine=eng)
+
+    def measure():
+        r = sweep(5, timing=True)
+        return r.extra["front_ms"] + r.extra["lens_ms"]
+
+    for k in range(warmup):
+        sweep(k)
+    tuned = autotune(eng, cb, cfg.total, {}, device_name=device_name, measure=measure, key_extra="|sweep")
+    for k in range(warmup):
+        sweep(k)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    times, res = [], []
+    for k in range(steps):
+        flush.zero_()
+        ev0.record(stream)
+        r = sweep(100 + k)
+        ev1.record(stream)
+        ev1.synchronize()
+        times.append(ev0.elapsed_time(ev1))
+        res.append(r)
+    sweep_ms = sum(times) / steps
+    msteps = sum(r.molecule_steps for r in res) / steps
+    # the loop of plain runs, on the same seed as the last sweep: counts must agree
+    eng.set_tuning(**plain_tuning)
+    cbs = config_beamlines(bl, cfg)
+    for cbx in cbs[:8]:  # warm-up: first runs of each kernel
+        eng.run(cbx, 10_000, xdist=xs, vdist=vs, seed=0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loop = loop_sweep(cbs, cfg, xdist=xs, vdist=vs, seed=100 + steps - 1, engine=eng)
+    loop_ms = (time.perf_counter() - t0) * 1e3
+    diff = np.abs(loop - res[-1].counts).sum(-1)
+    return {"workload": "256 lens voltages U[0,30kV] x 4 Stark tables (a=h*{6.7,13.3,20.0,26.6}GHz), "
+                        "molecules per configuration log-uniform [1e4,1e6] (numpy default_rng(0))",
+            "configs": cfg.n_configs, "molecules": cfg.total, "molecule_steps": msteps,
+            "ms_per_sweep": sweep_ms, "molecule_steps_per_s": msteps / (sweep_ms / 1e3),
+            "gpu_launches_per_sweep": res[-1].kernels, "cuda_graph": True,
+            "loop_of_plain_runs_ms": loop_ms, "speedup_vs_loop": loop_ms / sweep_ms,
+            "loop_count_difference": {"max_per_config": int(diff.max()), "total": int(diff.sum())},
+            "tuning": tuned["tuning"], "tuning_cached": tuned.get("cached", False),
+            "timing": "CUDA events on the launching stream around ctraj_run_sweep (counts back on the host), "
+                      "L2 flushed before each; loop timed with perf_counter"}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -358,6 +428,8 @@ def main():
 
     if rank != 0:
         return
+    sweep = None if args.no_sweep else bench_sweep(eng, stream, flush, args.steps, args.warmup,
+                                                   torch.cuda.get_device_name(local))
     achieved = lens_steps * FLOP_PER_RK4_STEP / (lens_ms / 1e3) / 1e12
     roofline = {"bound": "fp32", "kernel": "k_lens (RK4 through the hexapole lens)",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
@@ -377,7 +449,7 @@ def main():
                        "l2": "flushed between steps (256 MiB write outside the timed events)",
                        "parallelism": f"replicas x{world}",
                        "tuning": tuned["tuning"], "tuning_cached": tuned.get("cached", False)},
-            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "sweep": sweep,
             "gpu_launches": int(sum(r.kernels for r in results)),
             "molecule_steps_per_step": steps / args.steps, "counts_last_step": r0.counter_dict()}
     print(json.dumps(line), flush=True)
