@@ -155,6 +155,44 @@ class Sweep(ctypes.Structure):
 
 MAX_SWEEP_CONFIGS = 65536
 
+SOFT_NPARAMS = 6
+SOFT_V, SOFT_LENS_Z0, SOFT_APERTURE_R, SOFT_BORE_R, SOFT_SIGMA_VX, SOFT_SIGMA_VY = range(6)
+
+
+class SoftArgs(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_int64),
+        ("precision", ctypes.c_int32),
+        ("ic_mode", ctypes.c_int32),
+        ("normals", ctypes.c_void_p),
+        ("seed", ctypes.c_uint64),
+        ("offset", ctypes.c_uint64),
+        ("xdist", Distribution),
+        ("vdist", Distribution),
+        ("g", ctypes.c_double),
+        ("width", ctypes.c_double),
+        ("log_floor", ctypes.c_double),
+        ("aperture", ctypes.c_int32),
+        ("checkpoint", ctypes.c_int32),
+        ("want_grad", ctypes.c_int32),
+        ("timing", ctypes.c_int32),
+    ]
+
+
+class SoftResult(ctypes.Structure):
+    _fields_ = [
+        ("loss", ctypes.c_double),
+        ("grad", ctypes.c_double * SOFT_NPARAMS),
+        ("lens_molecules", ctypes.c_int64),
+        ("lens_steps", ctypes.c_int64),
+        ("dropped", ctypes.c_int64),
+        ("bad_steps", ctypes.c_int64),
+        ("kernels", ctypes.c_int32),
+        ("timed", ctypes.c_int32),
+        ("front_ms", ctypes.c_float),
+        ("lens_ms", ctypes.c_float),
+    ]
+
 # Entry points declared in include/ctraj.h: name -> (restype, argtypes)
 _P = ctypes.c_void_p
 SIGNATURES = {
@@ -173,6 +211,7 @@ SIGNATURES = {
                                     ctypes.c_int32, _P, _P]),
     "ctraj_run_sweep": (ctypes.c_int, [_P, ctypes.POINTER(Sweep), ctypes.POINTER(RunArgs), _P,
                                        ctypes.POINTER(RunStats)]),
+    "ctraj_soft_transmission": (ctypes.c_int, [_P, ctypes.POINTER(SoftArgs), _P, ctypes.POINTER(SoftResult)]),
     "ctraj_run_noalloc": (ctypes.c_int, [ctypes.POINTER(Element), ctypes.c_int32, ctypes.c_int32,
                                          ctypes.POINTER(ForceTable), ctypes.c_int32,
                                          ctypes.POINTER(RunArgs), _P, ctypes.POINTER(RunStats)]),

@@ -301,6 +301,78 @@ int ctraj_run_sweep(ctraj_context* ctx, const ctraj_sweep* sweep,
                     ctraj_run_stats* stats);
 
 /*
+ * Soft transmission and its gradient.  No reference counterpart: the
+ * reference has only hard counts (Counter, trajectory_simulator.py:106-158);
+ * this makes the beamline differentiable so it can be tuned by gradient
+ * descent.  Every hard aperture test up to the end of the lens (the circular
+ * apertures in front of the lens at both planes, the lens entrance, the bore
+ * test after each RK4 step) becomes the weight sigmoid((R - r) / width); the
+ * loss is the mean over molecules of the product of their weights.  Molecules
+ * whose log weight falls below log_floor are dropped (counted as weight 0).
+ *
+ * Beamline: circular apertures, then exactly one electrostatic lens with a
+ * Stark spline table and field order 2 (|E| = 3 V r^2 / R^3, R = p[4]), then
+ * only planes of infinite diameter (e.g. the detection plane).
+ *
+ * params[CTRAJ_SOFT_NPARAMS]: lens voltage, lens z0 (the lens moves, its
+ * length stays), the radius of the circular aperture at element index
+ * args->aperture (ignored when -1), the clip radius of the lens bore (the field
+ * radius R stays fixed), and the standard deviations of vx and vy (replacing
+ * those of args->vdist).  Initial conditions: Philox draws exactly as ctraj_run
+ * (CTRAJ_IC_DEVICE_DRAW), or the caller's unit normals (CTRAJ_IC_HOST:
+ * normals = (5, n) float64 n_vx, n_vy, n_vz, n_x, n_y; v = mu + sigma n,
+ * x = sigma_x n_x, y = sigma_y n_y).
+ *
+ * With want_grad the gradient d loss / d params is the exact derivative of
+ * the computation (discrete adjoint): lens states are checkpointed every
+ * `checkpoint` RK4 steps (1..64) and each segment is recomputed in the
+ * backward pass.  Blocks until the result is on the host.
+ */
+#define CTRAJ_SOFT_NPARAMS 6
+enum {
+  CTRAJ_SOFT_V = 0,
+  CTRAJ_SOFT_LENS_Z0 = 1,
+  CTRAJ_SOFT_APERTURE_R = 2,
+  CTRAJ_SOFT_BORE_R = 3,
+  CTRAJ_SOFT_SIGMA_VX = 4,
+  CTRAJ_SOFT_SIGMA_VY = 5
+};
+
+typedef struct ctraj_soft_args {
+  int64_t n;
+  int32_t precision;          /* 32 or 64 */
+  int32_t ic_mode;            /* CTRAJ_IC_DEVICE_DRAW or CTRAJ_IC_HOST (unit normals) */
+  const double* normals;      /* CTRAJ_IC_HOST: (5, n), host memory */
+  uint64_t seed;
+  uint64_t offset;
+  ctraj_distribution xdist;   /* CTRAJ_DIST_GAUSSIAN_POSITION */
+  ctraj_distribution vdist;   /* CTRAJ_DIST_GAUSSIAN_VELOCITY */
+  double g;
+  double width;               /* sigmoid width (m) */
+  double log_floor;           /* e.g. -30 */
+  int32_t aperture;           /* element index of the aperture parameter, or -1 */
+  int32_t checkpoint;         /* RK4 steps between lens checkpoints, 1..64 */
+  int32_t want_grad;
+  int32_t timing;
+} ctraj_soft_args;
+
+typedef struct ctraj_soft_result {
+  double loss;
+  double grad[CTRAJ_SOFT_NPARAMS];
+  int64_t lens_molecules;     /* molecules that reached the lens above log_floor */
+  int64_t lens_steps;         /* RK4 steps of the forward pass */
+  int64_t dropped;            /* molecules dropped below log_floor */
+  int64_t bad_steps;          /* molecules with an unusable rint(L/dz) (dropped) */
+  int32_t kernels;
+  int32_t timed;
+  float front_ms;             /* ballistic part */
+  float lens_ms;              /* lens forward (and backward) */
+} ctraj_soft_result;
+
+int ctraj_soft_transmission(ctraj_context* ctx, const ctraj_soft_args* args,
+                            const double* params, ctraj_soft_result* result);
+
+/*
  * Allocation-free run.  This entry point has no counterpart in the reference.
  *
  * ctraj_run_noalloc propagates molecules exactly as ctraj_run does (same
