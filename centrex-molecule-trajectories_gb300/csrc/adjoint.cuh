@@ -57,9 +57,11 @@ constexpr int kSoftThreads = 128;
 // Stat slots of a soft run (unsigned long long).
 enum : int { kSoftStatEntered = 0, kSoftStatSteps = 1, kSoftStatDropped = 2, kSoftStatBad = 3, kSoftStatCount = 4 };
 
+// One table interval, padded to one 16-byte (float) or 32-byte (double)
+// shared-memory access.
 template <class T>
-struct Coef3 {
-  T q0, q1, q2;
+struct alignas(4 * sizeof(T)) Coef4 {
+  T q0, q1, q2, pad;
 };
 
 // IEEE-rounded arithmetic without contraction, for both precisions, so that
@@ -74,6 +76,8 @@ __device__ __forceinline__ float sqrt_(float a) { return __fsqrt_rn(a); }
 __device__ __forceinline__ double sqrt_(double a) { return __dsqrt_rn(a); }
 __device__ __forceinline__ float div_(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ double div_(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float rcp_(float a) { return __frcp_rn(a); }
+__device__ __forceinline__ double rcp_(double a) { return __drcp_rn(a); }
 __device__ __forceinline__ float exp_(float a) { return expf(a); }
 __device__ __forceinline__ double exp_(double a) { return exp(a); }
 __device__ __forceinline__ float log1p_(float a) { return log1pf(a); }
@@ -85,7 +89,17 @@ __device__ __forceinline__ void log_sigmoid(T z, T& ls, T& dls) {
   const T e = exp_(z >= T(0) ? -z : z);  // in (0, 1]
   const T l = log1p_(e);
   ls = z >= T(0) ? -l : add_(z, -l);
-  dls = z >= T(0) ? div_(e, add_(T(1), e)) : div_(T(1), add_(T(1), e));
+  dls = mul_(z >= T(0) ? e : T(1), rcp_(add_(T(1), e)));
+}
+
+// The soft test of an edge of radius R at (x, y): log weight ls and its
+// derivative d with respect to R.
+template <class T>
+__device__ __forceinline__ void soft_test(T x, T y, T R, T inv_w, T& ls, T& d) {
+  const T r = sqrt_(fma_(y, y, mul_(x, x)));
+  T dls;
+  log_sigmoid(mul_(add_(R, -r), inv_w), ls, dls);
+  d = mul_(dls, inv_w);
 }
 
 // Launch-time constants of a soft run.
@@ -114,12 +128,22 @@ struct SoftPlan {
   int checkpoint;
 };
 
-// Queue of molecules that reach the lens entrance with log weight >= floor.
+// Queue of molecules that reach the lens entrance with log weight >= floor,
+// and (gradient runs) the queue of those still above it after the lens: their
+// molecule index and lens-queue slot (which indexes their checkpoints).
 struct SoftQueue {
   int32_t* id;
   unsigned int* count;
   unsigned int* max_steps;
+  int32_t* bid;
+  int32_t* bslot;
+  unsigned int* bcount;
 };
+
+// Per (survivor, segment): the segment's backward map
+//   lambda_in = A^T lambda_out + b,  dlw/dV += c . lambda_out + d
+// as 25 values A[4][4] (row q = the image of the unit vector e_q), b[4], c[4], d.
+constexpr int kSoftSegFields = 25;
 
 // Per-molecule terms (double): weight, then the six gradient terms.  They are
 // written to (kSoftAcc, count) columns indexed by molecule and summed in a
@@ -241,14 +265,25 @@ struct SoftTape {
   T P[4], Pp[4];
 };
 
+// The lens constants in T, converted once per kernel (a double-to-float
+// conversion per use would run on the FP64 pipe inside the step loop).
+template <class T>
+struct SoftK {
+  T beta, neg_s0, kappa, g, kb2, k1, nint;
+  int n_int;
+  __device__ explicit SoftK(const SoftPlan& S)
+      : beta(T(S.beta)), neg_s0(T(-S.s0)), kappa(T(S.kappa)), g(T(S.g)), kb2(T(2.0 * S.kappa * S.beta)),
+        k1(T(S.kappa1)), nint(T(S.n_int)), n_int(S.n_int) {}
+};
+
 template <class T, bool kStaged>
-__device__ __forceinline__ void soft_poly(const SoftPlan& S, const Coef3<T>* tab, T px, T py, T& P, T& Pp) {
+__device__ __forceinline__ void soft_poly(const SoftK<T>& C, const Coef4<T>* tab, T px, T py, T& P, T& Pp) {
   const T r2 = fma_(py, py, mul_(px, px));
-  const T s = fma_(T(S.beta), r2, T(-S.s0));
+  const T s = fma_(C.beta, r2, C.neg_s0);
   // interval index, clamped (the end pieces extrapolate); NaN gives the last
-  const int i = s >= T(0) ? (s < T(S.n_int) ? int(s) : S.n_int - 1) : (s < T(0) ? 0 : S.n_int - 1);
+  const int i = s >= T(0) ? (s < C.nint ? int(s) : C.n_int - 1) : (s < T(0) ? 0 : C.n_int - 1);
   const T u = add_(s, -T(i));
-  const Coef3<T> q = tab[i];
+  const Coef4<T> q = tab[i];
   P = fma_(u, fma_(u, q.q2, q.q1), q.q0);
   Pp = fma_(mul_(T(2), u), q.q2, q.q1);
 }
@@ -256,30 +291,30 @@ __device__ __forceinline__ void soft_poly(const SoftPlan& S, const Coef3<T>* tab
 // One RK4 step of the lens (the reference's scheme), compensated accumulation;
 // with te the state and stage polynomials are written to the tape.
 template <class T, bool kStaged>
-__device__ __forceinline__ void soft_step(const SoftPlan& S, const Coef3<T>* tab, T& x, T& y, T& vx, T& vy,
+__device__ __forceinline__ void soft_step(const SoftK<T>& C, const Coef4<T>* tab, T& x, T& y, T& vx, T& vy,
                                           T& cx, T& cy, T& cvx, T& cvy, const T dt, const T hdt, const T c2,
                                           const T dt6, const T dt26, SoftTape<T>* te) {
-  const T g = T(S.g), kappa = T(S.kappa);
+  const T g = C.g, kappa = C.kappa;
   T P, Pp;
   if (te) { te->x = x; te->y = y; te->vx = vx; te->vy = vy; }
-  soft_poly<T, kStaged>(S, tab, x, y, P, Pp);
+  soft_poly<T, kStaged>(C, tab, x, y, P, Pp);
   if (te) { te->P[0] = P; te->Pp[0] = Pp; }
   T w = mul_(kappa, P);
   const T l1x = mul_(w, x), l1y = fma_(w, y, -g);
   const T k2x = fma_(hdt, l1x, vx), k2y = fma_(hdt, l1y, vy);
   const T p2x = fma_(c2, vx, x), p2y = fma_(c2, vy, y);
-  soft_poly<T, kStaged>(S, tab, p2x, p2y, P, Pp);
+  soft_poly<T, kStaged>(C, tab, p2x, p2y, P, Pp);
   if (te) { te->P[1] = P; te->Pp[1] = Pp; }
   w = mul_(kappa, P);
   const T l2x = mul_(w, p2x), l2y = fma_(w, p2y, -g);
   const T k3x = fma_(hdt, l2x, vx), k3y = fma_(hdt, l2y, vy);
   const T p3x = fma_(hdt, k2x, x), p3y = fma_(hdt, k2y, y);
-  soft_poly<T, kStaged>(S, tab, p3x, p3y, P, Pp);
+  soft_poly<T, kStaged>(C, tab, p3x, p3y, P, Pp);
   if (te) { te->P[2] = P; te->Pp[2] = Pp; }
   w = mul_(kappa, P);
   const T l3x = mul_(w, p3x), l3y = fma_(w, p3y, -g);
   const T p4x = fma_(dt, k3x, x), p4y = fma_(dt, k3y, y);
-  soft_poly<T, kStaged>(S, tab, p4x, p4y, P, Pp);
+  soft_poly<T, kStaged>(C, tab, p4x, p4y, P, Pp);
   if (te) { te->P[3] = P; te->Pp[3] = Pp; }
   w = mul_(kappa, P);
   const T l4x = mul_(w, p4x), l4y = fma_(w, p4y, -g);
@@ -291,14 +326,15 @@ __device__ __forceinline__ void soft_step(const SoftPlan& S, const Coef3<T>* tab
   accumulate_c(vy, cvy, mul_(dt6, fma_(T(2), add_(l2y, l3y), add_(l1y, l4y))));
 }
 
-// Transposed Jacobian of one step: (lx, ly, lvx, lvy) holds d lw / d(state
-// after the step) on entry and d lw / d(state before it) on exit; gV gains the
-// step's d lw / dV.  Stage quantities are rebuilt from the tape entry.
-template <class T>
-__device__ __forceinline__ void soft_step_adjoint(const SoftPlan& S, const SoftTape<T>& e, const T dt,
-                                                  const T hdt, const T c2, const T dt6, const T dt26, T& lx,
-                                                  T& ly, T& lvx, T& lvy, T& gV) {
-  const T g = T(S.g), kappa = T(S.kappa), kb = T(S.kappa * S.beta), k1 = T(S.kappa1), beta = T(S.beta);
+// Transposed Jacobian of one step applied to NV adjoint vectors at once:
+// l[v] holds d(.) / d(state after the step) on entry and d(.) / d(state
+// before it) on exit; gV[v] gains the step's d(.) / dV.  Stage quantities are
+// rebuilt once from the tape entry and shared by the vectors.
+template <class T, int NV>
+__device__ __forceinline__ void soft_step_adjoint(const SoftK<T>& C, const SoftTape<T>& e, const T dt,
+                                                  const T hdt, const T c2, const T dt6, const T dt26,
+                                                  T (&l)[NV][4], T (&gV)[NV]) {
+  const T g = C.g, kappa = C.kappa, k1 = C.k1, beta = C.beta;
   const T x = e.x, y = e.y, vx = e.vx, vy = e.vy;
   // stage points
   T w = mul_(kappa, e.P[0]);
@@ -311,51 +347,63 @@ __device__ __forceinline__ void soft_step_adjoint(const SoftPlan& S, const SoftT
   const T p3x = fma_(hdt, k2x, x), p3y = fma_(hdt, k2y, y);
   const T p4x = fma_(dt, k3x, x), p4y = fma_(dt, k3y, y);
   const T px[4] = {x, p2x, p3x, p4x}, py[4] = {y, p2y, p3y, p4y};
-  // J^T g = w g + 2 (dw/dr^2) (p.g) p;  dw/dr^2 = kappa beta P';  dw/dV = kappa1 (P + beta P' r^2)
-  auto stage = [&](int j, T gx, T gy, T& ox, T& oy) {
-    const T wj = mul_(kappa, e.P[j]);
-    const T dj = mul_(kb, e.Pp[j]);
-    const T pg = fma_(py[j], gy, mul_(px[j], gx));
+  // per stage: w, 2 dw/dr^2 = 2 kappa beta P', dw/dV = kappa1 (P + beta P' r^2)
+  T wj[4], dj[4], ej[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    wj[j] = mul_(kappa, e.P[j]);
+    dj[j] = mul_(C.kb2, e.Pp[j]);
     const T r2 = fma_(py[j], py[j], mul_(px[j], px[j]));
-    const T f = mul_(mul_(T(2), dj), pg);
-    ox = fma_(f, px[j], mul_(wj, gx));
-    oy = fma_(f, py[j], mul_(wj, gy));
-    gV = fma_(mul_(k1, fma_(mul_(beta, e.Pp[j]), r2, e.P[j])), pg, gV);
+    ej[j] = mul_(k1, fma_(mul_(beta, e.Pp[j]), r2, e.P[j]));
+  }
+  // J^T g = w g + (2 dw/dr^2) (p.g) p
+  auto stage = [&](int j, T gx, T gy, T& ox, T& oy, T& gv) {
+    const T pg = fma_(py[j], gy, mul_(px[j], gx));
+    const T f = mul_(dj[j], pg);
+    ox = fma_(f, px[j], mul_(wj[j], gx));
+    oy = fma_(f, py[j], mul_(wj[j], gy));
+    gv = fma_(ej[j], pg, gv);
   };
-  const T gx = lx, gy = ly, gvx = lvx, gvy = lvy;
-  T gl1x = fma_(dt26, gx, mul_(dt6, gvx)), gl1y = fma_(dt26, gy, mul_(dt6, gvy));
-  T gl2x = fma_(dt26, gx, mul_(mul_(T(2), dt6), gvx)), gl2y = fma_(dt26, gy, mul_(mul_(T(2), dt6), gvy));
-  const T gl3x = gl2x, gl3y = gl2y;
-  const T gl4x = mul_(dt6, gvx), gl4y = mul_(dt6, gvy);
-  lvx = fma_(dt, gx, gvx);
-  lvy = fma_(dt, gy, gvy);
-  T ox, oy;
-  // stage 4: p4 = x + dt k3, k3 = v + hdt l2
-  stage(3, gl4x, gl4y, ox, oy);
-  lx = add_(lx, ox);
-  ly = add_(ly, oy);
-  lvx = fma_(dt, ox, lvx);
-  lvy = fma_(dt, oy, lvy);
-  gl2x = fma_(mul_(hdt, dt), ox, gl2x);
-  gl2y = fma_(mul_(hdt, dt), oy, gl2y);
-  // stage 3: p3 = x + hdt k2, k2 = v + hdt l1
-  stage(2, gl3x, gl3y, ox, oy);
-  lx = add_(lx, ox);
-  ly = add_(ly, oy);
-  lvx = fma_(hdt, ox, lvx);
-  lvy = fma_(hdt, oy, lvy);
-  gl1x = fma_(mul_(hdt, hdt), ox, gl1x);
-  gl1y = fma_(mul_(hdt, hdt), oy, gl1y);
-  // stage 2: p2 = x + c2 v
-  stage(1, gl2x, gl2y, ox, oy);
-  lx = add_(lx, ox);
-  ly = add_(ly, oy);
-  lvx = fma_(c2, ox, lvx);
-  lvy = fma_(c2, oy, lvy);
-  // stage 1: p1 = x
-  stage(0, gl1x, gl1y, ox, oy);
-  lx = add_(lx, ox);
-  ly = add_(ly, oy);
+  const T dt3 = mul_(T(2), dt6), hdt2 = mul_(hdt, hdt), hdtdt = mul_(hdt, dt);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    const T gx = l[v][0], gy = l[v][1], gvx = l[v][2], gvy = l[v][3];
+    T gl1x = fma_(dt26, gx, mul_(dt6, gvx)), gl1y = fma_(dt26, gy, mul_(dt6, gvy));
+    T gl2x = fma_(dt26, gx, mul_(dt3, gvx)), gl2y = fma_(dt26, gy, mul_(dt3, gvy));
+    const T gl3x = gl2x, gl3y = gl2y;
+    const T gl4x = mul_(dt6, gvx), gl4y = mul_(dt6, gvy);
+    T lx = gx, ly = gy;
+    T lvx = fma_(dt, gx, gvx), lvy = fma_(dt, gy, gvy);
+    T ox, oy;
+    // stage 4: p4 = x + dt k3, k3 = v + hdt l2
+    stage(3, gl4x, gl4y, ox, oy, gV[v]);
+    lx = add_(lx, ox);
+    ly = add_(ly, oy);
+    lvx = fma_(dt, ox, lvx);
+    lvy = fma_(dt, oy, lvy);
+    gl2x = fma_(hdtdt, ox, gl2x);
+    gl2y = fma_(hdtdt, oy, gl2y);
+    // stage 3: p3 = x + hdt k2, k2 = v + hdt l1
+    stage(2, gl3x, gl3y, ox, oy, gV[v]);
+    lx = add_(lx, ox);
+    ly = add_(ly, oy);
+    lvx = fma_(hdt, ox, lvx);
+    lvy = fma_(hdt, oy, lvy);
+    gl1x = fma_(hdt2, ox, gl1x);
+    gl1y = fma_(hdt2, oy, gl1y);
+    // stage 2: p2 = x + c2 v
+    stage(1, gl2x, gl2y, ox, oy, gV[v]);
+    lx = add_(lx, ox);
+    ly = add_(ly, oy);
+    lvx = fma_(c2, ox, lvx);
+    lvy = fma_(c2, oy, lvy);
+    // stage 1: p1 = x
+    stage(0, gl1x, gl1y, ox, oy, gV[v]);
+    l[v][0] = add_(lx, ox);
+    l[v][1] = add_(ly, oy);
+    l[v][2] = lvx;
+    l[v][3] = lvy;
+  }
 }
 
 // d lw / d(x, y) of the soft bore test at (x, y): -sigma(-z)/w * (x, y)/r
@@ -414,21 +462,46 @@ __global__ void __launch_bounds__(kThreads) k_soft_front(const __grid_constant__
 }
 
 // ---------------------------------------------------------------------------
-// k_soft_lens: per queued molecule, the lens forward pass (log weight, radius
-// derivatives, checkpoints when kGrad) and, when kGrad, the backward pass.
-// ckpt: (n_seg, 8, cap) values of T, SoA over queue slots.
+// Step parameters of a queued molecule (recomputed from its index).
+template <class T>
+struct SoftLensSteps {
+  int N;
+  T dt, hdt, c2, dt6, dt26;
+  __device__ SoftLensSteps(const SoftPlan& S, T vz) {
+    LensStep st;
+    lens_setup(S.lens, double(vz), st);  // succeeded in k_soft_front
+    N = st.n_total;
+    dt = T(st.dt);
+    hdt = mul_(T(0.5), dt);
+    c2 = S.lens.scheme == CTRAJ_RK4_CLASSIC ? hdt : dt;
+    dt6 = mul_(dt, T(1.0 / 6.0));
+    dt26 = T(st.dt * st.dt / 6.0);
+  }
+};
+
+template <class T>
+__device__ __forceinline__ void stage_table(const SoftPlan& S, const Coef4<T>* table, Coef4<T>* s_tab) {
+  for (int k = threadIdx.x; k < S.n_int; k += blockDim.x) s_tab[k] = table[k];
+  __syncthreads();
+}
+
+// k_soft_lens: per queued molecule, the lens forward pass: log weight, radius
+// derivatives, and with kGrad the checkpoints (state and carried rounding
+// errors every K steps; ckpt is (n_seg, 8, cap) values of T, SoA over slots)
+// and the queue of molecules that stay above the floor.  The floor test runs
+// every 8 steps (the log weight only decreases, so the dropped set is the
+// same) to keep it off the step-to-step dependency chain.
 template <class T, bool kGrad>
 __global__ void __launch_bounds__(kSoftThreads) k_soft_lens(const __grid_constant__ SoftPlan S, const SoftQueue Q,
-                                                            const Coef3<T>* __restrict__ table, T* ckpt,
+                                                            const Coef4<T>* __restrict__ table, T* ckpt,
                                                             size_t cap, double* __restrict__ contrib,
                                                             unsigned long long* stats) {
   extern __shared__ unsigned char s_raw[];
-  Coef3<T>* s_tab = reinterpret_cast<Coef3<T>*>(s_raw);
-  for (int k = threadIdx.x; k < S.n_int; k += blockDim.x) s_tab[k] = table[k];
-  __syncthreads();
+  Coef4<T>* s_tab = reinterpret_cast<Coef4<T>*>(s_raw);
+  stage_table(S, table, s_tab);
   const unsigned n_in = *Q.count;
-  const T inv_w = T(S.inv_w), bore = T(S.bore);
-  const bool classic = S.lens.scheme == CTRAJ_RK4_CLASSIC;
+  const T inv_w = T(S.inv_w), bore = T(S.bore), floor_ = T(S.log_floor);
+  const SoftK<T> C(S);
   const int K = S.checkpoint;
   unsigned long long steps = 0, dropped = 0, entered = 0;
   for (unsigned slot = blockIdx.x * blockDim.x + threadIdx.x; slot < n_in; slot += gridDim.x * blockDim.x) {
@@ -436,32 +509,56 @@ __global__ void __launch_bounds__(kSoftThreads) k_soft_lens(const __grid_constan
     SoftMol<T> m;
     m.init(S, i);
     m.front(S);
-    LensStep st;
-    lens_setup(S.lens, double(m.vz), st);  // succeeded in k_soft_front
-    const int N = st.n_total;
-    const T dt = T(st.dt), hdt = mul_(T(0.5), dt);
-    const T c2 = classic ? hdt : dt;
-    const T dt6 = mul_(dt, T(1.0 / 6.0)), dt26 = T(st.dt * st.dt / 6.0);
+    const SoftLensSteps<T> L(S, m.vz);
     T x = m.x, y = m.y, vx = m.vx, vy = m.vy, cx = T(0), cy = T(0), cvx = T(0), cvy = T(0);
     ++entered;
     bool alive = true;
     int n = 0;
-    for (; n < N; ++n) {
-      if (kGrad && n % K == 0) {
-        T* c = ckpt + size_t(n / K) * 8 * cap + slot;
-        c[0] = x; c[cap] = y; c[2 * cap] = vx; c[3 * cap] = vy;
-        c[4 * cap] = cx; c[5 * cap] = cy; c[6 * cap] = cvx; c[7 * cap] = cvy;
+    // One lens step plus the bore test of the state before it (the state
+    // after the previous step; the entrance test was done by m.front).  The
+    // test does not feed the dynamics, so its latency overlaps the step's.
+    auto step = [&](int k) {
+      const T qx = x, qy = y;
+      soft_step<T, true>(C, s_tab, x, y, vx, vy, cx, cy, cvx, cvy, L.dt, L.hdt, L.c2, L.dt6, L.dt26, nullptr);
+      T ls, d;
+      soft_test(qx, qy, bore, inv_w, ls, d);
+      m.lw = add_(m.lw, k > 0 ? ls : T(0));
+      m.d_bore = add_(m.d_bore, k > 0 ? d : T(0));
+    };
+    auto store_ckpt = [&](int k) {
+      T* c = ckpt + size_t(k / K) * 8 * cap + slot;
+      c[0] = x; c[cap] = y; c[2 * cap] = vx; c[3 * cap] = vy;
+      c[4 * cap] = cx; c[5 * cap] = cy; c[6 * cap] = cvx; c[7 * cap] = cvy;
+    };
+    if (K % 8 == 0) {
+      // groups of 8 steps without a branch; checkpoints and the floor test in between
+      for (; n + 8 <= L.N; n += 8) {
+        if (kGrad && n % K == 0) store_ckpt(n);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) step(n + u);
+        if (!(m.lw >= floor_)) {
+          alive = false;
+          n += 8;
+          break;
+        }
       }
-      soft_step<T, true>(S, s_tab, x, y, vx, vy, cx, cy, cvx, cvy, dt, hdt, c2, dt6, dt26, nullptr);
-      m.x = x;
-      m.y = y;
-      m.d_bore = add_(m.d_bore, m.check(bore, inv_w));
-      if (!(m.lw >= T(S.log_floor))) {
+    }
+    for (; alive && n < L.N; ++n) {
+      if (kGrad && n % K == 0) store_ckpt(n);
+      step(n);
+      if ((n & 7) == 7 && !(m.lw >= floor_)) {
         alive = false;
         ++n;
         break;
       }
     }
+    if (alive && L.N > 0) {  // the test after the last step
+      T ls, d;
+      soft_test(x, y, bore, inv_w, ls, d);
+      m.lw = add_(m.lw, ls);
+      m.d_bore = add_(m.d_bore, d);
+    }
+    if (!(m.lw >= floor_)) alive = false;
     steps += unsigned(n);
     if (!alive) {
       ++dropped;
@@ -474,53 +571,11 @@ __global__ void __launch_bounds__(kSoftThreads) k_soft_lens(const __grid_constan
     o[0] = Tw;
     o[(1 + kSoftAperture) * cnt] = Tw * double(m.d_ap);
     o[(1 + kSoftBore) * cnt] = Tw * double(m.d_bore);
-    if (!kGrad) continue;
-    // ---- backward through the lens, segment by segment
-    T lx = T(0), ly = T(0), lvx = T(0), lvy = T(0), gV = T(0);
-    SoftTape<T> tape[kSoftTape];
-    const int n_seg = (N + K - 1) / K;
-    for (int sg = n_seg - 1; sg >= 0; --sg) {
-      const T* c = ckpt + size_t(sg) * 8 * cap + slot;
-      x = c[0]; y = c[cap]; vx = c[2 * cap]; vy = c[3 * cap];
-      cx = c[4 * cap]; cy = c[5 * cap]; cvx = c[6 * cap]; cvy = c[7 * cap];
-      const int k0 = sg * K, k1 = min(N, k0 + K);
-      for (int k = k0; k < k1; ++k)
-        soft_step<T, true>(S, s_tab, x, y, vx, vy, cx, cy, cvx, cvy, dt, hdt, c2, dt6, dt26, &tape[k - k0]);
-      // (x, y) is the state after step k1 - 1
-      for (int k = k1 - 1; k >= k0; --k) {
-        const T ax = k == k1 - 1 ? x : tape[k - k0 + 1].x;
-        const T ay = k == k1 - 1 ? y : tape[k - k0 + 1].y;
-        check_adjoint(bore, inv_w, ax, ay, lx, ly);
-        soft_step_adjoint(S, tape[k - k0], dt, hdt, c2, dt6, dt26, lx, ly, lvx, lvy, gV);
-      }
+    if (kGrad) {
+      const unsigned b = atomicAdd(Q.bcount, 1u);
+      Q.bid[b] = int32_t(i);
+      Q.bslot[b] = int32_t(slot);
     }
-    // ---- backward through the ballistic planes (recomputed)
-    SoftMol<T> b;
-    b.init(S, i);
-    T px[kSoftMaxPlanes], py[kSoftMaxPlanes], pvy[kSoftMaxPlanes];
-    for (int p = 0; p < S.n_planes; ++p) {
-      b.fly(S, p);
-      px[p] = b.x;
-      py[p] = b.y;
-      pvy[p] = b.vy;
-    }
-    T gz0 = T(0);
-    for (int p = S.n_planes - 1; p >= 0; --p) {
-      const T R = p == S.n_planes - 1 ? bore : T(S.radius[p]);
-      if (R < T(INFINITY)) check_adjoint(R, inv_w, px[p], py[p], lx, ly);
-      const T t = b.flight_time(S, p);
-      if (p == S.n_planes - 1) {
-        // d t / d z0 = 1 / vz; d x / d t = v at the plane, d vy / d t = -g
-        const T gt = fma_(lvy, T(-S.g), fma_(ly, pvy[p], mul_(lx, b.vx)));
-        gz0 = div_(gt, b.vz);
-      }
-      lvx = fma_(t, lx, lvx);
-      lvy = fma_(t, ly, lvy);
-    }
-    o[(1 + kSoftV) * cnt] = Tw * double(gV);
-    o[(1 + kSoftZ0) * cnt] = Tw * double(gz0);
-    o[(1 + kSoftSigmaVx) * cnt] = Tw * double(mul_(lvx, m.nvx));
-    o[(1 + kSoftSigmaVy) * cnt] = Tw * double(mul_(lvy, m.nvy));
   }
   steps = warp_sum(steps);
   dropped = warp_sum(dropped);
@@ -529,6 +584,136 @@ __global__ void __launch_bounds__(kSoftThreads) k_soft_lens(const __grid_constan
     if (steps) atomicAdd(&stats[kSoftStatSteps], steps);
     if (dropped) atomicAdd(&stats[kSoftStatDropped], dropped);
     if (entered) atomicAdd(&stats[kSoftStatEntered], entered);
+  }
+}
+
+// k_soft_seg: one thread per (surviving molecule, lens segment), in parallel
+// over segments: recompute the segment from its checkpoint into the tape, then
+// run the transposed step Jacobians backwards over it for the four unit
+// vectors and the affine part (the segment's own bore tests), giving the
+// segment's backward map (A, b, c, d).  seg_out: (kSoftSegFields, bcap * max_seg).
+template <class T>
+__global__ void __launch_bounds__(kSoftThreads) k_soft_seg(const __grid_constant__ SoftPlan S, const SoftQueue Q,
+                                                           const Coef4<T>* __restrict__ table,
+                                                           const T* __restrict__ ckpt, size_t cap,
+                                                           T* __restrict__ seg_out, int max_seg, size_t bcap) {
+  extern __shared__ unsigned char s_raw[];
+  Coef4<T>* s_tab = reinterpret_cast<Coef4<T>*>(s_raw);
+  stage_table(S, table, s_tab);
+  const size_t n_work = size_t(*Q.bcount) * size_t(max_seg);
+  const size_t plane = bcap * size_t(max_seg);
+  const T inv_w = T(S.inv_w), bore = T(S.bore);
+  const SoftK<T> C(S);
+  const int K = S.checkpoint;
+  for (size_t wi = size_t(blockIdx.x) * blockDim.x + threadIdx.x; wi < n_work; wi += size_t(gridDim.x) * blockDim.x) {
+    const size_t b = wi / size_t(max_seg);
+    const int sg = int(wi % size_t(max_seg));
+    const int32_t slot = Q.bslot[b];
+    SoftMol<T> m;
+    m.init(S, Q.bid[b]);
+    const SoftLensSteps<T> L(S, m.vz);
+    const int k0 = sg * K;
+    if (k0 >= L.N) continue;
+    const int k1 = min(L.N, k0 + K);
+    const T* c = ckpt + size_t(sg) * 8 * cap + slot;
+    T x = c[0], y = c[cap], vx = c[2 * cap], vy = c[3 * cap];
+    T cx = c[4 * cap], cy = c[5 * cap], cvx = c[6 * cap], cvy = c[7 * cap];
+    SoftTape<T> tape[kSoftTape];
+    for (int k = k0; k < k1; ++k)
+      soft_step<T, true>(C, s_tab, x, y, vx, vy, cx, cy, cvx, cvy, L.dt, L.hdt, L.c2, L.dt6, L.dt26,
+                         &tape[k - k0]);
+    T lam[5][4], gv[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      gv[v] = T(0);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) lam[v][r] = T(v == r ? 1 : 0);
+    }
+    // (x, y) is the state after step k1 - 1
+    for (int k = k1 - 1; k >= k0; --k) {
+      const T ax = k == k1 - 1 ? x : tape[k - k0 + 1].x;
+      const T ay = k == k1 - 1 ? y : tape[k - k0 + 1].y;
+      check_adjoint(bore, inv_w, ax, ay, lam[4][0], lam[4][1]);
+      soft_step_adjoint<T, 5>(C, tape[k - k0], L.dt, L.hdt, L.c2, L.dt6, L.dt26, lam, gv);
+    }
+    T* o = seg_out + wi;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+#pragma unroll
+      for (int r = 0; r < 4; ++r) o[(q * 4 + r) * plane] = lam[q][r];
+      o[(20 + q) * plane] = gv[q];
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) o[(16 + r) * plane] = lam[4][r];
+    o[24 * plane] = gv[4];
+  }
+}
+
+// k_soft_compose: per surviving molecule, the segments' backward maps applied
+// from the last segment to the first, then the ballistic part reversed
+// (recomputed): d lw / d(lens z0) from the last flight time, d lw / d(sigma_v)
+// from the initial velocities.  Adds the weighted terms to contrib.
+template <class T>
+__global__ void __launch_bounds__(kSoftThreads) k_soft_compose(const __grid_constant__ SoftPlan S, const SoftQueue Q,
+                                                               const T* __restrict__ seg_out, int max_seg,
+                                                               size_t bcap, double* __restrict__ contrib) {
+  const unsigned nb = *Q.bcount;
+  const size_t plane = bcap * size_t(max_seg);
+  const T inv_w = T(S.inv_w), bore = T(S.bore);
+  for (unsigned b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+    const int64_t i = Q.bid[b];
+    SoftMol<T> m;
+    m.init(S, i);
+    const SoftLensSteps<T> L(S, m.vz);
+    const int n_seg = (L.N + S.checkpoint - 1) / S.checkpoint;
+    T lx = T(0), ly = T(0), lvx = T(0), lvy = T(0), gV = T(0);
+    for (int sg = n_seg - 1; sg >= 0; --sg) {
+      const T* o = seg_out + size_t(b) * size_t(max_seg) + size_t(sg);
+      const T lo[4] = {lx, ly, lvx, lvy};
+      T ln[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) ln[r] = o[(16 + r) * plane];
+      T g = o[24 * plane];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) ln[r] = fma_(o[(q * 4 + r) * plane], lo[q], ln[r]);
+        g = fma_(o[(20 + q) * plane], lo[q], g);
+      }
+      gV = add_(gV, g);
+      lx = ln[0];
+      ly = ln[1];
+      lvx = ln[2];
+      lvy = ln[3];
+    }
+    // the ballistic planes, recomputed, then reversed
+    T px[kSoftMaxPlanes], py[kSoftMaxPlanes], pvy[kSoftMaxPlanes];
+    for (int p = 0; p < S.n_planes; ++p) {
+      m.fly(S, p);
+      px[p] = m.x;
+      py[p] = m.y;
+      pvy[p] = m.vy;
+    }
+    T gz0 = T(0);
+    for (int p = S.n_planes - 1; p >= 0; --p) {
+      const T R = p == S.n_planes - 1 ? bore : T(S.radius[p]);
+      if (R < T(INFINITY)) check_adjoint(R, inv_w, px[p], py[p], lx, ly);
+      const T t = m.flight_time(S, p);
+      if (p == S.n_planes - 1) {
+        // d t / d z0 = 1 / vz; d x / d t = v at the plane, d vy / d t = -g
+        const T gt = fma_(lvy, T(-S.g), fma_(ly, pvy[p], mul_(lx, m.vx)));
+        gz0 = div_(gt, m.vz);
+      }
+      lvx = fma_(t, lx, lvx);
+      lvy = fma_(t, ly, lvy);
+    }
+    const size_t cnt = size_t(S.count);
+    double* o = contrib + size_t(i - S.first);
+    const double Tw = o[0];
+    o[(1 + kSoftV) * cnt] = Tw * double(gV);
+    o[(1 + kSoftZ0) * cnt] = Tw * double(gz0);
+    o[(1 + kSoftSigmaVx) * cnt] = Tw * double(mul_(lvx, m.nvx));
+    o[(1 + kSoftSigmaVy) * cnt] = Tw * double(mul_(lvy, m.nvy));
   }
 }
 

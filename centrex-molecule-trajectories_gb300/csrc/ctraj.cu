@@ -118,7 +118,7 @@ struct ctraj_context {
   DevBuf sweep_ctl;             // queue counters, chunk counters, totals, stats
   DevBuf sweep_queue[2 * CTRAJ_MAX_TABLES];
   // soft transmission (ctraj_soft_transmission)
-  DevBuf soft_table, soft_queue, soft_ckpt, soft_ctl, soft_contrib;
+  DevBuf soft_table, soft_queue, soft_ckpt, soft_ctl, soft_contrib, soft_seg;
   unsigned long long* sweep_host = nullptr;  // pinned: per-configuration counts, totals, stats
   size_t sweep_host_words = 0;
   cudaStream_t side[CTRAJ_MAX_TABLES] = {};
@@ -535,6 +535,7 @@ int ctraj_destroy(ctraj_context* c) {
   c->soft_ckpt.release();
   c->soft_ctl.release();
   c->soft_contrib.release();
+  c->soft_seg.release();
   for (auto& ev : c->ev)
     if (ev) cudaEventDestroy(ev);
   if (c->host_max) cudaFreeHost(c->host_max);
@@ -1239,17 +1240,17 @@ int soft_run(ctraj_context* c, const ctraj_soft_args* a, SoftPlan& S, int li, ct
   const double f = qmax > 0.0 && std::isfinite(qmax) ? std::ldexp(1.0, -std::ilogb(qmax)) : 1.0;
   S.kappa /= f;
   S.kappa1 /= f;
-  std::vector<Coef3<T>> host(t.n - 1);
+  std::vector<Coef4<T>> host(t.n - 1);
   for (int j = 0; j < t.n - 1; ++j) {
     const double* cj = &t.coef[size_t(j) * 4];
-    host[j] = Coef3<T>{T(f * cj[2]), T(f * (2.0 * cj[1] * h)), T(f * (3.0 * cj[0] * h * h))};
+    host[j] = Coef4<T>{T(f * cj[2]), T(f * (2.0 * cj[1] * h)), T(f * (3.0 * cj[0] * h * h)), T(0)};
   }
-  const size_t tb = host.size() * sizeof(Coef3<T>);
+  const size_t tb = host.size() * sizeof(Coef4<T>);
   if (tb > 200 * 1024) return fail(CTRAJ_EINVAL, "soft transmission: the lens table (%d knots) is too large", t.n);
   int st;
   const int64_t chunk = std::min<int64_t>(std::max<int64_t>(a->n, 1), kSoftChunk);
   if ((st = c->soft_table.ensure(tb))) return st;
-  if ((st = c->soft_queue.ensure(size_t(chunk) * 4))) return st;
+  if ((st = c->soft_queue.ensure(size_t(chunk) * 4 * 3))) return st;
   if ((st = c->soft_ctl.ensure(kSoftCtlBytes))) return st;
   if ((st = c->soft_contrib.ensure(size_t(chunk) * kSoftAcc * 8))) return st;
   CT_CUDA(cudaMemcpyAsync(c->soft_table.p, host.data(), tb, cudaMemcpyHostToDevice, s));
@@ -1259,7 +1260,9 @@ int soft_run(ctraj_context* c, const ctraj_soft_args* a, SoftPlan& S, int li, ct
     CT_CUDA(cudaMemcpyAsync(c->ics.p, a->normals, b, cudaMemcpyHostToDevice, s));
     S.normals = c->ics.as<double>();
   }
-  SoftQueue Q{c->soft_queue.as<int32_t>(), c->soft_ctl.as<unsigned>(0), c->soft_ctl.as<unsigned>(4)};
+  SoftQueue Q{c->soft_queue.as<int32_t>(), c->soft_ctl.as<unsigned>(0), c->soft_ctl.as<unsigned>(4),
+              c->soft_queue.as<int32_t>(size_t(chunk) * 4), c->soft_queue.as<int32_t>(size_t(chunk) * 8),
+              c->soft_ctl.as<unsigned>(8)};
   unsigned long long* stats = c->soft_ctl.as<unsigned long long>(256);
   double* partial = c->soft_ctl.as<double>(256 + 8 * kSoftStatCount);
   double* contrib = c->soft_contrib.as<double>();
@@ -1293,12 +1296,30 @@ int soft_run(ctraj_context* c, const ctraj_soft_args* a, SoftPlan& S, int li, ct
     if (count > 0) {
       const size_t cap = count;
       const size_t n_seg = (size_t(max_steps) + S.checkpoint - 1) / S.checkpoint + 1;
-      if (a->want_grad && (st = c->soft_ckpt.ensure(n_seg * 8 * cap * sizeof(T)))) return st;
+      const int max_seg = int(n_seg - 1);
+      if (a->want_grad) {
+        if ((st = c->soft_ckpt.ensure(n_seg * 8 * cap * sizeof(T)))) return st;
+        if ((st = c->soft_seg.ensure(size_t(kSoftSegFields) * cap * size_t(max_seg) * sizeof(T)))) return st;
+      }
       grid = int((cap + kSoftThreads - 1) / kSoftThreads);
-      kl<<<grid, kSoftThreads, tb, s>>>(S, Q, c->soft_table.as<Coef3<T>>(), c->soft_ckpt.as<T>(), cap, contrib,
+      kl<<<grid, kSoftThreads, tb, s>>>(S, Q, c->soft_table.as<Coef4<T>>(), c->soft_ckpt.as<T>(), cap, contrib,
                                          stats);
       CT_CUDA(cudaGetLastError());
       ++launches;
+      if (a->want_grad && max_seg > 0) {
+        // backward: every (survivor, segment) in parallel, then per survivor
+        // the composition and the ballistic part; both read the survivor
+        // count on the device
+        auto ks = k_soft_seg<T>;
+        CT_CUDA(cudaFuncSetAttribute(ks, cudaFuncAttributeMaxDynamicSharedMemorySize, int(tb)));
+        const int gs = blocks_per_sm(ks, kSoftThreads, tb) * c->sm_count * 4;
+        ks<<<gs, kSoftThreads, tb, s>>>(S, Q, c->soft_table.as<Coef4<T>>(), c->soft_ckpt.as<T>(), cap,
+                                        c->soft_seg.as<T>(), max_seg, cap);
+        CT_CUDA(cudaGetLastError());
+        k_soft_compose<T><<<grid, kSoftThreads, 0, s>>>(S, Q, c->soft_seg.as<T>(), max_seg, cap, contrib);
+        CT_CUDA(cudaGetLastError());
+        launches += 2;
+      }
     }
     k_soft_reduce<<<dim3(kSoftReduceBlocks, kSoftAcc), 256, 0, s>>>(contrib, S.count, partial);
     CT_CUDA(cudaGetLastError());

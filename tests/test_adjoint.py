@@ -130,8 +130,12 @@ def test_checkpoint_interval_does_not_change_the_gradient(engine):
     p0 = params(problem(1))
     outs = [soft_transmission(problem(50_000, seed=5, checkpoint=k), p0, engine=engine) for k in (64, 17, 1)]
     for o in outs[1:]:
+        # the forward pass is the same; the backward maps compose over
+        # different segments, so only rounding differs
         assert o.loss == outs[0].loss
-        np.testing.assert_array_equal(o.grad, outs[0].grad)
+        assert rel_err(o.grad, outs[0].grad).max() < FP32_REL, (o.grad, outs[0].grad)
+    again = soft_transmission(problem(50_000, seed=5, checkpoint=64), p0, engine=engine)
+    np.testing.assert_array_equal(again.grad, outs[0].grad)  # deterministic
     # the forward-only call gives the same loss
     f = soft_transmission(problem(50_000, seed=5), p0, want_grad=False, engine=engine)
     assert f.loss == outs[0].loss and f.grad is None
