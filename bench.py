@@ -23,6 +23,8 @@ Philox counters (replicas, weak scaling); time is the max over ranks.
 `sweep` (rank 0) times the batched lens sweep -- 256 voltages x 4 Stark
 tables, 2.1e8 molecules -- as one graph-replayed ctraj_run_sweep and as the
 loop of one plain run per configuration, and checks their counts agree.
+`adjoint` (rank 0) times full gradients of the soft transmission at 1e6
+molecules (grads/s) against one soft forward and one plain run.
 """
 from __future__ import annotations
 
@@ -67,6 +69,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-sweep", action="store_true", help="skip the batched-sweep measurement")
+    p.add_argument("--no-adjoint", action="store_true", help="skip the gradient measurement")
     p.add_argument("--profile", action="store_true",
                    help="only run the workload --steps times with the default launch knobs "
                         "(the command the ncu captures under profiles/ use)")
@@ -310,6 +313,81 @@ def bench_sweep(eng, stream, flush, steps: int, warmup: int, device_name: str):
                       "L2 flushed before each; loop timed with perf_counter"}
 
 
+def bench_adjoint(eng, stream, flush, steps: int, warmup: int):
+    """Full gradients of the soft transmission (sigmoid edges of width 0.2 mm)
+    of the lens beamline with respect to (V, lens z0, r_A1, r_bore, sigma_vx,
+    sigma_vy) at 1e6 molecules, FP32 discrete adjoint (checkpoint every 64
+    steps), against one soft forward and one plain (hard-count) run of the same
+    molecules; plus a central-difference check (h = 1e-4 relative) of the
+    gradient on 1e5 molecules with the FP64 forward."""
+    import numpy as np
+    import torch
+
+    from ctraj.adjoint import PARAM_NAMES, SoftProblem, soft_transmission
+    from ctraj.distributions import device_spec
+    from ctraj.workloads import lens_beamline, source
+
+    n = 1_000_000
+    prob = SoftProblem.from_beamline(lens_beamline(), n=n, aperture="A1", precision=32, checkpoint=64)
+    p0 = prob.initial_params()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        ts = []
+        for k in range(warmup):
+            fn(k)
+        for k in range(steps):
+            flush.zero_()
+            ev0.record(stream)
+            out = fn(100 + k)
+            ev1.record(stream)
+            ev1.synchronize()
+            ts.append(ev0.elapsed_time(ev1))
+        return sum(ts) / len(ts), out
+
+    def grad(seed):
+        prob.seed = seed
+        return soft_transmission(prob, p0, want_grad=True, engine=eng)
+
+    def fwd(seed):
+        prob.seed = seed
+        return soft_transmission(prob, p0, want_grad=False, engine=eng)
+
+    xd, vd = source()
+    xs, vs = device_spec(xd, "position"), device_spec(vd, "velocity")
+
+    def hard(seed):
+        return eng.run(prob.cb, n, xdist=xs, vdist=vs, seed=seed)
+
+    grad_ms, g = timed(grad)
+    fwd_ms, f = timed(fwd)
+    hard_ms, h = timed(hard)
+    # finite-difference check on 1e5 molecules
+    small = SoftProblem.from_beamline(lens_beamline(), n=100_000, aperture="A1", precision=64, seed=3)
+    small32 = SoftProblem.from_beamline(lens_beamline(), n=100_000, aperture="A1", precision=32, seed=3)
+    fd = np.zeros(6)
+    for k in range(6):
+        hk = 1e-4 * abs(p0[k])
+        pp, pm = p0.copy(), p0.copy()
+        pp[k] += hk
+        pm[k] -= hk
+        fd[k] = (soft_transmission(small, pp, want_grad=False, engine=eng).loss
+                 - soft_transmission(small, pm, want_grad=False, engine=eng).loss) / (2 * hk)
+    ga = soft_transmission(small32, p0, engine=eng).grad
+    rel = np.abs(ga - fd) / np.maximum(np.abs(fd), 1e-300)
+    return {"workload": "soft transmission of the lens beamline (sigmoid edges, width 0.2 mm), 1e6 molecules, "
+                        "FP32, gradient w.r.t. " + ", ".join(PARAM_NAMES),
+            "grads_per_s": 1e3 / grad_ms, "ms_per_gradient": grad_ms, "soft_forward_ms": fwd_ms,
+            "plain_run_ms": hard_ms, "gradient_over_soft_forward": grad_ms / fwd_ms,
+            "gradient_over_plain_run": grad_ms / hard_ms, "checkpoint_steps": 64,
+            "loss": g.loss, "gradient": dict(zip(PARAM_NAMES, map(float, g.grad))),
+            "lens_molecules": g.lens_molecules, "lens_steps": g.lens_steps,
+            "gpu_launches_per_gradient": g.kernels,
+            "fd_check": {"molecules": 100_000, "h": "1e-4 relative, central, FP64 forward",
+                         "max_rel_error_fp32_adjoint": float(rel.max())},
+            "timing": "CUDA events on the launching stream around the call (result on the host), L2 flushed before each"}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -430,6 +508,7 @@ def main():
         return
     sweep = None if args.no_sweep else bench_sweep(eng, stream, flush, args.steps, args.warmup,
                                                    torch.cuda.get_device_name(local))
+    adjoint = None if args.no_adjoint else bench_adjoint(eng, stream, flush, args.steps, args.warmup)
     achieved = lens_steps * FLOP_PER_RK4_STEP / (lens_ms / 1e3) / 1e12
     roofline = {"bound": "fp32", "kernel": "k_lens (RK4 through the hexapole lens)",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
@@ -450,6 +529,7 @@ def main():
                        "parallelism": f"replicas x{world}",
                        "tuning": tuned["tuning"], "tuning_cached": tuned.get("cached", False)},
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "sweep": sweep,
+            "adjoint": adjoint,
             "gpu_launches": int(sum(r.kernels for r in results)),
             "molecule_steps_per_step": steps / args.steps, "counts_last_step": r0.counter_dict()}
     print(json.dumps(line), flush=True)
