@@ -103,6 +103,8 @@ struct ctraj_context {
   DevBuf rec_rows, rec_ids, rec_count;
   unsigned* host_max = nullptr; // pinned: largest remaining lens step count of a queue
   DevBuf chunk_ctl;             // (count, max_steps) of the queue each lens chunk writes
+  DevBuf rec_stage;             // ring recording: staged records of the recorded lens
+  DevBuf ring_ent;              // ring recording: molecules stopped by the entrance test
   int chunk = 64;               // RK4 steps of the first lens chunk (compaction interval)
   int chunk_growth = 200;       // percent: each chunk's length relative to the previous
   int chunk_max = 1024;         // longest chunk
@@ -311,19 +313,20 @@ int blocks_per_sm(KernelT k, int threads, size_t smem) {
 using LensKernel = void (*)(const Plan, const RunDev, const int, const Queue, const Queue,
                             const Queue, const int, const LensArgs);
 
-template <bool kOut, bool kStaged>
+template <bool kOut, bool kStaged, bool kRing>
 LensKernel lens_kernel32(int force) {
+  using M = Mol32<kOut, false>;
   switch (force) {
-    case kForceStark2: return k_lens_chunk<Mol32<kOut, false>, kOut, kForceStark2, false, kStaged>;
-    case kForceStark1: return k_lens_chunk<Mol32<kOut, false>, kOut, kForceStark1, false, kStaged>;
-    default: return k_lens_chunk<Mol32<kOut, false>, kOut, kForceRadial, false, kStaged>;
+    case kForceStark2: return k_lens_chunk<M, kOut, kForceStark2, false, kStaged, false, kRing>;
+    case kForceStark1: return k_lens_chunk<M, kOut, kForceStark1, false, kStaged, false, kRing>;
+    default: return k_lens_chunk<M, kOut, kForceRadial, false, kStaged, false, kRing>;
   }
 }
 
-template <bool k64, bool kOut>
+template <bool k64, bool kOut, bool kRing = false>
 LensKernel lens_kernel(int force, bool staged) {
   if (k64) return k_lens_chunk<Mol64<false>, kOut, 0, true, false>;
-  return staged ? lens_kernel32<kOut, true>(force) : lens_kernel32<kOut, false>(force);
+  return staged ? lens_kernel32<kOut, true, kRing>(force) : lens_kernel32<kOut, false, kRing>(force);
 }
 
 // k_front, then for each lens: read the lens queue's size and largest
@@ -331,14 +334,16 @@ LensKernel lens_kernel(int force, bool staged) {
 // ceil(max / chunk) chunk kernels that ping-pong between two queues while
 // molecules leaving the lens collect in a third for the next lens.
 // *left receives the molecules still in a lens afterwards (always 0).
-template <bool k64, bool kOut>
-int launch_all(ctraj_context* c, const Plan& P, const RunDev& R, Queue* q, int* launches) {
+template <bool k64, bool kOut, bool kRing = false>
+int launch_all(ctraj_context* c, const Plan& P, const RunDev& R0, Queue* q, int* launches) {
   using MolT = typename std::conditional<k64, Mol64<false>, Mol32<kOut, false>>::type;
+  RunDev R = R0;  // ring recording fills in the staging buffers once the lens count is known
+  unsigned ring_slots = 0;
   const int64_t n = R.n;
   cudaStream_t s = c->stream;
   if (c->timing) CT_CUDA(cudaEventRecord(c->ev[0], s));
   if (n > 0) {
-    auto kf = k_front<MolT, kOut>;
+    auto kf = k_front<MolT, kOut, kRing>;
     int bps = blocks_per_sm(kf, kThreads, 0);
     int64_t want = (n + kThreads - 1) / kThreads;
     int grid = int(std::min<int64_t>(want, int64_t(bps) * c->sm_count * c->front_waves));
@@ -360,7 +365,26 @@ int launch_all(ctraj_context* c, const Plan& P, const RunDev& R, Queue* q, int* 
     CT_CUDA(cudaMemsetAsync(q[nxt].count, 0, kCtlWords * sizeof(unsigned), s));
     const bool staged = !k64 && P.lf[i].n_smem > 0;
     const size_t smem = staged ? size_t(P.lf[i].n_int) * sizeof(float4) : 0;
-    LensKernel kl = lens_kernel<k64, kOut>(P.lf[i].force, staged);
+    LensKernel kl = lens_kernel<k64, kOut, kRing>(P.lf[i].force, staged);
+    if (kRing && i == R.rec_lens) {
+      // staging: per lens entrant (record slot) the records and five scalars
+      R.rec_max = int(max_steps / unsigned(R.rec_stride)) + 3;
+      const size_t recb = align256(size_t(count) * size_t(R.rec_max) * sizeof(float4));
+      const size_t sb = align256(size_t(count) * 4);
+      int st = c->rec_stage.ensure(recb + 5 * sb + 2 * align256(size_t(count) * 8));
+      if (st) return st;
+      char* b = c->rec_stage.as<char>();
+      R.rec = reinterpret_cast<float4*>(b);
+      R.rec_n = reinterpret_cast<int32_t*>(b + recb);
+      R.rec_last = reinterpret_cast<int32_t*>(b + recb + sb);
+      R.rec_id = reinterpret_cast<int32_t*>(b + recb + 2 * sb);
+      R.rec_t0 = reinterpret_cast<float*>(b + recb + 3 * sb);
+      R.rec_vz = reinterpret_cast<float*>(b + recb + 4 * sb);
+      R.rec_r0 = reinterpret_cast<unsigned long long*>(b + recb + 5 * sb);
+      R.rec_m0 = reinterpret_cast<unsigned long long*>(b + recb + 5 * sb + align256(size_t(count) * 8));
+      CT_CUDA(cudaMemsetAsync(R.rec_n, 0, sb, s));
+      ring_slots = count;
+    }
     CT_CUDA(cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     const int64_t per_launch = int64_t(blocks_per_sm(kl, kLensThreads, smem)) * c->sm_count;
     const int grid =
@@ -394,6 +418,15 @@ int launch_all(ctraj_context* c, const Plan& P, const RunDev& R, Queue* q, int* 
     // the last chunk's continuation queue must be empty
     CT_CUDA(cudaMemcpyAsync(c->host_max + 2 + i, in.count, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     std::swap(cur, nxt);  // the next lens starts from the molecules queued at its entrance
+  }
+  if (kRing && n > 0) {  // also when no molecule reached the lens: entrance losses
+    k_ring_reserve<<<c->sm_count * 8, 256, 0, s>>>(R, ring_slots);
+    CT_CUDA(cudaGetLastError());
+    if constexpr (!k64) {
+      k_ring_write<Mol32<false, false>><<<c->sm_count * 8, 256, 0, s>>>(P, R, ring_slots);
+      CT_CUDA(cudaGetLastError());
+    }
+    *launches += 2;
   }
   if (c->timing) {
     if (!started) CT_CUDA(cudaEventRecord(c->ev[2], s));
@@ -443,6 +476,7 @@ int prepare(ctraj_context* c, const ctraj_run_args* a, Plan& P, RunDev& R) {
   if ((st = build_plan(c, a, P))) return st;
   std::memset(&R, 0, sizeof R);
   R.n = a->n;
+  R.rec_lens = -1;
   R.seed = a->seed;
   R.offset = a->offset;
   R.ic_mode = a->ic_mode;
@@ -518,6 +552,8 @@ int ctraj_destroy(ctraj_context* c) {
   c->rec_ids.release();
   c->rec_count.release();
   c->chunk_ctl.release();
+  c->rec_stage.release();
+  c->ring_ent.release();
   if (c->sweep_exec) cudaGraphExecDestroy(c->sweep_exec);
   for (int t = 0; t < CTRAJ_MAX_TABLES; ++t) {
     if (c->side[t]) cudaStreamSynchronize(c->side[t]);
@@ -631,13 +667,36 @@ int ctraj_set_force_table(ctraj_context* c, int32_t id, const ctraj_force_table*
   return CTRAJ_OK;
 }
 
-int ctraj_run(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* stats) {
+// ctraj_run, and with ring != NULL ctraj_run_ring.
+static int run_impl(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* stats, const ctraj_ring* ring) {
   if (!c) return fail(CTRAJ_EINVAL, "ctx is NULL");
   int st = validate_run(c, a);
   if (st) return st;
   Plan P;
   RunDev R;
   if ((st = prepare(c, a, P, R))) return st;
+  if (ring) {
+    if (a->precision != 32) return fail(CTRAJ_EINVAL, "ring recording runs in precision 32 only");
+    if (!ring->rows || !ring->index || !ring->heads || ring->capacity_rows < 1 || ring->capacity_molecules < 1 ||
+        ring->stride < 1)
+      return fail(CTRAJ_EINVAL, "bad ring (buffers, capacities >= 1, stride >= 1)");
+    if (ring->lens != P.first_lens || P.first_lens >= P.n_el)
+      return fail(CTRAJ_EINVAL, "the recorded lens must be the first lens of the beamline (element %d)",
+                  P.first_lens);
+    R.rec_lens = ring->lens;
+    R.rec_stride = ring->stride;
+    R.rec_entrance_label = P.el[ring->lens].label;
+    R.ring = *ring;
+    // list of the molecules stopped by the entrance test: count | ids | rows taken | entries taken
+    const size_t m = size_t(std::max<int64_t>(a->n, 1));
+    if ((st = c->ring_ent.ensure(256 + align256(m * 4) + 2 * align256(m * 8)))) return st;
+    char* b = c->ring_ent.as<char>();
+    R.ent_count = reinterpret_cast<unsigned*>(b);
+    R.ent_id = reinterpret_cast<int32_t*>(b + 256);
+    R.ent_r0 = reinterpret_cast<unsigned long long*>(b + 256 + align256(m * 4));
+    R.ent_m0 = reinterpret_cast<unsigned long long*>(b + 256 + align256(m * 4) + align256(m * 8));
+    CT_CUDA(cudaMemsetAsync(R.ent_count, 0, 4, c->stream));
+  }
   const int64_t n = a->n;
   const size_t cap = size_t(std::max<int64_t>(n, 1));
   int n_lens = 0;
@@ -645,7 +704,7 @@ int ctraj_run(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* stats)
   // two queues per lens (chunk ping-pong) plus one collecting the next lens's entrants
   const int n_queues = n_lens == 0 ? 1 : (n_lens == 1 ? 2 : 3);
   for (int k = 0; k < n_queues; ++k)
-    if ((st = c->queue[k].ensure(queue_bytes(cap, a->precision)))) return st;
+    if ((st = c->queue[k].ensure(queue_bytes(cap, a->precision, ring != nullptr)))) return st;
   unsigned* ctl = c->qctl.as<unsigned>();
   unsigned long long* counts = c->qctl.as<unsigned long long>(256);
   unsigned long long* dstats = c->qctl.as<unsigned long long>(256 + 8 * (CTRAJ_MAX_LABELS + 1));
@@ -653,7 +712,8 @@ int ctraj_run(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* stats)
   // never written, because nothing follows the last lens
   Queue q[3];
   for (int k = 0; k < 3; ++k)
-    layout_queue(&c->queue[std::min(k, n_queues - 1)], cap, a->precision, ctl + kCtlWords * k, &q[k]);
+    layout_queue(&c->queue[std::min(k, n_queues - 1)], cap, a->precision, ctl + kCtlWords * k, &q[k],
+                 ring != nullptr);
   CT_CUDA(cudaMemsetAsync(c->qctl.p, 0, 4096, c->stream));
   R.counts = counts;
   R.stats = dstats;
@@ -674,7 +734,10 @@ int ctraj_run(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* stats)
   int launches = 0;
   std::memset(c->host_max, 0, (2 + CTRAJ_MAX_ELEMENTS) * sizeof(unsigned));
   c->timing = a->timing != 0;
-  if (a->precision == 32)
+  if (ring)
+    st = out ? launch_all<false, true, true>(c, P, R, q, &launches)
+             : launch_all<false, false, true>(c, P, R, q, &launches);
+  else if (a->precision == 32)
     st = out ? launch_all<false, true>(c, P, R, q, &launches) : launch_all<false, false>(c, P, R, q, &launches);
   else
     st = out ? launch_all<true, true>(c, P, R, q, &launches) : launch_all<true, false>(c, P, R, q, &launches);
@@ -716,6 +779,15 @@ int ctraj_run(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* stats)
     return fail(CTRAJ_ESTEPS, "%llu molecules have a non-finite or oversize lens step count rint(L/dz)",
                 hs[kStatBadSteps]);
   return CTRAJ_OK;
+}
+
+int ctraj_run(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* stats) {
+  return run_impl(c, a, stats, nullptr);
+}
+
+int ctraj_run_ring(ctraj_context* c, const ctraj_run_args* a, const ctraj_ring* ring, ctraj_run_stats* stats) {
+  if (!ring) return fail(CTRAJ_EINVAL, "ring is NULL");
+  return run_impl(c, a, stats, ring);
 }
 
 int ctraj_record(ctraj_context* c, const ctraj_run_args* a, const int64_t* ids, int64_t n_ids,

@@ -146,23 +146,51 @@ __device__ __forceinline__ bool enter_lens_front(M& m, const Plan& P, int li, Le
   return true;
 }
 
+// What push_lens stores in Queue::cfg: nothing, the given tag (a sweep's
+// configuration or a carried record slot), or the slot itself (a new record
+// slot for ring recording).
+enum : int { kTagNone = 0, kTagCarry = 1, kTagSlot = 2 };
+
 // Append the lanes with push == true to Q and raise Q's largest remaining
-// step count (all lanes call).
-template <bool kSweep = false, class M>
-__device__ __forceinline__ void push_lens(const Queue& Q, bool push, const M& m, const LensStep& st,
-                                          int cfg = 0) {
+// step count (all lanes call).  Returns the lane's slot.
+template <int kTag = kTagNone, class M>
+__device__ __forceinline__ unsigned push_lens(const Queue& Q, bool push, const M& m, const LensStep& st,
+                                              int tag = 0) {
   const unsigned slot = queue_slot(push, Q.count);
   if (push) {
     m.store(Q, slot, st);
-    if (kSweep) Q.cfg[slot] = cfg;
+    if (kTag == kTagCarry) Q.cfg[slot] = tag;
+    if (kTag == kTagSlot) Q.cfg[slot] = int(slot);
   }
   const unsigned rem = push ? unsigned(st.n_total < 0 ? st.bound : st.n_total - st.n_done) : 0u;
   const unsigned wmax = __reduce_max_sync(kFull, rem);
   if ((threadIdx.x & 31) == 0 && wmax) atomicMax(Q.max_steps, wmax);
+  return slot;
+}
+
+// Ring row r (mod capacity): x, y, z, vx, vy, vz, t, step.
+__device__ __forceinline__ void ring_row(const ctraj_ring& G, unsigned long long r, float x, float y, float z,
+                                         float vx, float vy, float vz, float t, float step) {
+  float4* row = reinterpret_cast<float4*>(G.rows + size_t(r % (unsigned long long)G.capacity_rows) * 8);
+  row[0] = make_float4(x, y, z, vx);
+  row[1] = make_float4(vy, vz, t, step);
+}
+
+__device__ __forceinline__ void ring_entry(const ctraj_ring& G, unsigned long long m, int64_t id,
+                                           unsigned long long first, int rows, int label) {
+  ctraj_ring_entry en;
+  en.molecule = id;
+  en.first_row = first;
+  en.rows = rows;
+  en.label = label;
+  G.index[m % (unsigned long long)G.capacity_molecules] = en;
 }
 
 // ---------------------------------------------------------------------------
-template <class M, bool kOut>
+// kRing (FP32 ring recording): the molecules queued at the recorded lens
+// (the first lens) get their queue slot as record slot, and those stopped by
+// its entrance test are appended to the ring at once.
+template <class M, bool kOut, bool kRing = false>
 __global__ void __launch_bounds__(kThreads) k_front(const __grid_constant__ Plan P, const RunDev R,
                                                     const Queue Q) {
   __shared__ BlockTally S;
@@ -189,8 +217,11 @@ __global__ void __launch_bounds__(kThreads) k_front(const __grid_constant__ Plan
         band += (m.margin < double(kEdgeBand)) ? 1 : 0;
         write_outputs<M, kOut>(R, m, label);
       }
+      if constexpr (kRing) {  // listed; k_ring_reserve / k_ring_write append them
+        if (label == R.rec_entrance_label && lens_at == R.rec_lens) R.ent_id[atomicAdd(R.ent_count, 1u)] = int32_t(i);
+      }
     }
-    push_lens(Q, label == kQueued, m, st);
+    push_lens<kRing ? kTagSlot : kTagNone>(Q, label == kQueued, m, st);
     tally_warp(S, label, P.n_labels);
   }
   stat_add(S, kStatSteps, steps);
@@ -230,7 +261,7 @@ __global__ void __launch_bounds__(kThreads) k_sweep_front(const __grid_constant_
       }
       if (label != kQueued) steps += unsigned(m.rows);
     }
-    for (int t = 0; t < n_tables; ++t) push_lens<true>(Qs.q[t], label == kQueued && tab == t, m, st, cfg);
+    for (int t = 0; t < n_tables; ++t) push_lens<kTagCarry>(Qs.q[t], label == kQueued && tab == t, m, st, cfg);
     tally_warp(S, label, P.n_labels);
     tally_cfg(R, cfg, label, P.n_labels);
   }
@@ -245,7 +276,11 @@ enum : int { kIdle = 0, kRun = 1, kLost = 2, kExit = 3, kBad = 4 };
 // kSweep (batched sweeps, FP32 only): every molecule carries its configuration;
 // the staged table is unscaled and the configuration's beta and kappa scale it;
 // tallies are also kept per configuration.
-template <class M, bool kOut, int F, bool k64, bool kStaged, bool kSweep = false>
+// kRing (ring recording, FP32 only): in the recorded lens every molecule
+// carries its record slot and stages (x, y, vx, vy) at its entrance, after
+// every rec_stride-th step and where it is lost; k_ring_gather appends the
+// records of the molecules lost inside to the ring.
+template <class M, bool kOut, int F, bool k64, bool kStaged, bool kSweep = false, bool kRing = false>
 __global__ void __launch_bounds__(kLensThreads, 2) k_lens_chunk(const __grid_constant__ Plan P, const RunDev R,
                                                          const int li, const Queue Qin,
                                                          const Queue Qcont, const Queue Qnext,
@@ -287,12 +322,21 @@ __global__ void __launch_bounds__(kLensThreads, 2) k_lens_chunk(const __grid_con
     int n0 = 0, cfg = 0;
     float beta = 0.f, kappa = 0.f;
     bool fresh = false;
+    int tag = 0, to_rec = 0;
+    const bool rec_on = kRing && li == R.rec_lens;
     if (idx < n_in) {
       m.load_state(Qin, idx, P, st);
       if (kSweep) {
         const int c = Qin.cfg[idx];
         beta = __ldg(R.cfg_beta + c);
         kappa = __ldg(R.cfg_kappa + c);
+      }
+      if constexpr (kRing) {
+        if (rec_on) {
+          tag = Qin.cfg[idx];
+          to_rec = R.rec_stride - st.n_done % R.rec_stride;
+          if (st.n_done == 0) R.rec[size_t(tag) * R.rec_max] = make_float4(m.x, m.y, m.vx, m.vy);
+        }
       }
       bool ok = true;
       fresh = st.n_total < 0;
@@ -322,6 +366,12 @@ __global__ void __launch_bounds__(kLensThreads, 2) k_lens_chunk(const __grid_con
         }
         ++st.n_done;
         m.lens_row(P, li, st);
+        if constexpr (kRing) {
+          if (rec_on && --to_rec == 0) {
+            to_rec = R.rec_stride;
+            R.rec[size_t(tag) * R.rec_max + st.n_done / R.rec_stride] = make_float4(m.x, m.y, m.vx, m.vy);
+          }
+        }
         if (lost) phase = kLost;
         else if (st.n_done == st.n_total) phase = kExit;
       }
@@ -331,6 +381,23 @@ __global__ void __launch_bounds__(kLensThreads, 2) k_lens_chunk(const __grid_con
     if (idx < n_in) {
       m.load_rest(Qin, idx, st, !fresh);
       if (kSweep) cfg = Qin.cfg[idx];
+    }
+    if constexpr (kRing) {
+      if (rec_on && idx < n_in && phase != kRun) {
+        int n_rec = 0;
+        if (phase == kLost) {  // the state after the losing step closes the record
+          const int s = R.rec_stride, k = st.n_done;
+          if (k % s != 0) R.rec[size_t(tag) * R.rec_max + k / s + 1] = make_float4(m.x, m.y, m.vx, m.vy);
+          n_rec = k / s + 1 + (k % s != 0 ? 1 : 0);
+          R.rec_last[tag] = k;
+        }
+        R.rec_n[tag] = n_rec;  // 0: left the lens (or unusable step count), not recorded
+      }
+      if (rec_on && idx < n_in && fresh) {
+        R.rec_id[tag] = m.id;
+        R.rec_t0[tag] = m.t;
+        R.rec_vz[tag] = m.vz;
+      }
     }
     lsteps += unsigned(st.n_done - n0);
     int label = kNone;
@@ -363,8 +430,8 @@ __global__ void __launch_bounds__(kLensThreads, 2) k_lens_chunk(const __grid_con
         write_outputs<M, kOut>(R, m, label);
       }
     }
-    push_lens<kSweep>(Qcont, phase == kRun, m, st, cfg);
-    push_lens<kSweep>(Qnext, enter, m, nst, cfg);
+    push_lens<(kSweep || kRing) ? kTagCarry : kTagNone>(Qcont, phase == kRun, m, st, kRing ? tag : cfg);
+    push_lens<(kSweep || kRing) ? kTagCarry : kTagNone>(Qnext, enter, m, nst, kRing ? tag : cfg);
     tally_warp(S, label, P.n_labels);
     if (kSweep) tally_cfg(R, cfg, label, P.n_labels);
   }
@@ -375,6 +442,79 @@ __global__ void __launch_bounds__(kLensThreads, 2) k_lens_chunk(const __grid_con
   stat_add(S, kStatTableRange, range);
   stat_add(S, kStatRangeError, rerr);
   tally_flush(S, R, P.n_labels);
+}
+
+// ---------------------------------------------------------------------------
+// Ring recording, appended in two launches so that no write lands on a newer
+// one: k_ring_reserve takes each record's rows and index entry from the heads
+// (molecules lost inside the recorded lens: rec_n > 0 staged records;
+// molecules stopped by its entrance test: one record each), k_ring_write then
+// reads the final heads and writes only what lies within the last
+// capacity_rows rows / capacity_molecules entries, where positions are
+// distinct.  One thread per record slot or listed molecule.
+__global__ void __launch_bounds__(256) k_ring_reserve(const RunDev R, unsigned n_slots) {
+  const ctraj_ring& G = R.ring;
+  const unsigned n_ent = *R.ent_count;
+  const unsigned stride = gridDim.x * blockDim.x;
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n_slots + n_ent; s += stride) {
+    const bool lens = s < n_slots;
+    const int n_rec = lens ? R.rec_n[s] : 1;
+    if (n_rec <= 0) continue;
+    const unsigned long long r0 = atomicAdd(&G.heads[0], (unsigned long long)n_rec);
+    const unsigned long long m0 = atomicAdd(&G.heads[1], 1ull);
+    if (lens) {
+      R.rec_r0[s] = r0;
+      R.rec_m0[s] = m0;
+    } else {
+      R.ent_r0[s - n_slots] = r0;
+      R.ent_m0[s - n_slots] = m0;
+    }
+  }
+}
+
+// z and t of a record after k RK4 steps are z0 + k dz and t0 + k dt with the
+// molecule's own step (electrostatic_lens.py:87-88), in double, as the
+// trajectory rows of the replay kernel have them.  A molecule stopped by the
+// entrance test is re-walked from its initial conditions to the entrance.
+template <class M>
+__global__ void __launch_bounds__(256) k_ring_write(const __grid_constant__ Plan P, const RunDev R,
+                                                    unsigned n_slots) {
+  const ctraj_element& e = P.el[R.rec_lens];
+  const ctraj_ring& G = R.ring;
+  const unsigned n_ent = *R.ent_count;
+  const unsigned long long hr = G.heads[0], hm = G.heads[1];
+  const unsigned long long cr = (unsigned long long)G.capacity_rows, cm = (unsigned long long)G.capacity_molecules;
+  const unsigned stride = gridDim.x * blockDim.x;
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n_slots + n_ent; s += stride) {
+    if (s < n_slots) {
+      const int n_rec = R.rec_n[s];
+      if (n_rec <= 0) continue;
+      const unsigned long long r0 = R.rec_r0[s], m0 = R.rec_m0[s];
+      const float vz = R.rec_vz[s];
+      LensStep st;
+      lens_setup(e, double(vz), st);
+      const int last = R.rec_last[s];
+      const double t0 = double(R.rec_t0[s]);
+      for (int j = 0; j < n_rec; ++j) {
+        if (r0 + j + cr < hr) continue;  // overwritten by a newer record
+        const int k = j == n_rec - 1 ? last : j * R.rec_stride;
+        const float4 a = R.rec[size_t(s) * R.rec_max + j];
+        ring_row(G, r0 + j, a.x, a.y, float(e.z0 + double(k) * st.dz), a.z, a.w, vz,
+                 float(t0 + double(k) * st.dt), float(k));
+      }
+      if (m0 + cm >= hm) ring_entry(G, m0, R.rec_id[s], r0, n_rec, e.label_inside);
+    } else {
+      const unsigned k = s - n_slots;
+      const unsigned long long r0 = R.ent_r0[k], m0 = R.ent_m0[k];
+      const int32_t id = R.ent_id[k];
+      M m;
+      m.init(P, R, id);
+      int lens_at = -1;
+      const int label = walk(m, P, 0, &lens_at);
+      if (r0 + cr >= hr) ring_row(G, r0, m.x, m.y, float(e.z0), m.vx, m.vy, m.vz, m.t, 0.0f);
+      if (m0 + cm >= hm) ring_entry(G, m0, id, r0, 1, label);
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -665,8 +665,8 @@ __device__ int walk(M& m, const Plan& P, int from, int* lens_at) {
         break;
       case CTRAJ_ELECTROSTATIC_LENS:
         m.fly(P, i, 0);
+        *lens_at = i;  // also reported for a loss at the entrance test
         if (m.lens_entrance_out(P, i)) return e.label;
-        *lens_at = i;
         return kQueued;
       default:
         return e.label;

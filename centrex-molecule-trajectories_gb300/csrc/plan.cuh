@@ -119,6 +119,27 @@ struct RunDev {
   const float* cfg_kappa;     // n_cfg
   const int32_t* cfg_table;   // n_cfg: which lens queue / table
   unsigned long long* cfg_counts;  // n_cfg x (n_labels + 1)
+  // ring recording (ctraj_run_ring): the molecules reaching lens rec_lens get
+  // a record slot (their queue position at the front, carried in Queue::cfg);
+  // (x, y, vx, vy) is staged every rec_stride RK4 steps, and the molecules
+  // lost on the lens are appended to the ring by k_ring_gather.
+  int rec_lens;               // -1: off
+  int rec_stride;
+  int rec_max;                // staged records per slot
+  int rec_entrance_label;     // counter slot of the recorded lens's entrance test
+  float4* rec;                // (slots, rec_max)
+  int32_t* rec_n;             // per slot: records staged if lost inside the lens, else 0
+  int32_t* rec_last;          // per slot: RK4 steps done when lost
+  int32_t* rec_id;            // per slot: molecule index
+  float* rec_t0;              // per slot: time at the lens entrance
+  float* rec_vz;
+  unsigned long long* rec_r0; // per slot: first ring row and index entry taken
+  unsigned long long* rec_m0;
+  int32_t* ent_id;            // molecules stopped by the entrance test (listed by k_front)
+  unsigned* ent_count;
+  unsigned long long* ent_r0;
+  unsigned long long* ent_m0;
+  ctraj_ring ring;
 };
 
 enum : int {
@@ -146,7 +167,7 @@ struct Queue {
   int32_t* id;
   int32_t* n_done;
   int32_t* n_total;
-  int32_t* cfg;         // configuration of the molecule (batched sweeps only)
+  int32_t* cfg;         // configuration (batched sweeps) or record slot (ring recording)
   unsigned int* count;      // entries written
   unsigned int* max_steps;  // largest n_total - n_done written (sizes the chunk loop)
   unsigned int* head;       // entries taken by the warps of the kernel reading the queue

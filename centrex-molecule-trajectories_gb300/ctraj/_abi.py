@@ -155,6 +155,27 @@ class Sweep(ctypes.Structure):
 
 MAX_SWEEP_CONFIGS = 65536
 
+
+class RingEntry(ctypes.Structure):
+    _fields_ = [
+        ("molecule", ctypes.c_int64),
+        ("first_row", ctypes.c_uint64),
+        ("rows", ctypes.c_int32),
+        ("label", ctypes.c_int32),
+    ]
+
+
+class Ring(ctypes.Structure):
+    _fields_ = [
+        ("rows", ctypes.c_void_p),
+        ("capacity_rows", ctypes.c_int64),
+        ("index", ctypes.c_void_p),
+        ("capacity_molecules", ctypes.c_int64),
+        ("heads", ctypes.c_void_p),
+        ("stride", ctypes.c_int32),
+        ("lens", ctypes.c_int32),
+    ]
+
 SOFT_NPARAMS = 6
 SOFT_V, SOFT_LENS_Z0, SOFT_APERTURE_R, SOFT_BORE_R, SOFT_SIGMA_VX, SOFT_SIGMA_VY = range(6)
 
@@ -212,6 +233,7 @@ SIGNATURES = {
     "ctraj_run_sweep": (ctypes.c_int, [_P, ctypes.POINTER(Sweep), ctypes.POINTER(RunArgs), _P,
                                        ctypes.POINTER(RunStats)]),
     "ctraj_soft_transmission": (ctypes.c_int, [_P, ctypes.POINTER(SoftArgs), _P, ctypes.POINTER(SoftResult)]),
+    "ctraj_run_ring": (ctypes.c_int, [_P, ctypes.POINTER(RunArgs), ctypes.POINTER(Ring), ctypes.POINTER(RunStats)]),
     "ctraj_run_noalloc": (ctypes.c_int, [ctypes.POINTER(Element), ctypes.c_int32, ctypes.c_int32,
                                          ctypes.POINTER(ForceTable), ctypes.c_int32,
                                          ctypes.POINTER(RunArgs), _P, ctypes.POINTER(RunStats)]),

@@ -182,7 +182,9 @@ class Engine:
 
     def run(self, cb: CompiledBeamline, n: int, precision: int = 32, ics=None, xdist=None,
             vdist=None, seed: int = 0, offset: int = 0, g: float = G, outputs: bool = False,
-            device_outputs: dict | None = None, timing: bool = False) -> RunResult:
+            device_outputs: dict | None = None, timing: bool = False, ring=None) -> RunResult:
+        """ctraj_run; with ``ring`` (a ctraj.ring.HBMRing) ctraj_run_ring, which
+        also appends the molecules lost on the first lens to the ring."""
         self.load(cb)
         a, keep = self._args(n, precision, ics, xdist, vdist, seed, offset, g)
         a.timing = 1 if timing else 0
@@ -205,7 +207,12 @@ class Engine:
             a.out_label, a.out_final = label.ctypes.data, final.ctypes.data
             a.out_rows, a.out_margin = rows.ctypes.data, margin.ctypes.data
         st = _abi.RunStats()
-        status = self.lib.ctraj_run(self.ctx, ctypes.byref(a), ctypes.byref(st))
+        if ring is None:
+            status = self.lib.ctraj_run(self.ctx, ctypes.byref(a), ctypes.byref(st))
+        else:
+            lenses = [i for i, e in enumerate(cb.elements) if e.type == _abi.ELECTROSTATIC_LENS]
+            rs = ring.struct(lenses[0] if lenses else -1)
+            status = self.lib.ctraj_run_ring(self.ctx, ctypes.byref(a), ctypes.byref(rs), ctypes.byref(st))
         del keep
         _abi.check(status, self.lib)
         if st.timed:

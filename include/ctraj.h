@@ -287,6 +287,43 @@ int ctraj_record(ctraj_context* ctx, const ctraj_run_args* args,
  * The chunk sequence is sized without a device-to-host read: its last chunk
  * runs every molecule still inside the lens to the end.
  */
+/*
+ * Ring recording of the molecules lost on one lens.  Replaces keeping full
+ * Trajectory objects for apertures of interest (trajectory_simulator.py:75-76,
+ * molecule.py:111-167) when the run is too large to replay: during the run
+ * itself, every molecule that reaches the lens is staged every `stride` RK4
+ * steps; the ones lost on it (label "Inside lens", plus "Lens entrance" for
+ * those stopped by the entrance test) are appended to a caller-owned device
+ * ring of rows.  A molecule's records are: the lens entrance state (step 0),
+ * the state after every stride-th RK4 step, and the state where it was lost.
+ * Rows are float32 (x, y, z, vx, vy, vz, t, step); row r of the run is stored
+ * at rows[(r mod capacity_rows) * 8].  heads[0] and heads[1] count the rows and
+ * molecules appended so far (monotone; the caller zeroes them to start a new
+ * ring); molecule m's entry is index[m mod capacity_molecules].  Older
+ * records are overwritten once a head passes the capacity.  FP32 runs only;
+ * the recorded lens must be the first lens of the beamline.
+ */
+typedef struct ctraj_ring_entry {
+  int64_t molecule;   /* index of the molecule in the run (Philox counter - offset) */
+  uint64_t first_row; /* value of heads[0] when its rows were appended          */
+  int32_t rows;
+  int32_t label;      /* counter slot it was lost on                             */
+} ctraj_ring_entry;
+
+typedef struct ctraj_ring {
+  float* rows;                /* device: capacity_rows x 8 */
+  int64_t capacity_rows;
+  ctraj_ring_entry* index;    /* device: capacity_molecules */
+  int64_t capacity_molecules;
+  unsigned long long* heads;  /* device: 2 counters */
+  int32_t stride;             /* RK4 steps between records (>= 1) */
+  int32_t lens;               /* element index of the recorded lens */
+} ctraj_ring;
+
+/* ctraj_run plus ring recording (args as for ctraj_run, precision 32). */
+int ctraj_run_ring(ctraj_context* ctx, const ctraj_run_args* args,
+                   const ctraj_ring* ring, ctraj_run_stats* stats);
+
 #define CTRAJ_MAX_SWEEP_CONFIGS 65536
 typedef struct ctraj_sweep {
   int32_t n_configs;

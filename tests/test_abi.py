@@ -56,10 +56,10 @@ def test_struct_layout_matches_header():
     #include <stddef.h>
     #include "ctraj.h"
     int main(void) {
-      printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(ctraj_element), sizeof(ctraj_force_table),
+      printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(ctraj_element), sizeof(ctraj_force_table),
              sizeof(ctraj_distribution), sizeof(ctraj_run_args), sizeof(ctraj_run_stats),
              sizeof(ctraj_tuning), sizeof(ctraj_sweep), sizeof(ctraj_soft_args),
-             sizeof(ctraj_soft_result));
+             sizeof(ctraj_soft_result), sizeof(ctraj_ring_entry), sizeof(ctraj_ring));
       printf("%zu %zu %zu %zu\n", offsetof(ctraj_element, z0), offsetof(ctraj_element, p),
              offsetof(ctraj_run_args, g), offsetof(ctraj_run_args, counts));
       return 0;
@@ -75,7 +75,8 @@ def test_struct_layout_matches_header():
                                             ctypes.sizeof(_abi.Distribution), ctypes.sizeof(_abi.RunArgs),
                                             ctypes.sizeof(_abi.RunStats), ctypes.sizeof(_abi.Tuning),
                                             ctypes.sizeof(_abi.Sweep), ctypes.sizeof(_abi.SoftArgs),
-                                            ctypes.sizeof(_abi.SoftResult)]
+                                            ctypes.sizeof(_abi.SoftResult), ctypes.sizeof(_abi.RingEntry),
+                                            ctypes.sizeof(_abi.Ring)]
     assert list(map(int, offs.split())) == [_abi.Element.z0.offset, _abi.Element.p.offset,
                                            _abi.RunArgs.g.offset, _abi.RunArgs.counts.offset]
 
