@@ -70,6 +70,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-sweep", action="store_true", help="skip the batched-sweep measurement")
     p.add_argument("--no-adjoint", action="store_true", help="skip the gradient measurement")
+    p.add_argument("--no-large", action="store_true", help="skip the 1e9-molecule streamed run and the Adam tuning")
     p.add_argument("--profile", action="store_true",
                    help="only run the workload --steps times with the default launch knobs "
                         "(the command the ncu captures under profiles/ use)")
@@ -388,6 +389,57 @@ def bench_adjoint(eng, stream, flush, steps: int, warmup: int):
             "timing": "CUDA events on the launching stream around the call (result on the host), L2 flushed before each"}
 
 
+def bench_large(eng, stream, flush, n_total: int = 1_000_000_000, chunk: int = 134_000_000):
+    """The lens beamline at 1e9 molecules, streamed in runs of 1.34e8 with the
+    molecules lost on the lens recorded every 50 RK4 steps into an HBM ring,
+    then 200 Adam steps on (lens V, lens z0) through the adjoint at 1e6
+    molecules per step."""
+    import numpy as np
+    import torch
+
+    from ctraj.adjoint import SoftProblem, soft_transmission
+    from ctraj.compiler import compile_beamline
+    from ctraj.distributions import device_spec
+    from ctraj.ring import HBMRing
+    from ctraj.stream import adam_tune, run_streamed
+    from ctraj.workloads import lens_beamline, source
+
+    cb = compile_beamline(lens_beamline())
+    xd, vd = source()
+    xs, vs = device_spec(xd, "position"), device_spec(vd, "velocity")
+    ring = HBMRing(capacity_rows=200_000_000, capacity_molecules=20_000_000, stride=50)
+    run_streamed(cb, 2_000_000, chunk=chunk, xdist=xs, vdist=vs, seed=1, ring=ring, engine=eng)  # warm-up
+    ring.reset()
+    torch.cuda.synchronize()
+    flush.zero_()
+    t0 = time.perf_counter()
+    st = run_streamed(cb, n_total, chunk=chunk, xdist=xs, vdist=vs, seed=2, ring=ring, engine=eng)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    rows, mols = ring.counts()
+    # Adam on V and z0
+    prob = SoftProblem.from_beamline(lens_beamline(), n=1_000_000, aperture="A1", precision=32)
+    p0 = prob.initial_params()
+    adam_tune(prob, steps=3, engine=eng)  # warm-up
+    opt = adam_tune(prob, which=("V", "lens_z0"), steps=200, lr=0.01, engine=eng, seed0=1000)
+    prob.seed = 99
+    before = soft_transmission(prob, p0, want_grad=False, engine=eng).loss
+    after = soft_transmission(prob, opt["params"], want_grad=False, engine=eng).loss
+    return {"workload": f"lens beamline, {n_total:.0e} molecules streamed in runs of {chunk:.3g}, "
+                        "molecules lost on the lens recorded every 50 RK4 steps into an HBM ring; "
+                        "then 200 Adam steps on (lens V, lens z0) at 1e6 molecules per step",
+            "molecules": n_total, "runs": st.chunks, "molecule_steps": st.molecule_steps,
+            "seconds": wall, "molecule_steps_per_s": st.molecule_steps / wall,
+            "kernel_ms_sum": float(sum(st.chunk_ms)), "gpu_launches": st.kernels,
+            "counts": st.counter_dict(), "ring_rows": rows, "ring_molecules": mols,
+            "ring_capacity_rows": ring.capacity_rows,
+            "adam": {"steps": 200, "seconds": opt["seconds"], "steps_per_s": 200 / opt["seconds"],
+                     "V_start": float(p0[0]), "V_end": float(opt["params"][0]),
+                     "z0_start": float(p0[1]), "z0_end": float(opt["params"][1]),
+                     "soft_transmission_start": before, "soft_transmission_end": after},
+            "timing": "wall clock (perf_counter) around the streamed runs incl. host syncs between runs"}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -509,6 +561,7 @@ def main():
     sweep = None if args.no_sweep else bench_sweep(eng, stream, flush, args.steps, args.warmup,
                                                    torch.cuda.get_device_name(local))
     adjoint = None if args.no_adjoint else bench_adjoint(eng, stream, flush, args.steps, args.warmup)
+    large = None if args.no_large else bench_large(eng, stream, flush)
     achieved = lens_steps * FLOP_PER_RK4_STEP / (lens_ms / 1e3) / 1e12
     roofline = {"bound": "fp32", "kernel": "k_lens (RK4 through the hexapole lens)",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
@@ -529,7 +582,7 @@ def main():
                        "parallelism": f"replicas x{world}",
                        "tuning": tuned["tuning"], "tuning_cached": tuned.get("cached", False)},
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "sweep": sweep,
-            "adjoint": adjoint,
+            "adjoint": adjoint, "large": large,
             "gpu_launches": int(sum(r.kernels for r in results)),
             "molecule_steps_per_step": steps / args.steps, "counts_last_step": r0.counter_dict()}
     print(json.dumps(line), flush=True)

@@ -502,7 +502,7 @@ __global__ void __launch_bounds__(256) k_ring_write(const __grid_constant__ Plan
         ring_row(G, r0 + j, a.x, a.y, float(e.z0 + double(k) * st.dz), a.z, a.w, vz,
                  float(t0 + double(k) * st.dt), float(k));
       }
-      if (m0 + cm >= hm) ring_entry(G, m0, R.rec_id[s], r0, n_rec, e.label_inside);
+      if (m0 + cm >= hm) ring_entry(G, m0, int64_t(R.offset) + R.rec_id[s], r0, n_rec, e.label_inside);
     } else {
       const unsigned k = s - n_slots;
       const unsigned long long r0 = R.ent_r0[k], m0 = R.ent_m0[k];
@@ -512,7 +512,7 @@ __global__ void __launch_bounds__(256) k_ring_write(const __grid_constant__ Plan
       int lens_at = -1;
       const int label = walk(m, P, 0, &lens_at);
       if (r0 + cr >= hr) ring_row(G, r0, m.x, m.y, float(e.z0), m.vx, m.vy, m.vz, m.t, 0.0f);
-      if (m0 + cm >= hm) ring_entry(G, m0, id, r0, 1, label);
+      if (m0 + cm >= hm) ring_entry(G, m0, int64_t(R.offset) + id, r0, 1, label);
     }
   }
 }

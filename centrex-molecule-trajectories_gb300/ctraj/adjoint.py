@@ -77,6 +77,19 @@ class SoftProblem:
     def lens(self):
         return [e for e in self.cb.elements if e.type == _abi.ELECTROSTATIC_LENS][0]
 
+    def param_bounds(self) -> np.ndarray:
+        """(6, 2) physical limits: V >= 0; the lens stays between the element in
+        front of it and the one behind it (1 mm clear); radii and velocity
+        spreads positive."""
+        els = list(self.cb.elements)
+        li = [i for i, e in enumerate(els) if e.type == _abi.ELECTROSTATIC_LENS][0]
+        L = els[li].z1 - els[li].z0
+        lo_z = (els[li - 1].z1 + 1e-3) if li > 0 else -np.inf
+        hi_z = (els[li + 1].z0 - L - 1e-3) if li + 1 < len(els) else np.inf
+        tiny = 1e-6
+        return np.array([[0.0, np.inf], [lo_z, hi_z], [tiny, np.inf], [tiny, np.inf], [tiny, np.inf],
+                         [tiny, np.inf]])
+
     def initial_params(self) -> np.ndarray:
         L = self.lens()
         r_ap = self.cb.elements[self.aperture].p[0] / 2 if self.aperture >= 0 else 0.0

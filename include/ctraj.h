@@ -304,7 +304,7 @@ int ctraj_record(ctraj_context* ctx, const ctraj_run_args* args,
  * the recorded lens must be the first lens of the beamline.
  */
 typedef struct ctraj_ring_entry {
-  int64_t molecule;   /* index of the molecule in the run (Philox counter - offset) */
+  int64_t molecule;   /* args->offset + index of the molecule in the run (its Philox counter) */
   uint64_t first_row; /* value of heads[0] when its rows were appended          */
   int32_t rows;
   int32_t label;      /* counter slot it was lost on                             */

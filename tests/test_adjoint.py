@@ -43,6 +43,10 @@ def test_initial_params_follow_the_beamline():
     np.testing.assert_allclose(p, [30e3, 0.80, 6e-3, 17.5e-3, 20.0, 20.0])
     with pytest.raises(ValueError):
         SoftProblem.from_beamline(lens_beamline(), n=10, aperture="nope")
+    lim = prob.param_bounds()
+    assert lim[0, 0] == 0.0  # V >= 0
+    # the 0.60 m lens stays between A1 (ends at 0.301 m) and the 3.0 m plane, 1 mm clear
+    np.testing.assert_allclose(lim[1], [0.302, 3.0 - 0.6 - 1e-3])
 
 
 def test_torch_reference_autograd_matches_finite_differences():
