@@ -71,9 +71,13 @@ def parse():
     p.add_argument("--no-sweep", action="store_true", help="skip the batched-sweep measurement")
     p.add_argument("--no-adjoint", action="store_true", help="skip the gradient measurement")
     p.add_argument("--no-large", action="store_true", help="skip the 1e9-molecule streamed run and the Adam tuning")
-    p.add_argument("--profile", action="store_true",
-                   help="only run the workload --steps times with the default launch knobs "
-                        "(the command the ncu captures under profiles/ use)")
+    p.add_argument("--profile", nargs="?", const="lens", default=None,
+                   choices=["lens", "sweep", "adjoint", "ring"],
+                   help="only run one workload --steps times with the default launch knobs (the commands "
+                        "the ncu captures under profiles/ use): the lens beamline (--molecules), the "
+                        "batched sweep (counts scaled by --sweep-scale), the gradient at 1e6 molecules, "
+                        "or a ring-recording run (--molecules)")
+    p.add_argument("--sweep-scale", type=float, default=1.0, help="molecule counts of --profile sweep x this")
     return p.parse_args()
 
 
@@ -90,11 +94,37 @@ def run_profile(args):
     xd, vd = source()
     xs, vs = device_spec(xd, "position"), device_spec(vd, "velocity")
     eng = Engine(0)
+    n = int(args.molecules)
     for k in range(args.steps):
-        r = eng.run(cb, int(args.molecules), xdist=xs, vdist=vs, seed=k, timing=True)
-        print(json.dumps({"run": k, "kernels": r.kernels, "front_ms": r.extra["front_ms"],
-                          "lens_ms": r.extra["lens_ms"], "molecule_steps": r.molecule_steps,
-                          "lens_steps": r.lens_steps, "counts": r.counter_dict()}), flush=True)
+        if args.profile == "sweep":
+            import numpy as np
+
+            from ctraj.sweep import run_sweep
+            from ctraj.workloads import sweep_configs
+
+            if k == 0:
+                cfg = sweep_configs()
+                cfg.n_molecules = np.maximum(1, np.rint(cfg.n_molecules * args.sweep_scale)).astype(np.int64)
+            r = run_sweep(cb, cfg, xdist=xs, vdist=vs, seed=k, timing=True, engine=eng)
+            out = {"molecules": cfg.total, "kernels": r.kernels, **r.extra, "molecule_steps": r.molecule_steps}
+        elif args.profile == "adjoint":
+            from ctraj.adjoint import SoftProblem, soft_transmission
+
+            prob = SoftProblem.from_beamline(lens_beamline(), n=1_000_000, aperture="A1", seed=k)
+            o = soft_transmission(prob, prob.initial_params(), engine=eng, timing=True)
+            out = {"loss": o.loss, "grad": o.grad.tolist(), "kernels": o.kernels, **o.extra}
+        else:
+            ring = None
+            if args.profile == "ring":
+                from ctraj.ring import HBMRing
+
+                ring = HBMRing(capacity_rows=50_000_000, capacity_molecules=5_000_000, stride=50)
+            r = eng.run(cb, n, xdist=xs, vdist=vs, seed=k, timing=True, ring=ring)
+            out = {"kernels": r.kernels, **r.extra, "molecule_steps": r.molecule_steps,
+                   "lens_steps": r.lens_steps, "counts": r.counter_dict()}
+            if ring is not None:
+                out["ring"] = ring.counts()
+        print(json.dumps({"run": k, "profile": args.profile, **out}), flush=True)
     eng.close()
 
 
