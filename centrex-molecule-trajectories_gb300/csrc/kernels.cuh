@@ -455,19 +455,39 @@ __global__ void __launch_bounds__(kLensThreads, 2) k_lens_chunk(const __grid_con
 __global__ void __launch_bounds__(256) k_ring_reserve(const RunDev R, unsigned n_slots) {
   const ctraj_ring& G = R.ring;
   const unsigned n_ent = *R.ent_count;
+  const unsigned total = n_slots + n_ent;
+  const int lane = threadIdx.x & 31;
   const unsigned stride = gridDim.x * blockDim.x;
-  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < n_slots + n_ent; s += stride) {
+  // warp-uniform loop; one pair of atomics per warp (prefix sums over the lanes)
+  for (unsigned base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total; base += stride) {
+    const unsigned s = base + lane;
     const bool lens = s < n_slots;
-    const int n_rec = lens ? R.rec_n[s] : 1;
-    if (n_rec <= 0) continue;
-    const unsigned long long r0 = atomicAdd(&G.heads[0], (unsigned long long)n_rec);
-    const unsigned long long m0 = atomicAdd(&G.heads[1], 1ull);
-    if (lens) {
-      R.rec_r0[s] = r0;
-      R.rec_m0[s] = m0;
-    } else {
-      R.ent_r0[s - n_slots] = r0;
-      R.ent_m0[s - n_slots] = m0;
+    const int n_rec = s < total ? (lens ? R.rec_n[s] : 1) : 0;
+    const bool take = n_rec > 0;
+    unsigned long long rows = (unsigned long long)(take ? n_rec : 0);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {  // inclusive scan of the row counts
+      const unsigned long long v = __shfl_up_sync(kFull, rows, o);
+      if (lane >= o) rows += v;
+    }
+    const unsigned mask = __ballot_sync(kFull, take);
+    unsigned long long rbase = 0, mbase = 0;
+    if (lane == 31) {
+      if (rows) rbase = atomicAdd(&G.heads[0], rows);
+      if (mask) mbase = atomicAdd(&G.heads[1], (unsigned long long)__popc(mask));
+    }
+    rbase = __shfl_sync(kFull, rbase, 31);
+    mbase = __shfl_sync(kFull, mbase, 31);
+    if (take) {
+      const unsigned long long r0 = rbase + rows - (unsigned long long)n_rec;
+      const unsigned long long m0 = mbase + __popc(mask & ((1u << lane) - 1u));
+      if (lens) {
+        R.rec_r0[s] = r0;
+        R.rec_m0[s] = m0;
+      } else {
+        R.ent_r0[s - n_slots] = r0;
+        R.ent_m0[s - n_slots] = m0;
+      }
     }
   }
 }
