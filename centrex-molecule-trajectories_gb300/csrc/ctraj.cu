@@ -785,6 +785,38 @@ int ctraj_run(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* stats)
   return run_impl(c, a, stats, nullptr);
 }
 
+int ctraj_plane(ctraj_context* c, const ctraj_run_args* a, const int64_t* ids, int64_t n_ids, double z_plane,
+                double* out) {
+  if (!c) return fail(CTRAJ_EINVAL, "ctx is NULL");
+  int st = validate_run(c, a);
+  if (st) return st;
+  if (n_ids < 0 || (n_ids > 0 && (!ids || !out))) return fail(CTRAJ_EINVAL, "bad plane arguments");
+  if (!std::isfinite(z_plane)) return fail(CTRAJ_EINVAL, "z_plane is not finite");
+  for (int64_t k = 0; k < n_ids; ++k)
+    if (ids[k] < 0 || ids[k] >= a->n) return fail(CTRAJ_EINVAL, "id %lld out of range", (long long)ids[k]);
+  if (n_ids == 0) return CTRAJ_OK;
+  Plan P;
+  RunDev R;
+  if ((st = prepare(c, a, P, R))) return st;
+  for (int i = 0; i < P.n_el; ++i) P.lf[i].n_smem = 0;  // the replay reads tables from global memory
+  const size_t ob = size_t(n_ids) * 8 * 8;
+  if ((st = c->rec_rows.ensure(ob))) return st;
+  if ((st = c->rec_ids.ensure(size_t(n_ids) * 8))) return st;
+  CT_CUDA(cudaMemcpyAsync(c->rec_ids.p, ids, size_t(n_ids) * 8, cudaMemcpyHostToDevice, c->stream));
+  const int threads = 128;
+  const int grid = int((n_ids + threads - 1) / threads);
+  if (a->precision == 32)
+    k_plane<Mol32<true, true>, false><<<grid, threads, 0, c->stream>>>(P, R, c->rec_ids.as<int64_t>(), n_ids,
+                                                                       z_plane, c->rec_rows.as<double>());
+  else
+    k_plane<Mol64<true>, true><<<grid, threads, 0, c->stream>>>(P, R, c->rec_ids.as<int64_t>(), n_ids, z_plane,
+                                                                c->rec_rows.as<double>());
+  CT_CUDA(cudaGetLastError());
+  CT_CUDA(cudaMemcpyAsync(out, c->rec_rows.p, ob, cudaMemcpyDeviceToHost, c->stream));
+  CT_CUDA(cudaStreamSynchronize(c->stream));
+  return CTRAJ_OK;
+}
+
 int ctraj_run_ring(ctraj_context* c, const ctraj_run_args* a, const ctraj_ring* ring, ctraj_run_stats* stats) {
   if (!ring) return fail(CTRAJ_EINVAL, "ring is NULL");
   return run_impl(c, a, stats, ring);

@@ -555,17 +555,9 @@ __device__ __forceinline__ bool step_any(M& m, const Plan& P, int li, const floa
   }
 }
 
+// The whole path of one molecule with every trajectory row sent to m.sink.
 template <class M, bool k64>
-__global__ void __launch_bounds__(128) k_record(const __grid_constant__ Plan P, const RunDev R,
-                                                const int64_t* ids, int64_t n_ids, int stride,
-                                                int max_rows, double* rows_out, int32_t* count_out,
-                                                unsigned* overflow) {
-  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k >= n_ids) return;
-  RowSink sink{rows_out + size_t(k) * size_t(max_rows) * 10, max_rows, stride, 0, 0, false};
-  M m;
-  m.sink = &sink;
-  m.init(P, R, ids[k]);
+__device__ void replay(M& m, const Plan& P) {
   int from = 0;
   for (;;) {
     int lens_at = -1;
@@ -596,8 +588,58 @@ __global__ void __launch_bounds__(128) k_record(const __grid_constant__ Plan P, 
     from = lens_at + 1;
   }
   m.flush_last();
+}
+
+template <class M, bool k64>
+__global__ void __launch_bounds__(128) k_record(const __grid_constant__ Plan P, const RunDev R,
+                                                const int64_t* ids, int64_t n_ids, int stride,
+                                                int max_rows, double* rows_out, int32_t* count_out,
+                                                unsigned* overflow) {
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n_ids) return;
+  RowSink sink{rows_out + size_t(k) * size_t(max_rows) * 10, max_rows, stride, 0, 0, false};
+  M m;
+  m.sink = &sink;
+  m.init(P, R, ids[k]);
+  replay<M, k64>(m, P);
   count_out[k] = sink.written;
   if (sink.written > max_rows) atomicAdd(overflow, 1u);
+}
+
+// z-plane post-processing (post_processing.py:20-140): replay each molecule and
+// return its position and velocity at the plane z = zp, taken from the row at
+// zp or advanced from the row before it by x + v dt + a dt^2 / 2, v + a dt with
+// dt = (zp - z) / vz (take_timestep, :9-17), in double.  out: (n_ids, 8) =
+// x, y, z, vx, vy, vz, status (0: the molecule ends before the plane, 1:
+// advanced, 2: a row lies on the plane), 0.
+template <class M, bool k64>
+__global__ void __launch_bounds__(128) k_plane(const __grid_constant__ Plan P, const RunDev R, const int64_t* ids,
+                                               int64_t n_ids, double zp, double* out) {
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n_ids) return;
+  RowSink sink{nullptr, 0, 1, 0, 0, false};
+  sink.plane = true;
+  sink.zp = zp;
+  M m;
+  m.sink = &sink;
+  m.init(P, R, ids[k]);
+  replay<M, k64>(m, P);
+  double* o = out + size_t(k) * 8;
+  for (int c = 0; c < 8; ++c) o[c] = c < 6 ? nan("") : 0.0;
+  if (sink.written == 0 || sink.last[2] < zp) return;  // molecule.x()[2] < z: skipped
+  if (sink.pexact) {
+    for (int c = 0; c < 6; ++c) o[c] = sink.exact[c];
+    o[6] = 2.0;
+    return;
+  }
+  const double* h = sink.pcross == 3 ? sink.last : sink.hit;
+  const double dt = (zp - h[2]) / h[5];
+  const double dt2 = dmul(dt, dt);
+  for (int c = 0; c < 3; ++c) {
+    o[c] = dadd(dadd(h[c], dmul(h[3 + c], dt)), dmul(h[6 + c], dt2) / 2.0);
+    o[3 + c] = dadd(h[3 + c], dmul(h[6 + c], dt));
+  }
+  o[6] = 1.0;
 }
 
 }  // namespace ctraj

@@ -180,6 +180,18 @@ struct RowSink {
   int64_t row;   // index of the last stored row (0 = initial)
   int written;
   bool last_written;
+  // Plane mode (stride 1, out unused): follow the rows to the crossing of the
+  // plane z = zp the way post_processing.py:37-76 reads a trajectory: the first
+  // row anywhere with z == zp (pexact; the lens's last steps can overshoot z1
+  // and the exit snap come back to it), else the row before the first one with
+  // z >= zp (pcross = 2; 3 when that is the first row: Python's index -1, the
+  // last row); rows with a non-finite value are skipped, as drop_nans
+  // (molecule.py:160-167) removes them.
+  bool plane;
+  bool pexact;
+  int pcross;
+  double zp;
+  double prev[10], hit[10], last[10], exact[10];
   __device__ void put(double x, double y, double z, double vx, double vy, double vz, double ax,
                       double ay, double az, double t) {
     ++row;
@@ -188,6 +200,29 @@ struct RowSink {
   }
   __device__ void write(double x, double y, double z, double vx, double vy, double vz, double ax,
                         double ay, double az, double t) {
+    if (plane) {
+      const double r[10] = {x, y, z, vx, vy, vz, ax, ay, az, t};
+      bool finite = true;
+      for (int k = 0; k < 10; ++k) finite = finite && isfinite(r[k]);
+      if (finite) {
+        if (!pexact && z == zp) {
+          for (int k = 0; k < 10; ++k) exact[k] = r[k];
+          pexact = true;
+        }
+        if (pcross == 0 && !(z < zp)) {
+          if (written == 0) {
+            pcross = 3;
+          } else {
+            for (int k = 0; k < 10; ++k) hit[k] = prev[k];
+            pcross = 2;
+          }
+        }
+        for (int k = 0; k < 10; ++k) prev[k] = last[k] = r[k];
+        ++written;
+      }
+      last_written = true;
+      return;
+    }
     if (written < max_rows) {
       double* o = out + size_t(written) * 10;
       o[0] = x; o[1] = y; o[2] = z; o[3] = vx; o[4] = vy; o[5] = vz;

@@ -12,10 +12,11 @@ from .distributions import (CeNTREXPositionDistribution, CeNTREXVelocityDistribu
                             GaussianDistribution, GaussianPositionDistribution)
 from .molecule import Molecule, Trajectory
 from .stark import StarkForce, TwoLevelStark, hexapole_force, reference_radial_table
+from .trajectory_simulator import Counter, SimulationResult, TrajectorySimulator
 
 __all__ = [
     "Beamline", "CircularAperture", "RectangularAperture", "FieldPlates", "ElectrostaticLens",
     "GaussianDistribution", "CeNTREXVelocityDistribution", "CeNTREXPositionDistribution",
     "GaussianPositionDistribution", "Molecule", "Trajectory", "StarkForce", "TwoLevelStark",
-    "hexapole_force", "reference_radial_table",
+    "hexapole_force", "reference_radial_table", "TrajectorySimulator", "Counter", "SimulationResult",
 ]

@@ -234,6 +234,7 @@ SIGNATURES = {
                                        ctypes.POINTER(RunStats)]),
     "ctraj_soft_transmission": (ctypes.c_int, [_P, ctypes.POINTER(SoftArgs), _P, ctypes.POINTER(SoftResult)]),
     "ctraj_run_ring": (ctypes.c_int, [_P, ctypes.POINTER(RunArgs), ctypes.POINTER(Ring), ctypes.POINTER(RunStats)]),
+    "ctraj_plane": (ctypes.c_int, [_P, ctypes.POINTER(RunArgs), _P, ctypes.c_int64, ctypes.c_double, _P]),
     "ctraj_run_noalloc": (ctypes.c_int, [ctypes.POINTER(Element), ctypes.c_int32, ctypes.c_int32,
                                          ctypes.POINTER(ForceTable), ctypes.c_int32,
                                          ctypes.POINTER(RunArgs), _P, ctypes.POINTER(RunStats)]),

@@ -222,6 +222,22 @@ class Engine:
                          edge_band=st.edge_band, table_range=st.table_range, kernels=st.kernels,
                          label=label, final=final, rows=rows, margin=margin, extra=res_extra)
 
+    def plane(self, cb: CompiledBeamline, n: int, ids, z: float, precision: int = 32, ics=None, xdist=None,
+              vdist=None, seed: int = 0, offset: int = 0, g: float = G) -> np.ndarray:
+        """ctraj_plane: (len(ids), 8) x, y, z, vx, vy, vz, status, 0 of molecules `ids` of a run
+        at the plane z (status 0: ends before the plane)."""
+        self.load(cb)
+        a, keep = self._args(n, precision, ics, xdist, vdist, seed, offset, g)
+        counts = np.zeros(len(cb.labels) + 1, np.int64)
+        a.counts = counts.ctypes.data
+        ids = np.ascontiguousarray(ids, dtype=np.int64)
+        out = np.empty((ids.size, 8), np.float64)
+        status = self.lib.ctraj_plane(self.ctx, ctypes.byref(a), ids.ctypes.data, ids.size, float(z),
+                                      out.ctypes.data)
+        del keep
+        _abi.check(status, self.lib)
+        return out
+
     def record(self, cb: CompiledBeamline, n: int, ids, stride: int = 1, max_rows: int = 64,
                precision: int = 32, ics=None, xdist=None, vdist=None, seed: int = 0,
                offset: int = 0, g: float = G):

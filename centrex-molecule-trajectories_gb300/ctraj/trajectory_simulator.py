@@ -21,7 +21,7 @@ a (6, n) initial-condition array, ``precision`` (32 or 64) and ``device``.
 from __future__ import annotations
 
 import os
-from dataclasses import dataclass
+from dataclasses import dataclass, field
 from typing import List
 
 import numpy as np
@@ -87,13 +87,17 @@ class Counter:
 
 @dataclass
 class SimulationResult:
-    """trajectory_simulator.py:180-191."""
+    """trajectory_simulator.py:180-191.  ``replay`` (extension) holds what
+    ctraj.post_processing needs to re-propagate ``molecules`` on the device:
+    the compiled beamline, the run's initial-condition source and the
+    molecules' indices in the run."""
 
     counter: Counter
     beamline: object
     xdist: Distribution
     vdist: Distribution
     molecules: List[Molecule]
+    replay: dict | None = field(default=None, repr=False, compare=False)
 
 
 class TrajectorySimulator:
@@ -130,6 +134,7 @@ class TrajectorySimulator:
                       outputs=want_out)
         self.last_run = res
         molecules = []
+        ids = np.zeros(0, np.int64)
         if want_out:
             names = res.label_names()
             ids = np.array([i for i, s in enumerate(names) if s in aoi], dtype=np.int64)
@@ -146,8 +151,10 @@ class TrajectorySimulator:
                     molecules.append(m)
         self.counter = Counter()
         self.counter.counter_dict = res.counter_dict()
-        self.result = SimulationResult(self.counter, beamline, xdist, vdist, molecules)
-        self.results[run_name] = SimulationResult(self.counter, beamline, xdist, vdist, molecules)
+        replay = dict(device=self.device, cb=cb, n=n, precision=prec, ics=ics, xdist=xs, vdist=vs, seed=seed,
+                      g=g, ids=ids)
+        self.result = SimulationResult(self.counter, beamline, xdist, vdist, molecules, replay)
+        self.results[run_name] = SimulationResult(self.counter, beamline, xdist, vdist, molecules, replay)
 
     @staticmethod
     def _max_rows(cb, beamline, vz) -> int:

@@ -258,6 +258,19 @@ int ctraj_record(ctraj_context* ctx, const ctraj_run_args* args,
                  int32_t max_rows, double* rows, int32_t* row_count);
 
 /*
+ * z-plane post-processing: post_processing.py find_radial_pos_dist /
+ * find_vel_dist (:20-140) for the molecules ids[] of the run described by args
+ * (same ICs as that run), evaluated on the device by replaying each molecule.
+ * out: (n_ids, 8) float64 x, y, z, vx, vy, vz, status, 0 per molecule, the
+ * state at the plane z = z_plane: the trajectory row lying on the plane if
+ * there is one (status 2), else the row before the first one past the plane
+ * advanced by take_timestep (:9-17, status 1); status 0 (and NaN state) when
+ * the molecule's last row is before the plane (the reference skips it).
+ */
+int ctraj_plane(ctraj_context* ctx, const ctraj_run_args* args, const int64_t* ids,
+                int64_t n_ids, double z_plane, double* out);
+
+/*
  * Batched sweep: many lens configurations in one launch sequence.  Replaces
  * the caller's loop of one run_simulation per configuration (the per-state
  * sweep of examples/lens_simulation_different_states.py:136-156 builds one
