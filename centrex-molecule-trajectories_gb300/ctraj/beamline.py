@@ -24,6 +24,12 @@ class Beamline:
     def sort_elements(self):
         self.elements.sort(key=lambda e: e.z0)
 
+    def save_to_hdf(self, filepath, run_name: str) -> None:
+        """beamline.py:78-90: one group per element under run_name/beamline."""
+        from .hdf import save_beamline
+
+        save_beamline(self, filepath, run_name)
+
     def find_element(self, name):
         for element in self.elements:
             if element.name == name:

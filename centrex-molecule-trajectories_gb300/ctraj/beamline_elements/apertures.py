@@ -30,6 +30,12 @@ class BeamlineElement:
     def N_steps(self) -> int:  # pragma: no cover - overridden
         raise NotImplementedError
 
+    def save_to_hdf(self, filepath, parent_group_path: str) -> None:
+        """apertures.py:56-78: group parent/name with attrs class and the fields."""
+        from ..hdf import save_element
+
+        save_element(self, filepath, parent_group_path)
+
 
 @dataclass
 class CircularAperture(BeamlineElement):

@@ -37,6 +37,12 @@ class ElectrostaticLens(BeamlineElement):
     dt: Optional[float] = None
     scheme: str = "reference"
 
+    def save_to_hdf(self, filepath, parent_group_path: str) -> None:
+        """electrostatic_lens.py:145-166 (the force table is not saved)."""
+        from ..hdf import save_lens
+
+        save_lens(self, filepath, parent_group_path)
+
     def N_steps(self) -> int:
         """1 + rint(L/dz), electrostatic_lens.py:120-125."""
         import numpy as np

@@ -38,6 +38,10 @@ class GaussianDistribution(Distribution):
     def draw(self, n: int) -> np.ndarray:
         return norm.rvs(loc=self.mean, scale=self.sigma, size=n)
 
+    def save_to_hdf(self, filepath, run_name: str, group_name: str = ""):
+        """distributions.py:48-52."""
+        raise NotImplementedError("Saving GaussianDistribution to hdf is not implemented. Save child class instead.")
+
 
 @dataclass
 class CeNTREXVelocityDistribution(Distribution):
@@ -53,6 +57,12 @@ class CeNTREXVelocityDistribution(Distribution):
                          GaussianDistribution(self.vy, self.sigmay).draw(n),
                          GaussianDistribution(self.vz, self.sigmaz).draw(n)))
 
+    def save_to_hdf(self, filepath, run_name: str):
+        """distributions.py:78-98: group run_name/velocity_distribution."""
+        from .hdf import save_distribution
+
+        save_distribution(self, filepath, run_name, "velocity_distribution", "velocity")
+
 
 @dataclass
 class CeNTREXPositionDistribution(Distribution):
@@ -63,6 +73,12 @@ class CeNTREXPositionDistribution(Distribution):
         theta = uniform.rvs(size=n) * 2 * np.pi
         r = np.sqrt(uniform.rvs(size=n)) * self.d / 2
         return np.array((r * np.cos(theta), r * np.sin(theta), np.full(n, self.z)))
+
+    def save_to_hdf(self, filepath, run_name: str):
+        """distributions.py:122-142: group run_name/position_distribution."""
+        from .hdf import save_distribution
+
+        save_distribution(self, filepath, run_name, "position_distribution", "position")
 
 
 @dataclass
@@ -75,6 +91,12 @@ class GaussianPositionDistribution(Distribution):
         x = GaussianDistribution(0, self.sigmax).draw(n)
         y = GaussianDistribution(0, self.sigmay).draw(n)
         return np.vstack((x, y, np.full(n, self.z)))
+
+    def save_to_hdf(self, filepath, run_name: str):
+        """distributions.py:166-186: group run_name/position_distribution."""
+        from .hdf import save_distribution
+
+        save_distribution(self, filepath, run_name, "position_distribution", "position")
 
 
 def device_spec(dist, role: str) -> _abi.Distribution | None:

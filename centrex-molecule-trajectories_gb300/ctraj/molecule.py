@@ -31,6 +31,12 @@ class Trajectory:
         rows = np.asarray(rows, dtype=np.float64)
         return cls(rows[:, 0:3].copy(), rows[:, 3:6].copy(), rows[:, 6:9].copy(), rows[:, 9].copy())
 
+    def save_to_hdf(self, file, run_name: str, group_name: str) -> None:
+        """molecule.py:169-185 (datasets x, v, a, t of the group run_name/group_name)."""
+        from .hdf import save_trajectory
+
+        save_trajectory(self, file, run_name, group_name)
+
     def drop_nans(self):
         """molecule.py:160-167."""
         self.x = self.x[np.all(np.isfinite(self.x), axis=1), :]
@@ -65,3 +71,9 @@ class Molecule:
 
     def set_dead(self):
         self.alive = False
+
+    def save_to_hdf(self, file, run_name: str, group_name: str):
+        """molecule.py:97-106: the trajectory plus attrs aperture_hit and alive."""
+        from .hdf import save_molecule
+
+        save_molecule(self, file, run_name, group_name)

@@ -73,16 +73,10 @@ class Counter:
                 self.counter_dict[key] = self.counter_dict.get(key, 0) + value
 
     def save_to_hdf(self, filepath, run_name: str) -> None:
-        import h5py  # optional, as in the reference
+        """trajectory_simulator.py:160-176: attrs label -> count of run_name/counter."""
+        from .hdf import save_counter
 
-        with h5py.File(filepath, "a") as f:
-            group_path = run_name + "/counter"
-            try:
-                f.create_group(group_path)
-            except ValueError:
-                raise ValueError("Can't save counter. Group already exists!")
-            for key, value in self.counter_dict.items():
-                f[group_path].attrs[key] = value
+        save_counter(self, filepath, run_name)
 
 
 @dataclass
@@ -98,6 +92,18 @@ class SimulationResult:
     vdist: Distribution
     molecules: List[Molecule]
     replay: dict | None = field(default=None, repr=False, compare=False)
+
+    def save_to_hdf(self, filepath, run_name: str) -> None:
+        """trajectory_simulator.py:218-244 (layout in ctraj.hdf)."""
+        from .hdf import save_result
+
+        save_result(self, filepath, run_name)
+
+    def save_molecules_to_hdf(self, filepath, run_name: str) -> None:
+        """trajectory_simulator.py:246-254: run_name/trajectories/molecule_<i>."""
+        from .hdf import save_molecules
+
+        save_molecules(self, filepath, run_name)
 
 
 class TrajectorySimulator:
