@@ -190,6 +190,13 @@ int build_lens_tables(ctraj_context* c) {
   std::vector<float4> host;
   for (int i = 0; i < n_el; ++i) {
     const ctraj_element& e = c->elements[i];
+    if (e.type == CTRAJ_HONEYCOMB) {  // cell centres (x, y, 0, 0)
+      const HostTable& t = c->tables[e.table];
+      c->lens_offset[i] = host.size();
+      c->lens_n_int[i] = t.n;
+      for (int k = 0; k < t.n; ++k) host.push_back(make_float4(float(t.knots[k]), float(t.values[k]), 0.f, 0.f));
+      continue;
+    }
     if (e.type != CTRAJ_ELECTROSTATIC_LENS) continue;
     const HostTable& t = c->tables[e.table];
     const double x0 = t.knots[0], h = (t.knots[t.n - 1] - t.knots[0]) / double(t.n - 1);
@@ -222,6 +229,26 @@ int build_lens_tables(ctraj_context* c) {
   return CTRAJ_OK;
 }
 
+// FP32 constants of a honeycomb: hexagon half width R sqrt(3)/2, R, and the
+// inverse row and cell pitches that place the nearest-centre window.
+void honeycomb_constants(const ctraj_element& e, ElemF& f) {
+  f.c[0] = float(e.p[0] * std::sqrt(3.0) / 2.0);
+  f.c[1] = float(e.p[0]);
+  f.c[2] = float(e.p[2]);
+  f.c[3] = float(e.p[3]);
+}
+
+// A honeycomb's mesh table: kind MESH, whole rows of p[1] cells.
+int check_honeycomb(const ctraj_element& e, int i, int kind, int n) {
+  if (kind != CTRAJ_TABLE_MESH) return fail(CTRAJ_EINVAL, "honeycomb element %d: table %d is not a mesh table", i, e.table);
+  const double nx = e.p[1];
+  if (!(nx >= 1.0) || nx != std::floor(nx) || nx > double(n) || n % int(nx) != 0)
+    return fail(CTRAJ_EINVAL, "honeycomb element %d: %d cells do not form rows of p[1] = %g cells", i, n, nx);
+  if (!std::isfinite(e.p[2]) || !std::isfinite(e.p[3]) || !(e.p[0] >= 0.0))
+    return fail(CTRAJ_EINVAL, "honeycomb element %d: bad radius or pitches", i);
+  return CTRAJ_OK;
+}
+
 int build_plan(ctraj_context* c, const ctraj_run_args* a, Plan& P) {
   std::memset(&P, 0, sizeof P);
   const int n_el = int(c->elements.size());
@@ -251,6 +278,15 @@ int build_plan(ctraj_context* c, const ctraj_run_args* a, Plan& P) {
         f.c[0] = float(e.p[0]);
         f.c[1] = float(e.p[1]);
         break;
+      case CTRAJ_HONEYCOMB:
+        honeycomb_constants(e, f);
+        break;
+    }
+    if (e.type == CTRAJ_HONEYCOMB) {
+      LensF& L = P.lf[i];
+      L.q = c->lens_tables.as<float4>(c->lens_offset[i] * sizeof(float4));
+      L.n_int = c->lens_n_int[i];
+      L.cols = int(e.p[1]);
     }
     if (e.type == CTRAJ_ELECTROSTATIC_LENS) {
       if (P.first_lens == n_el) P.first_lens = i;
@@ -294,8 +330,15 @@ int check_beamline(const ctraj_context* c) {
       if (e.table < 0 || e.table >= CTRAJ_MAX_TABLES || !c->tables[e.table].n)
         return fail(CTRAJ_ESTATE, "lens element %zu uses force table %d, which is not set", i, e.table);
       const HostTable& t = c->tables[e.table];
+      if (t.kind == CTRAJ_TABLE_MESH) return fail(CTRAJ_EINVAL, "lens element %zu: table %d is a mesh table", i, e.table);
       if (t.kind == CTRAJ_TABLE_STARK_SPLINE && e.field_order != 1 && e.field_order != 2)
         return fail(CTRAJ_EINVAL, "lens element %zu: field_order must be 1 or 2", i);
+    } else if (e.type == CTRAJ_HONEYCOMB) {
+      if (e.table < 0 || e.table >= CTRAJ_MAX_TABLES || !c->tables[e.table].n)
+        return fail(CTRAJ_ESTATE, "honeycomb element %zu uses mesh table %d, which is not set", i, e.table);
+      const HostTable& t = c->tables[e.table];
+      int st = check_honeycomb(e, int(i), t.kind, t.n);
+      if (st) return st;
     }
   }
   return CTRAJ_OK;
@@ -624,13 +667,13 @@ int ctraj_set_beamline(ctraj_context* c, const ctraj_element* el, int32_t n_el, 
   if (n_el > 0 && !el) return fail(CTRAJ_EINVAL, "elements is NULL");
   for (int i = 0; i < n_el; ++i) {
     const ctraj_element& e = el[i];
-    if (e.type < CTRAJ_CIRCULAR_APERTURE || e.type > CTRAJ_ELECTROSTATIC_LENS)
+    if (e.type < CTRAJ_CIRCULAR_APERTURE || e.type > CTRAJ_HONEYCOMB)
       return fail(CTRAJ_EINVAL, "element %d: unknown type %d", i, e.type);
     if (e.label < -1 || e.label >= n_labels || e.label_inside < -1 || e.label_inside >= n_labels)
       return fail(CTRAJ_EINVAL, "element %d: label out of range", i);
     if (i > 0 && e.z0 < el[i - 1].z0) return fail(CTRAJ_EINVAL, "elements are not sorted by z0 (element %d)", i);
-    if (e.type == CTRAJ_ELECTROSTATIC_LENS && (e.table < 0 || e.table >= CTRAJ_MAX_TABLES))
-      return fail(CTRAJ_EINVAL, "element %d: force table id %d out of range", i, e.table);
+    if ((e.type == CTRAJ_ELECTROSTATIC_LENS || e.type == CTRAJ_HONEYCOMB) && (e.table < 0 || e.table >= CTRAJ_MAX_TABLES))
+      return fail(CTRAJ_EINVAL, "element %d: table id %d out of range", i, e.table);
   }
   c->elements.assign(el, el + n_el);
   c->n_labels = n_labels;
@@ -643,16 +686,23 @@ int ctraj_set_beamline(ctraj_context* c, const ctraj_element* el, int32_t n_el, 
 int ctraj_set_force_table(ctraj_context* c, int32_t id, const ctraj_force_table* t) {
   if (!c || !t) return fail(CTRAJ_EINVAL, "NULL argument");
   if (id < 0 || id >= CTRAJ_MAX_TABLES) return fail(CTRAJ_EINVAL, "table id %d out of range", id);
-  if (t->n_knots < 2 || !t->knots) return fail(CTRAJ_EINVAL, "table needs at least 2 knots");
-  if (t->kind == CTRAJ_TABLE_STARK_SPLINE && !t->coef) return fail(CTRAJ_EINVAL, "spline table without coef");
-  if (t->kind == CTRAJ_TABLE_RADIAL_LINEAR && !t->values) return fail(CTRAJ_EINVAL, "radial table without values");
-  if (t->kind != CTRAJ_TABLE_STARK_SPLINE && t->kind != CTRAJ_TABLE_RADIAL_LINEAR)
-    return fail(CTRAJ_EINVAL, "unknown table kind %d", t->kind);
-  const double h = (t->knots[t->n_knots - 1] - t->knots[0]) / double(t->n_knots - 1);
-  if (!(h > 0)) return fail(CTRAJ_EINVAL, "table knots must ascend");
-  for (int j = 1; j < t->n_knots; ++j)
-    if (std::fabs((t->knots[j] - t->knots[j - 1]) - h) > 1e-6 * h)
-      return fail(CTRAJ_EINVAL, "table knots must be uniformly spaced (knot %d)", j);
+  if (t->kind == CTRAJ_TABLE_MESH) {
+    if (t->n_knots < 1 || !t->knots || !t->values) return fail(CTRAJ_EINVAL, "mesh table needs at least one cell");
+    for (int j = 0; j < t->n_knots; ++j)
+      if (!std::isfinite(t->knots[j]) || !std::isfinite(t->values[j]))
+        return fail(CTRAJ_EINVAL, "mesh table: cell %d is not finite", j);
+  } else {
+    if (t->n_knots < 2 || !t->knots) return fail(CTRAJ_EINVAL, "table needs at least 2 knots");
+    if (t->kind == CTRAJ_TABLE_STARK_SPLINE && !t->coef) return fail(CTRAJ_EINVAL, "spline table without coef");
+    if (t->kind == CTRAJ_TABLE_RADIAL_LINEAR && !t->values) return fail(CTRAJ_EINVAL, "radial table without values");
+    if (t->kind != CTRAJ_TABLE_STARK_SPLINE && t->kind != CTRAJ_TABLE_RADIAL_LINEAR)
+      return fail(CTRAJ_EINVAL, "unknown table kind %d", t->kind);
+    const double h = (t->knots[t->n_knots - 1] - t->knots[0]) / double(t->n_knots - 1);
+    if (!(h > 0)) return fail(CTRAJ_EINVAL, "table knots must ascend");
+    for (int j = 1; j < t->n_knots; ++j)
+      if (std::fabs((t->knots[j] - t->knots[j - 1]) - h) > 1e-6 * h)
+        return fail(CTRAJ_EINVAL, "table knots must be uniformly spaced (knot %d)", j);
+  }
   HostTable& ht = c->tables[id];
   ht.kind = t->kind;
   ht.n = t->n_knots;
@@ -1530,6 +1580,13 @@ int noalloc_scratch(char** out) {
 }
 
 int noalloc_check_table(const ctraj_force_table& t, int k) {
+  if (t.kind == CTRAJ_TABLE_MESH) {
+    if (t.n_knots < 1 || !t.knots || !t.values) return fail(CTRAJ_EINVAL, "table %d: mesh needs at least one cell", k);
+    for (int j = 0; j < t.n_knots; ++j)
+      if (!std::isfinite(t.knots[j]) || !std::isfinite(t.values[j]))
+        return fail(CTRAJ_EINVAL, "table %d: cell %d is not finite", k, j);
+    return CTRAJ_OK;
+  }
   if (t.n_knots < 2 || !t.knots) return fail(CTRAJ_EINVAL, "table %d needs at least 2 knots", k);
   if (t.kind == CTRAJ_TABLE_STARK_SPLINE && !t.coef) return fail(CTRAJ_EINVAL, "table %d: no coef", k);
   if (t.kind == CTRAJ_TABLE_RADIAL_LINEAR && !t.values) return fail(CTRAJ_EINVAL, "table %d: no values", k);
@@ -1570,10 +1627,30 @@ int noalloc_plan(const ctraj_element* el, int n_el, int n_labels, const ctraj_fo
     } else if (e.type == CTRAJ_FIELD_PLATES) {
       f.c[0] = float(e.p[0]);
       f.c[1] = float(e.p[1]);
+    } else if (e.type == CTRAJ_HONEYCOMB) {
+      honeycomb_constants(e, f);
     }
-    if (e.type != CTRAJ_ELECTROSTATIC_LENS) continue;
-    if (e.table < 0 || e.table >= n_tab) return fail(CTRAJ_ESTATE, "lens element %d uses table %d, not given", i, e.table);
+    if (e.type != CTRAJ_ELECTROSTATIC_LENS && e.type != CTRAJ_HONEYCOMB) continue;
+    if (e.table < 0 || e.table >= n_tab) return fail(CTRAJ_ESTATE, "element %d uses table %d, not given", i, e.table);
     const ctraj_force_table& t = tabs[e.table];
+    if (e.type == CTRAJ_HONEYCOMB) {  // cell centres (x, y, 0, 0)
+      int st = check_honeycomb(e, i, t.kind, t.n_knots);
+      if (st) return st;
+      if (offset + size_t(t.n_knots) > size_t(CTRAJ_NOALLOC_MAX_INTERVALS))
+        return fail(CTRAJ_EINVAL, "lens and mesh tables exceed %d entries", CTRAJ_NOALLOC_MAX_INTERVALS);
+      for (int j0 = 0; j0 < t.n_knots; j0 += 256) {
+        const int m = std::min(256, t.n_knots - j0);
+        for (int j = 0; j < m; ++j)
+          buf[j] = make_float4(float(t.knots[j0 + j]), float(t.values[j0 + j]), 0.f, 0.f);
+        CT_CUDA(cudaMemcpyAsync(dev_tables + offset + j0, buf, m * sizeof(float4), cudaMemcpyHostToDevice, s));
+      }
+      P.lf[i].q = dev_tables + offset;
+      P.lf[i].n_int = t.n_knots;
+      P.lf[i].cols = int(e.p[1]);
+      offset += size_t(t.n_knots);
+      continue;
+    }
+    if (t.kind == CTRAJ_TABLE_MESH) return fail(CTRAJ_EINVAL, "lens element %d: table %d is a mesh table", i, e.table);
     if (t.kind == CTRAJ_TABLE_STARK_SPLINE && e.field_order != 1 && e.field_order != 2)
       return fail(CTRAJ_EINVAL, "lens element %d: field_order must be 1 or 2", i);
     if (P.first_lens == n_el) P.first_lens = i;
@@ -1709,7 +1786,7 @@ extern "C" int ctraj_run_noalloc(const ctraj_element* el, int32_t n_el, int32_t 
   if (n_tab < 0 || n_tab > CTRAJ_MAX_TABLES || (n_tab > 0 && !tabs)) return fail(CTRAJ_EINVAL, "bad tables");
   for (int i = 0; i < n_el; ++i) {
     const ctraj_element& e = el[i];
-    if (e.type < CTRAJ_CIRCULAR_APERTURE || e.type > CTRAJ_ELECTROSTATIC_LENS)
+    if (e.type < CTRAJ_CIRCULAR_APERTURE || e.type > CTRAJ_HONEYCOMB)
       return fail(CTRAJ_EINVAL, "element %d: unknown type %d", i, e.type);
     if (e.label < -1 || e.label >= n_labels || e.label_inside < -1 || e.label_inside >= n_labels)
       return fail(CTRAJ_EINVAL, "element %d: label out of range", i);

@@ -113,6 +113,98 @@ __device__ inline void lens_force64(const Plan& P, const ctraj_element& e, doubl
 }
 
 // ---------------------------------------------------------------------------
+// Honeycomb nearest cell (meshes.py:104-108)
+// ---------------------------------------------------------------------------
+// The reference takes numpy's argmin over ALL centres of
+// sqrt((px - xc)**2 + (py - yc)**2): the first of equal minima, 0 when no
+// distance is finite.  The centres form hexalattice rows of nx cells (odd rows
+// shifted by half a pitch), so the nearest centre of an interior point is at
+// most one row and one cell from the rounded estimate, and the second-nearest
+// at most two.  Outside the grid the estimate is clamped; the nearest and
+// second-nearest centres of a point beyond the first or last row are among
+// the outermost four rows (the nearest of each row is its cell closest in x,
+// and rows alternate their half-pitch shift), so the window takes rows
+// j0-2..j0+2, widened to four rows at either end, and cells i0-2..i0+2 of each.
+// Scanning the window rows and cells in ascending order visits cells in
+// ascending index, so strict < keeps the first minimum as argmin does.
+
+// rows of the search window around the (clamped) estimate j0 of ny rows
+__device__ __forceinline__ void window_rows(int j0, int ny, int& lo, int& hi) {
+  lo = j0 == ny - 1 ? max(ny - 4, 0) : max(j0 - 2, 0);
+  hi = j0 == 0 ? min(3, ny - 1) : min(j0 + 2, ny - 1);
+}
+
+// round(u) clamped to [0, hi]; NaN -> 0
+__device__ __forceinline__ int window_index(double u, int hi) {
+  const double r = floor(u + 0.5);
+  if (!(r >= 0.0)) return 0;
+  return r >= double(hi) ? hi : int(r);
+}
+
+// FP64, the reference's operations; best / second: the two smallest distances.
+__device__ inline int mesh_nearest64(const TableD& T, const double* p, double px, double py, double& best,
+                                     double& second) {
+  const int nx = int(p[1]), ny = T.n / nx;
+  const int j0 = window_index((py - __ldg(T.values)) * p[2], ny - 1);
+  int lo, hi;
+  window_rows(j0, ny, lo, hi);
+  int idx = -1;
+  best = INFINITY;
+  second = INFINITY;
+  for (int j = lo; j <= hi; ++j) {
+    const int row = j * nx;
+    const int i0 = window_index((px - __ldg(T.knots + row)) * p[3], nx - 1);
+    for (int k = row + max(i0 - 2, 0); k <= row + min(i0 + 2, nx - 1); ++k) {
+      const double dx = dadd(px, -__ldg(T.knots + k)), dy = dadd(py, -__ldg(T.values + k));
+      const double d = __dsqrt_rn(dadd(dmul(dx, dx), dmul(dy, dy)));
+      if (d < best) {
+        second = best;
+        best = d;
+        idx = k;
+      } else if (d < second) {
+        second = d;
+      }
+    }
+  }
+  return idx < 0 ? 0 : idx;
+}
+
+// FP32 on the float4 (x, y, 0, 0) centre table; squared distances.
+__device__ __forceinline__ int window_index32(float u, int hi) {
+  const float r = floorf(u + 0.5f);
+  if (!(r >= 0.0f)) return 0;
+  return r >= float(hi) ? hi : int(r);
+}
+
+__device__ inline int mesh_nearest32(const LensF& L, const ElemF& f, float px, float py, float& best2,
+                                     float& second2) {
+  const int nx = L.cols, ny = L.n_int / nx;
+  const int j0 = window_index32((py - __ldg(&L.q[0].y)) * f.c[2], ny - 1);
+  int lo, hi;
+  window_rows(j0, ny, lo, hi);
+  int idx = -1;
+  best2 = INFINITY;
+  second2 = INFINITY;
+  for (int j = lo; j <= hi; ++j) {
+    const int row = j * nx;
+    const int i0 = window_index32((px - __ldg(&L.q[row].x)) * f.c[3], nx - 1);
+    for (int k = row + max(i0 - 2, 0); k <= row + min(i0 + 2, nx - 1); ++k) {
+      const float4 c = __ldg(L.q + k);
+      const float dx = px - c.x, dy = py - c.y;
+      const float d2 = __fmaf_rn(dy, dy, __fmul_rn(dx, dx));
+      if (d2 < best2) {
+        second2 = best2;
+        best2 = d2;
+        idx = k;
+      } else if (d2 < second2) {
+        second2 = d2;
+      }
+    }
+  }
+  return idx < 0 ? 0 : idx;
+}
+
+// ---------------------------------------------------------------------------
 // FP32 force: w such that a_perp = w * (x, y)
 // ---------------------------------------------------------------------------
 // kStaged: the whole table is in shared memory (s_tab); otherwise it is read
@@ -343,6 +435,27 @@ struct Mol64 {
     update(dt, P);
     return false;
   }
+  // Honeycomb test at the plane just reached (meshes.py:98-116): cell = the
+  // nearest centre, looked up while it is None or 0 (`if not idx`); lost when
+  // outside that cell's hexagon, |dx| < R sqrt(3)/2 and |dy| < R - |dx|/sqrt(3).
+  // Margins: half the gap between nearest and second-nearest centre, and the
+  // nearer hexagon side.
+  __device__ bool honeycomb_out(const Plan& P, int i, int& cell) {
+    const ctraj_element& e = P.el[i];
+    const TableD& T = P.td[e.table];
+    if (cell <= 0) {
+      double best, second;
+      cell = mesh_nearest64(T, e.p, x[0], x[1], best, second);
+      note(dadd(second, -best) / 2.0);
+    }
+    const double s3 = __dsqrt_rn(3.0), R = e.p[0];
+    const double dx = fabs(dadd(x[0], -__ldg(T.knots + cell))), dy = fabs(dadd(x[1], -__ldg(T.values + cell)));
+    const double hw = dmul(R, s3) / 2.0, q = __ddiv_rn(dx, s3);
+    const double side = dadd(hw, -dx), slant = dmul(dadd(dadd(R, -q), -dy), s3 / 2.0);
+    note(side < slant ? side : slant);
+    return !(dx < hw && dy < dadd(R, -q));
+  }
+
   __device__ bool lens_entrance_out(const Plan& P, int i) { return circle_out(P, i); }
 
   __device__ double vel_z() const { return v[2]; }
@@ -554,6 +667,22 @@ struct Mol32 {
     row_out();
     return false;
   }
+  // Honeycomb (meshes.py:98-116) on the float centre table; ef c[0] = R sqrt(3)/2,
+  // c[1] = R.
+  __device__ bool honeycomb_out(const Plan& P, int i, int& cell) {
+    const LensF& L = P.lf[i];
+    const float* c = P.ef[i].c;
+    if (cell <= 0) {
+      float best2, second2;
+      cell = mesh_nearest32(L, P.ef[i], x, y, best2, second2);
+      if (kOut) note(0.5f * (sqrtf(second2) - sqrtf(best2)));
+    }
+    const float4 q = __ldg(L.q + cell);
+    const float dx = fabsf(x - q.x), dy = fabsf(y - q.y);
+    const float lim = __fmaf_rn(-0.57735026919f, dx, c[1]);
+    if (kOut) note(fminf(c[0] - dx, 0.8660254038f * (lim - dy)));
+    return !(dx < c[0] && dy < lim);
+  }
   __device__ bool lens_entrance_out(const Plan& P, int i) { return circle_out(P, i); }
 
   __device__ double vel_z() const { return double(vz); }
@@ -698,6 +827,14 @@ __device__ int walk(M& m, const Plan& P, int from, int* lens_at) {
         m.fly(P, i, 0);
         if (m.plates(P, i)) return e.label;
         break;
+      case CTRAJ_HONEYCOMB: {
+        int cell = -1;  // None
+        m.fly(P, i, 0);
+        if (m.honeycomb_out(P, i, cell)) return e.label;
+        m.fly(P, i, 1);
+        if (m.honeycomb_out(P, i, cell)) return e.label;
+        break;
+      }
       case CTRAJ_ELECTROSTATIC_LENS:
         m.fly(P, i, 0);
         *lens_at = i;  // also reported for a loss at the entrance test

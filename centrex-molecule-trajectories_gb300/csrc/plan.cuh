@@ -22,7 +22,8 @@ enum : int {
 struct ElemF {
   float gap;   // (float)(z0 - z1 of the previous element); flight into this element
   float len;   // (float)(z1 - z0)
-  float c[4];  // circle: (d/2)^2; rect: x1, x2, y1, y2; plates: x1, x2; lens: (d/2)^2
+  float c[4];  // circle: (d/2)^2; rect: x1, x2, y1, y2; plates: x1, x2; lens: (d/2)^2;
+               // honeycomb: R sqrt(3)/2, R, 1 / row pitch, 1 / cell pitch
 };
 
 // FP32 constants of one lens (indexed by element).
@@ -34,6 +35,7 @@ struct LensF {
   int n_int;        // intervals in the table
   int n_smem;       // leading intervals staged in shared memory
   int force;        // kForce*
+  int cols;         // honeycomb: q = cell centres (x, y, 0, 0), n_int = cells, cols = cells per row
 };
 
 // The FP32 constants of the one lens a k_lens_chunk launch integrates, passed

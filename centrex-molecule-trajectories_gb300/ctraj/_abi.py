@@ -37,6 +37,7 @@ CIRCULAR_APERTURE = 1
 RECTANGULAR_APERTURE = 2
 FIELD_PLATES = 3
 ELECTROSTATIC_LENS = 4
+HONEYCOMB = 5
 
 STEP_DZ = 0
 STEP_DT = 1
@@ -45,6 +46,7 @@ RK4_CLASSIC = 1
 
 TABLE_STARK_SPLINE = 1
 TABLE_RADIAL_LINEAR = 2
+TABLE_MESH = 3
 
 DIST_NONE = 0
 DIST_GAUSSIAN_POSITION = 1

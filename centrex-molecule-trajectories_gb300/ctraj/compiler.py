@@ -6,7 +6,8 @@ one ``ctraj_element`` each, duck-typed on the class name so the reference's own
 objects and this package's mirrors both compile.  It also builds the counter
 label table, reproducing the strings the reference credits:
 
-* apertures and field plates: ``element.name`` (apertures.py:113,188,242,264)
+* apertures, field plates and honeycombs: ``element.name`` (apertures.py:113,188,242,264,
+  meshes.py:114)
 * electrostatic lens: "Lens entrance" and "Inside lens" (electrostatic_lens.py:63,117)
 * survivors: "Detected" (beamline.py:34-35), the last count slot
 
@@ -179,6 +180,24 @@ def compile_beamline(beamline) -> CompiledBeamline:
                 max_rows += 1 + int(np.rint(e.L / e.dz))
             else:
                 max_rows += 1  # per-molecule step count; recording sizes it from vz
+        elif kind == "Honeycomb":
+            s.type = _abi.HONEYCOMB
+            s.label = slot(e.name)
+            xc = np.ascontiguousarray(np.asarray(e.xcoords, np.float64).reshape(-1))
+            yc = np.ascontiguousarray(np.asarray(e.ycoords, np.float64).reshape(-1))
+            nx, ny = int(e.nx), int(e.ny)
+            if xc.size != nx * ny or yc.size != xc.size:
+                raise ValueError(f"Honeycomb {e.name!r}: {xc.size} centres for a {nx} x {ny} grid")
+            if len(tables) >= _abi.MAX_TABLES:
+                raise ValueError(f"at most {_abi.MAX_TABLES} distinct force and mesh tables")
+            s.table = len(tables)
+            tables.append(Table(_abi.TABLE_MESH, xc, values=yc))
+            pitch = float(e.cell_wall_length * np.sqrt(3))  # hexalattice min_diam
+            s.p[0] = float((e.cell_wall_length * np.sqrt(3) - e.cell_wall_thickness / 2) / 2)
+            s.p[1] = float(nx)
+            s.p[2] = 1.0 / (pitch * np.sqrt(3) / 2)
+            s.p[3] = 1.0 / pitch
+            max_rows += 2
         else:
             raise TypeError(f"beamline element type {kind} has no device implementation")
         arr[i] = s

@@ -31,8 +31,9 @@ def field_items(obj) -> list:
     return list(vars(obj).items())
 
 
-def save_element(element, filepath, parent_group_path: str) -> None:
-    """BeamlineElement.save_to_hdf (apertures.py:56-78)."""
+def save_element(element, filepath, parent_group_path: str, skip=()) -> None:
+    """BeamlineElement.save_to_hdf (apertures.py:56-78); Honeycomb skips its
+    patches (meshes.py:172-175)."""
     h5py = _h5py()
     with h5py.File(filepath, "a") as f:
         try:
@@ -40,6 +41,8 @@ def save_element(element, filepath, parent_group_path: str) -> None:
             f.create_group(group_path)
             f[group_path].attrs["class"] = type(element).__name__
             for key, value in field_items(element):
+                if key in skip:
+                    continue
                 f[group_path].attrs[key] = value
         except ValueError:
             print("Can't save beamline element. Group already exists!")

@@ -63,6 +63,7 @@ enum {
   CTRAJ_RECTANGULAR_APERTURE = 2, /* apertures.py:147-196 */
   CTRAJ_FIELD_PLATES = 3,         /* apertures.py:213-277 */
   CTRAJ_ELECTROSTATIC_LENS = 4,   /* electrostatic_lens.py:23-125 */
+  CTRAJ_HONEYCOMB = 5,            /* meshes.py:26-178 */
 };
 
 enum { CTRAJ_STEP_DZ = 0, CTRAJ_STEP_DT = 1 };           /* lens step mode  */
@@ -78,6 +79,16 @@ enum { CTRAJ_RK4_REFERENCE = 0, CTRAJ_RK4_CLASSIC = 1 }; /* lens RK4 scheme */
  *   circular aperture : p[0] = d (diameter)
  *   rectangular       : p[0] = x1, p[1] = x2, p[2] = y1, p[3] = y2 (w spans X, h spans Y)
  *   field plates      : p[0] = x1, p[1] = x2
+ *   honeycomb         : p[0] = circumradius of each cell's hexagon (pointy side
+ *                       along y, the matplotlib RegularPolygon of meshes.py:71-78);
+ *                       table = a CTRAJ_TABLE_MESH with the cell centres of an
+ *                       hexalattice grid (rows of p[1] cells, odd rows shifted
+ *                       by half a pitch); p[1] = cells per row, p[2] = 1 / row
+ *                       pitch in y, p[3] = 1 / cell pitch in x.  p[1..3] only
+ *                       place the device's nearest-centre search window (5 x 5
+ *                       cells around the estimate, 4 rows at the grid's ends);
+ *                       the cell found is the reference's argmin over all
+ *                       centres for such a grid.
  *   electrostatic lens: p[0] = d (bore diameter), p[1] = dz, p[2] = dt,
  *                       p[3] = V (electrode voltage), p[4] = R (field radius),
  *                       p[5] = mass (kg), p[6] = alpha with |E| = alpha r^n
@@ -87,7 +98,7 @@ enum { CTRAJ_RK4_REFERENCE = 0, CTRAJ_RK4_CLASSIC = 1 }; /* lens RK4 scheme */
  * label        counter slot credited when a molecule is lost on this element
  *              (for the lens: the "Lens entrance" slot, electrostatic_lens.py:63)
  * label_inside lens only: the "Inside lens" slot (electrostatic_lens.py:117)
- * table        lens only: force table id (ctraj_set_force_table)
+ * table        lens: force table id (ctraj_set_force_table); honeycomb: mesh table id
  * step_mode    lens only: CTRAJ_STEP_DZ -> N = rint(L/dz), dt = dz/vz (:87-88);
  *              CTRAJ_STEP_DT -> dz = vz*dt per molecule, then as DZ
  * scheme       lens only: CTRAJ_RK4_REFERENCE reproduces the reference's stage-2
@@ -119,14 +130,18 @@ enum {
    * the reference's interp1d table (electrostatic_lens.py:194-209).  Lookups
    * above the last knot are errors (CTRAJ_ERANGE), as interp1d raises.        */
   CTRAJ_TABLE_RADIAL_LINEAR = 2,
+  /* Cell centres of a honeycomb mesh: knots = x, values = y (n_knots cells, in
+   * the order the nearest-centre search scans them, meshes.py:104-108).       */
+  CTRAJ_TABLE_MESH = 3,
 };
 
 typedef struct ctraj_force_table {
   int32_t kind;
   int32_t n_knots;
-  const double* knots;  /* n_knots, ascending and uniformly spaced            */
+  const double* knots;  /* n_knots; STARK_SPLINE, RADIAL_LINEAR: ascending and
+                           uniformly spaced; MESH: cell centre x, any order    */
   const double* coef;   /* STARK_SPLINE: (n_knots - 1) * 4                    */
-  const double* values; /* RADIAL_LINEAR: n_knots                             */
+  const double* values; /* RADIAL_LINEAR, MESH: n_knots                       */
 } ctraj_force_table;
 
 /* ---- initial-condition distributions (distributions.py) ------------------- */
@@ -234,7 +249,9 @@ typedef struct ctraj_tuning {
 int ctraj_set_tuning(ctraj_context* ctx, const ctraj_tuning* tuning);
 int ctraj_get_tuning(ctraj_context* ctx, ctraj_tuning* tuning);
 
-/* ElectrostaticLens.a_interp / lens_acceleration table (electrostatic_lens.py:174-213). */
+/* ElectrostaticLens.a_interp / lens_acceleration table (electrostatic_lens.py:174-213),
+ * or the cell centres of a Honeycomb (meshes.py:53-62, kind CTRAJ_TABLE_MESH,
+ * at least one cell). */
 int ctraj_set_force_table(ctraj_context* ctx, int32_t table_id,
                           const ctraj_force_table* table);
 
@@ -450,7 +467,7 @@ int ctraj_soft_transmission(ctraj_context* ctx, const ctraj_soft_args* args,
  * the GPU (from two host threads, or on two streams) race: serialize them.
  */
 #define CTRAJ_NOALLOC_MAX_MOLECULES 131072
-#define CTRAJ_NOALLOC_MAX_INTERVALS 16384 /* FP32 table intervals over all lenses */
+#define CTRAJ_NOALLOC_MAX_INTERVALS 16384 /* FP32 table intervals over all lenses + honeycomb cells */
 #define CTRAJ_NOALLOC_SCRATCH_BYTES (32u << 20)
 int ctraj_run_noalloc(const ctraj_element* elements, int32_t n_elements,
                       int32_t n_labels, const ctraj_force_table* tables,

@@ -22,6 +22,9 @@
  *                           STARK_SPLINE   a_r(r) = -(W'(E) * dE/dr) / m with
  *                                          E = alpha r^n and W' the scipy PPoly
  *                                          derivative (nu = 1) evaluation order
+ *   honeycomb             meshes.py:85-117 (argmin over all cell centres, re-done
+ *                         while the cell index is 0 -- `if not idx`; hexagon
+ *                         interior of the RegularPolygon of meshes.py:71-78)
  *   propagate             beamline.py:20-38 (walk, early exit, "Detected")
  *   rows                  Trajectory.update / drop_nans (molecule.py:133-167):
  *                         the step count is the number of finite-t rows - 1
@@ -336,6 +339,50 @@ static void lens(mol_t* m, const beam_t* b, const ctraj_element* e, int* range_c
   mol_update(m, dt, b->g);
 }
 
+/* Honeycomb.propagate_through, meshes.py:87-117: flight to z0 and z1; at each
+ * plane the molecule must lie inside the hexagon of "its" cell, the cell with
+ * the nearest centre found at z0 -- and again at z1 when that cell has index
+ * 0, because the reference tests `if not idx:` (:104) and 0 is falsy.  The
+ * distances are numpy's sqrt((px - xc)**2 + (py - yc)**2) (:105-107), the first
+ * minimum wins (argmin); the hexagon is matplotlib's RegularPolygon((xc, yc),
+ * 6, radius=R) with a vertex on +y (:71-78), interior: |dx| < R sqrt(3)/2 and
+ * |dy| < R - |dx|/sqrt(3).  Edge margins: the hexagon's sides and half the gap
+ * between the nearest and second-nearest centre. */
+static void honeycomb(mol_t* m, const beam_t* b, const ctraj_element* e) {
+  const ctraj_force_table* t = &b->tab[e->table];
+  const double zs[2] = {e->z0, e->z1};
+  const double s3 = sqrt(3.0), R = e->p[0];
+  int idx = -1; /* None */
+  for (int i = 0; i < 2; i++) {
+    double dt = (zs[i] - m->s.x[2]) / m->s.v[2];
+    mol_update(m, dt, b->g);
+    const double px = m->s.x[0], py = m->s.x[1];
+    if (idx <= 0) {
+      double best = INFINITY, second = INFINITY;
+      for (int k = 0; k < t->n_knots; k++) {
+        const double dx = px - t->knots[k], dy = py - t->values[k];
+        const double d = sqrt(dx * dx + dy * dy);
+        if (d < best) {
+          second = best;
+          best = d;
+          idx = k;
+        } else if (d < second) {
+          second = d;
+        }
+      }
+      if (idx < 0) idx = 0; /* no finite distance: argmin of all-NaN is 0 */
+      note_margin(m, (second - best) / 2.0);
+    }
+    const double dx = fabs(px - t->knots[idx]), dy = fabs(py - t->values[idx]);
+    const double side = R * s3 / 2.0 - dx, slant = (R - dx / s3 - dy) * (s3 / 2.0);
+    note_margin(m, side < slant ? side : slant);
+    if (!(dx < R * s3 / 2.0 && dy < R - dx / s3)) {
+      kill(m, e->label);
+      return;
+    }
+  }
+}
+
 /* Molecule.init_trajectory + Beamline.propagate_through */
 static void propagate(const beam_t* b, const double ic[6], mol_t* m, int* range_count) {
   m->alive = 1;
@@ -357,6 +404,7 @@ static void propagate(const beam_t* b, const double ic[6], mol_t* m, int* range_
       case CTRAJ_RECTANGULAR_APERTURE: rectangular_aperture(m, e, b->g); break;
       case CTRAJ_FIELD_PLATES: field_plates(m, e, b->g); break;
       case CTRAJ_ELECTROSTATIC_LENS: lens(m, b, e, range_count); break;
+      case CTRAJ_HONEYCOMB: honeycomb(m, b, e); break;
       default: m->err = CTRAJ_EINVAL; m->alive = 0; break;
     }
   }

@@ -8,7 +8,8 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-CASES = ["config0", "config1", "example_lens", "kat_circle", "kat_rect", "kat_plates", "kat_lens"]
+CASES = ["config0", "config1", "example_lens", "kat_circle", "kat_rect", "kat_plates", "kat_lens",
+         "kat_honeycomb"]
 
 
 def available():

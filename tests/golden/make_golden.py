@@ -189,8 +189,114 @@ def kat_cases():
             [0.0, 0.0, 2.2, 0.0, 0.0, 184.0],       # on axis: r == 0 branch
             [1e-3, 1e-3, 0.0, 0.0, 0.0, -184.0],    # negative vz: N = rint(L/dz) with dz fixed
         ]).T)
+    cases["kat_honeycomb"] = honeycomb_case()
     # the classic-RK4 scheme and field order 1 are extensions: no reference output exists
     return cases
+
+
+# ---- honeycomb (meshes.py) ---------------------------------------------------
+#
+# The reference's Honeycomb takes its cell centres from hexalattice.make_grid
+# and its hexagons from matplotlib.patches.RegularPolygon; neither package is
+# installed.  Stand-ins restating both are installed into the reference's
+# meshes module, so its own __post_init__ (nx, ny, patch radius) and
+# propagate_through (flights, argmin, the `if not idx` re-lookup, labels) run.
+# The fixture therefore pins that control flow and arithmetic, and checks the
+# product's lattice and hexagon test against these independent restatements
+# (a polygon crossing-number test on cos/sin vertices, like matplotlib's
+# point_in_path); it does not pin hexalattice or matplotlib themselves.
+
+HALF_SQRT3 = np.sqrt(3) / 2
+
+
+def stand_in_make_grid(nx, ny, n=0, min_diam=1.0, align_to_origin=True, crop_circ=0.0, rotate_deg=0.0):
+    """hexalattice make_grid for the arguments meshes.py:54-62 passes: rows of nx
+    cells (odd rows shifted half a pitch), the centre cell moved to the origin."""
+    import math
+
+    assert n == 0 and align_to_origin and crop_circ == 0 and rotate_deg == 0
+    mid_row, mid_col = math.ceil(ny / 2) - 1, math.ceil(nx / 2) - 1
+    mid_x = (mid_col + (0.5 if mid_row % 2 else 0.0)) * min_diam
+    mid_y = (mid_row * HALF_SQRT3) * min_diam
+    xs, ys = [], []
+    for j in range(ny):
+        for i in range(nx):
+            xs.append((i + (0.5 if j % 2 else 0.0)) * min_diam - mid_x)
+            ys.append((j * HALF_SQRT3) * min_diam - mid_y)
+    return np.array(xs).reshape(-1, 1), np.array(ys).reshape(-1, 1)
+
+
+class StandInRegularPolygon:
+    """matplotlib RegularPolygon(xy, numVertices, radius) with orientation 0:
+    vertices at angles pi/2 + 2 pi k / n; contains_point by crossing number."""
+
+    def __init__(self, xy, numVertices, radius=5.0, orientation=0.0, **kwargs):
+        x0, y0 = (float(np.ravel(v)[0]) for v in xy)
+        th = np.pi / 2 + 2 * np.pi / numVertices * np.arange(numVertices) + orientation
+        self.vx = radius * np.cos(th) + x0
+        self.vy = radius * np.sin(th) + y0
+
+    def contains_point(self, point):
+        px, py = float(point[0]), float(point[1])
+        if not (np.isfinite(px) and np.isfinite(py)):
+            return False
+        inside = False
+        j = len(self.vx) - 1
+        for i in range(len(self.vx)):
+            if (self.vy[i] > py) != (self.vy[j] > py):
+                xc = (self.vx[j] - self.vx[i]) * (py - self.vy[i]) / (self.vy[j] - self.vy[i]) + self.vx[i]
+                if px < xc:
+                    inside = not inside
+            j = i
+        return inside
+
+
+def install_mesh_stand_ins():
+    import trajectories.beamline_elements.meshes as meshes
+
+    meshes.hexalattice.make_grid = stand_in_make_grid
+    meshes.RegularPolygon = StandInRegularPolygon
+
+
+def honeycomb_case():
+    """Aperture, honeycomb, lens, a coarser honeycomb behind the lens, plane."""
+    lc = 25.4e-3 / 16
+    hc0, hc_len, vz = 0.5, 0.0254, 184.0
+    nx = int(np.ceil(2 * 25.4e-3 / (lc * np.sqrt(3))))
+    ny = int(np.ceil(2 * 25.4e-3 / (lc * 3 / 2)))
+    xc, yc = (a.ravel() for a in stand_in_make_grid(nx, ny, 0, lc * np.sqrt(3)))
+    t_fly = hc_len / vz
+    mid = (int(np.ceil(ny / 2)) - 1) * nx + int(np.ceil(nx / 2)) - 1
+
+    def hop(a, b, dx=2e-4, dy=1e-4):
+        """starts near cell a's centre at z0, reaches cell b's centre at z1"""
+        x0, y0 = xc[a] + dx, yc[a] + dy
+        return [x0, y0, hc0, (xc[b] - x0) / t_fly, (yc[b] - y0) / t_fly, vz]
+
+    known = np.array([
+        hop(0, 1),               # cell 0 at z0: looked up again at z1, survives in cell 1
+        hop(1, 2),               # cell 1 keeps its index: outside it at z1, lost
+        hop(mid, mid),           # centre cell, straight through
+        hop(mid, mid + 1),       # drifts into the neighbour: lost
+        hop(0, 0, 0.0, 0.0),     # centre of cell 0
+        [0.028, 0.0, hc0, 0.0, 0.0, vz],    # outside the grid, inside the aperture: lost
+        [-0.027, 0.026, hc0, 0.0, 0.0, vz],  # beyond a corner: lost
+        [xc[mid] + 1.25e-3, yc[mid], hc0, 0.0, 0.0, vz],  # in the wall band between cells: lost
+    ]).T
+    rng = np.random.default_rng(7)
+    beam = draw_ics(rng, 1500, 6e-3, 6e-3, 0.0, 4.0, 4.0, 184.0, 12.0)
+    lens = dict(cls="ElectrostaticLens", name="ES lens", z0=1.0, L=0.3, d=0.03, dz=1e-3, V=20e3,
+                force=dict(table="hex_kat", V=20e3, R=0.015, mass=TLF_MASS, order=2))
+    return dict(
+        elements=[
+            dict(cls="CircularAperture", name="Aperture", z0=0.2, L=0.005, d=0.15),
+            dict(cls="Honeycomb", name="Honeycomb", z0=hc0, L=hc_len),
+            lens,
+            dict(cls="Honeycomb", name="Honeycomb 2", z0=1.6, L=0.01, width=0.03, height=0.03,
+                 cell_wall_length=25.4e-3 / 8, cell_wall_thickness=2e-4),
+            dict(cls="CircularAperture", name="Detection plane", z0=2.0, L=0.0, d=INF),
+        ],
+        ics=np.hstack([known, beam]))
 
 
 def draw_ics(rng, n, sx, sy, z, svx, svy, vz, svz):
@@ -242,9 +348,10 @@ def build_reference_beamline(specs, tables):
     from trajectories.beamline_elements.apertures import (CircularAperture, FieldPlates,
                                                           RectangularAperture)
     from trajectories.beamline_elements.electrostatic_lens import ElectrostaticLens
+    from trajectories.beamline_elements.meshes import Honeycomb
 
     classes = dict(CircularAperture=CircularAperture, RectangularAperture=RectangularAperture,
-                   FieldPlates=FieldPlates, ElectrostaticLens=ElectrostaticLens)
+                   FieldPlates=FieldPlates, ElectrostaticLens=ElectrostaticLens, Honeycomb=Honeycomb)
     elems = []
     for s in specs:
         kw = {k: v for k, v in s.items() if k not in ("cls", "force", "dt")}
@@ -300,6 +407,7 @@ def main():
     import refstubs
 
     refstubs.install(args.reference_src)
+    install_mesh_stand_ins()
     import numpy
     import scipy
 

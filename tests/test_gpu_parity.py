@@ -80,7 +80,8 @@ def test_fp32_within_tolerance(engine, case):
     assert np.mean(r.rows[same] == o["rows"][same]) > 0.999
 
 
-@pytest.mark.parametrize("case", [c for c in CASES if c in ("config0", "config1", "example_lens", "kat_lens")])
+@pytest.mark.parametrize("case", [c for c in CASES
+                                  if c in ("config0", "config1", "example_lens", "kat_lens", "kat_honeycomb")])
 def test_record_traces_match_reference(engine, case):
     fx = fixtures.load(case)
     cb = compile_beamline(fixtures.build_beamline(fx))
