@@ -105,10 +105,13 @@ struct ctraj_context {
   DevBuf chunk_ctl;             // (count, max_steps) of the queue each lens chunk writes
   DevBuf rec_stage;             // ring recording: staged records of the recorded lens
   DevBuf ring_ent;              // ring recording: molecules stopped by the entrance test
+  DevBuf lens_order;            // persistent lens pass: bucket counts | entrant order
   int chunk = 64;               // RK4 steps of the first lens chunk (compaction interval)
   int chunk_growth = 200;       // percent: each chunk's length relative to the previous
   int chunk_max = 1024;         // longest chunk
   int front_waves = 4;          // k_front grid in units of resident CTAs
+  int lens_mode = CTRAJ_LENS_PERSISTENT;  // FP32 lens pass
+  int lens_interval = 256;      // persistent mode: steps between CTA compactions
   bool timing = false;
   // before front, after front, before the first lens chunk, after the last one
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -372,6 +375,48 @@ LensKernel lens_kernel(int force, bool staged) {
   return staged ? lens_kernel32<kOut, true, kRing>(force) : lens_kernel32<kOut, false, kRing>(force);
 }
 
+// The persistent FP32 lens pass of lens element i over queue Qin (count
+// entries, at most max_steps steps each): order the entrants longest first,
+// then one k_lens_persist launch, one CTA per SM.
+template <bool kOut>
+int launch_persistent(ctraj_context* c, const Plan& P, const RunDev& R, int i, const Queue& Qin, const Queue& Qnext,
+                      unsigned count, unsigned max_steps, int* launches) {
+  cudaStream_t s = c->stream;
+  using M = Mol32<kOut, false>;
+  using PK = void (*)(const Plan, const RunDev, const int, const Queue, const Queue, const LensArgs,
+                      const unsigned*, const int);
+  const bool staged = P.lf[i].n_smem > 0;
+  PK k;
+  switch (P.lf[i].force) {
+    case kForceStark2:
+      k = staged ? k_lens_persist<M, kOut, kForceStark2, true> : k_lens_persist<M, kOut, kForceStark2, false>;
+      break;
+    case kForceStark1:
+      k = staged ? k_lens_persist<M, kOut, kForceStark1, true> : k_lens_persist<M, kOut, kForceStark1, false>;
+      break;
+    default:
+      k = staged ? k_lens_persist<M, kOut, kForceRadial, true> : k_lens_persist<M, kOut, kForceRadial, false>;
+      break;
+  }
+  const size_t smem = (staged ? size_t(P.lf[i].n_int) * sizeof(float4) : 0) + kPersistThreads * sizeof(SwapSlot);
+  CT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  int st = c->lens_order.ensure((size_t(kOrderBuckets) + count) * sizeof(unsigned));
+  if (st) return st;
+  unsigned* hist = c->lens_order.as<unsigned>();
+  unsigned* order = hist + kOrderBuckets;
+  const float scale = float(kOrderBuckets - 1) / (float(max_steps) + 1.0f);
+  const int grid = c->sm_count * 4;
+  CT_CUDA(cudaMemsetAsync(hist, 0, kOrderBuckets * sizeof(unsigned), s));
+  k_order_count<<<grid, 256, 0, s>>>(P, i, Qin, scale, hist);
+  k_order_scan<<<1, kOrderBuckets, 0, s>>>(hist);
+  k_order_place<<<grid, 256, 0, s>>>(P, i, Qin, scale, hist, order);
+  k<<<c->sm_count, kPersistThreads, smem, s>>>(P, R, i, Qin, Qnext, lens_args(P, i, true), order,
+                                                c->lens_interval);
+  CT_CUDA(cudaGetLastError());
+  *launches += 4;
+  return CTRAJ_OK;
+}
+
 // k_front, then for each lens: read the lens queue's size and largest
 // remaining step count (one small device-to-host copy), and launch
 // ceil(max / chunk) chunk kernels that ping-pong between two queues while
@@ -427,6 +472,15 @@ int launch_all(ctraj_context* c, const Plan& P, const RunDev& R0, Queue* q, int*
       R.rec_m0 = reinterpret_cast<unsigned long long*>(b + recb + 5 * sb + align256(size_t(count) * 8));
       CT_CUDA(cudaMemsetAsync(R.rec_n, 0, sb, s));
       ring_slots = count;
+    }
+    if constexpr (!k64 && !kRing) {
+      if (c->lens_mode == CTRAJ_LENS_PERSISTENT) {
+        int st = launch_persistent<kOut>(c, P, R, i, q[cur], q[nxt], count, max_steps, launches);
+        if (st) return st;
+        c->host_max[2 + i] = 0;  // no continuation queue
+        std::swap(cur, nxt);
+        continue;
+      }
     }
     CT_CUDA(cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     const int64_t per_launch = int64_t(blocks_per_sm(kl, kLensThreads, smem)) * c->sm_count;
@@ -597,6 +651,7 @@ int ctraj_destroy(ctraj_context* c) {
   c->chunk_ctl.release();
   c->rec_stage.release();
   c->ring_ent.release();
+  c->lens_order.release();
   if (c->sweep_exec) cudaGraphExecDestroy(c->sweep_exec);
   for (int t = 0; t < CTRAJ_MAX_TABLES; ++t) {
     if (c->side[t]) cudaStreamSynchronize(c->side[t]);
@@ -626,13 +681,19 @@ int ctraj_destroy(ctraj_context* c) {
 int ctraj_set_tuning(ctraj_context* c, const ctraj_tuning* t) {
   if (!c || !t) return fail(CTRAJ_EINVAL, "NULL argument");
   if (t->chunk_first < 1 || t->chunk_max < t->chunk_first || t->chunk_max > 1000000 ||
-      t->chunk_growth < 100 || t->chunk_growth > 1000 || t->front_waves < 1 || t->front_waves > 64)
-    return fail(CTRAJ_EINVAL, "tuning out of range (chunk_first %d, chunk_growth %d, chunk_max %d, front_waves %d)",
-                t->chunk_first, t->chunk_growth, t->chunk_max, t->front_waves);
+      t->chunk_growth < 100 || t->chunk_growth > 1000 || t->front_waves < 1 || t->front_waves > 64 ||
+      (t->lens_mode != CTRAJ_LENS_PERSISTENT && t->lens_mode != CTRAJ_LENS_CHUNKED) || t->lens_interval < 1 ||
+      t->lens_interval > 100000)
+    return fail(CTRAJ_EINVAL,
+                "tuning out of range (chunk_first %d, chunk_growth %d, chunk_max %d, front_waves %d, lens_mode %d, "
+                "lens_interval %d)",
+                t->chunk_first, t->chunk_growth, t->chunk_max, t->front_waves, t->lens_mode, t->lens_interval);
   c->chunk = t->chunk_first;
   c->chunk_growth = t->chunk_growth;
   c->chunk_max = t->chunk_max;
   c->front_waves = t->front_waves;
+  c->lens_mode = t->lens_mode;
+  c->lens_interval = t->lens_interval;
   ++c->generation;
   return CTRAJ_OK;
 }
@@ -643,6 +704,8 @@ int ctraj_get_tuning(ctraj_context* c, ctraj_tuning* t) {
   t->chunk_growth = c->chunk_growth;
   t->chunk_max = c->chunk_max;
   t->front_waves = c->front_waves;
+  t->lens_mode = c->lens_mode;
+  t->lens_interval = c->lens_interval;
   return CTRAJ_OK;
 }
 

@@ -17,6 +17,10 @@
 //   are lost at very different steps.  Molecules that leave the lens do the
 //   exit snap and the ballistic elements after it here, then are tallied or
 //   queued at the next lens.
+// k_lens_persist (FP32 runs): the whole lens in one launch, lanes refilled
+//   from the queue as their molecules finish, the last molecules compacted
+//   into few warps (see the kernel); k_lens_chunk remains the path for FP64,
+//   ring recording and batched sweeps.
 // k_record: replays chosen molecules one thread each and writes their
 //   trajectory rows (trajectory recording for apertures of interest).
 //
@@ -434,6 +438,275 @@ __global__ void __launch_bounds__(kLensThreads, 2) k_lens_chunk(const __grid_con
     push_lens<(kSweep || kRing) ? kTagCarry : kTagNone>(Qnext, enter, m, nst, kRing ? tag : cfg);
     tally_warp(S, label, P.n_labels);
     if (kSweep) tally_cfg(R, cfg, label, P.n_labels);
+  }
+  stat_add(S, kStatSteps, steps);
+  stat_add(S, kStatLensSteps, lsteps);
+  stat_add(S, kStatEdgeBand, band);
+  stat_add(S, kStatBadSteps, bad);
+  stat_add(S, kStatTableRange, range);
+  stat_add(S, kStatRangeError, rerr);
+  tally_flush(S, R, P.n_labels);
+}
+
+// ---------------------------------------------------------------------------
+// Lens-entrant order for k_lens_persist: longest step count first.  In a lens
+// pass the molecules that need the most RK4 steps (the slowest, ~5000 steps
+// at dt = 1 us) form the critical path; taking them first starts that path
+// at once.  A counting sort on L / dz in kOrderBuckets buckets, three
+// launches: count, exclusive scan (one block), place.  The order changes no
+// result: molecules are independent and tallies are integer sums.
+constexpr int kOrderBuckets = 1024;
+
+// bucket 0 = most steps; scale = (kOrderBuckets - 1) / (largest step count + 1)
+__device__ __forceinline__ int order_bucket(const ctraj_element& e, float vz, float scale) {
+  const float dz = e.step_mode == CTRAJ_STEP_DT ? fabsf(vz) * float(e.p[2]) : float(e.p[1]);
+  const float u = float(kOrderBuckets - 1) - (float(e.p[7]) / dz) * scale;  // NaN, -inf -> 0
+  return u > 0.0f ? (u < float(kOrderBuckets - 1) ? int(u) : kOrderBuckets - 1) : 0;
+}
+
+__global__ void __launch_bounds__(256) k_order_count(const __grid_constant__ Plan P, const int li, const Queue Q,
+                                                     const float scale, unsigned* hist) {
+  const unsigned n = *Q.count;
+  for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+    atomicAdd(hist + order_bucket(P.el[li], Q.vz[j], scale), 1u);
+}
+
+__global__ void __launch_bounds__(kOrderBuckets) k_order_scan(unsigned* hist) {
+  __shared__ unsigned t[kOrderBuckets];
+  const int i = threadIdx.x;
+  const unsigned own = hist[i];
+  t[i] = own;
+  __syncthreads();
+  for (int o = 1; o < kOrderBuckets; o <<= 1) {
+    const unsigned v = i >= o ? t[i - o] : 0u;
+    __syncthreads();
+    t[i] += v;
+    __syncthreads();
+  }
+  hist[i] = t[i] - own;
+}
+
+__global__ void __launch_bounds__(256) k_order_place(const __grid_constant__ Plan P, const int li, const Queue Q,
+                                                     const float scale, unsigned* cursor, unsigned* order) {
+  const unsigned n = *Q.count;
+  for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+    order[atomicAdd(cursor + order_bucket(P.el[li], Q.vz[j], scale), 1u)] = j;
+}
+
+// ---------------------------------------------------------------------------
+// k_lens_persist: one launch integrates a whole lens queue (FP32), one CTA
+// per SM, 16 warps.
+//
+// Phase A (molecules left in the queue): every kPersistService steps a warp
+// finalises its lanes whose molecule was lost or left the lens (exit snap,
+// the elements after the lens, tally, next-lens queue) and refills them from
+// the queue in `order`, so lanes stay busy while work remains.
+// Phase B (queue empty): every `interval` steps the CTA counts its molecules
+// and, when they fit in fewer warps, moves them through shared memory into
+// the lowest warps.  The emptied warps wait at the barrier without issuing,
+// so the last, longest-lived molecules run with little contention for the
+// SM's issue slots -- their step time approaches the latency of one RK4 step.
+//
+// The molecule state a lane carries (SwapSlot) is what the RK4 loop needs;
+// the rest (t, vz, rows, id, queued margin) is read back from the queue entry
+// at finalisation, as k_lens_chunk does.
+struct SwapSlot {
+  float4 a;  // x, y, vx, vy
+  float4 b;  // cx, cy, cvx, cvy
+  double dt, snap;
+  int4 c;    // n_done, n_total, n0, idx
+  unsigned flags, phase;
+  float margin, pad;
+};
+
+constexpr int kPersistThreads = 512;
+constexpr int kPersistService = 16;
+
+template <class M, bool kOut, int F, bool kStaged>
+__global__ void __launch_bounds__(kPersistThreads, 1) k_lens_persist(const __grid_constant__ Plan P, const RunDev R,
+                                                                     const int li, const Queue Qin, const Queue Qnext,
+                                                                     const LensArgs L, const unsigned* order,
+                                                                     const int interval) {
+  extern __shared__ float4 s_dyn[];
+  __shared__ BlockTally S;
+  __shared__ unsigned s_wcount[kPersistThreads / 32];
+  const float4* s_tab = s_dyn;
+  SwapSlot* s_swap = reinterpret_cast<SwapSlot*>(s_dyn + (kStaged ? L.n_int : 0));
+  const unsigned n_in = *(volatile unsigned*)Qin.count;
+  if (n_in == 0) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned lanes_lt = (1u << lane) - 1u;
+  // each warp's first 32 entries are fixed and interleaved across CTAs, so
+  // that a short queue spreads over all SMs; the rest are taken in order
+  const unsigned static_entries = gridDim.x * kPersistThreads;
+  tally_init(S);
+  if (kStaged)
+    for (int k = threadIdx.x; k < L.n_int; k += blockDim.x) s_dyn[k] = __ldg(L.q + k);
+  __syncthreads();
+  const ctraj_element& e = P.el[li];
+  const bool classic = e.scheme == CTRAJ_RK4_CLASSIC;
+  unsigned long long steps = 0, lsteps = 0, band = 0, bad = 0, range = 0, rerr = 0;
+
+  M m;
+  LensStep st, nst;
+  st.n_done = 0;
+  int phase = kIdle;
+  unsigned flags = 0;
+  float dt = 0.f, hdt = 0.f, c2 = 0.f, dt6 = 0.f, dt26 = 0.f;
+  int n0 = 0;
+  bool fresh = false;
+  unsigned idx = 0;
+
+  auto derive = [&]() {
+    dt = float(st.dt);
+    hdt = 0.5f * dt;
+    c2 = classic ? hdt : dt;
+    dt6 = dt * (1.0f / 6.0f);
+    dt26 = float(st.dt * st.dt / 6.0);
+  };
+  auto take = [&](unsigned j) {  // queue position j
+    idx = order ? __ldg(order + j) : j;
+    flags = 0;
+    m.load_state(Qin, idx, P, st);
+    bool ok = true;
+    fresh = st.n_total < 0;
+    if (fresh) {  // step setup deferred by the front kernel
+      m.load_vz(Qin, idx);
+      ok = enter_lens(m, P, li, st);
+    }
+    n0 = st.n_done;
+    derive();
+    phase = !ok ? kBad : (st.n_done < st.n_total ? kRun : kExit);
+  };
+  auto run = [&](int n_steps) {
+    if (!__any_sync(kFull, phase == kRun)) return;
+    for (int k = 0; k < n_steps; ++k) {
+      if (phase == kRun) {
+        bool lost = m.template lens_step<F, kStaged>(L, dt, hdt, c2, dt6, dt26, s_tab, flags);
+        if (F == kForceRadial && (flags & 2u)) lost = true;
+        ++st.n_done;
+        if (lost) phase = kLost;
+        else if (st.n_done == st.n_total) phase = kExit;
+      }
+    }
+  };
+  // all lanes: the lanes whose molecule is lost or left the lens are tallied
+  // (or queued at the next lens) and become idle
+  auto finalize = [&]() {
+    if (!__any_sync(kFull, phase == kLost || phase == kExit || phase == kBad)) return;
+    int label = kNone;
+    bool enter = false;
+    if (phase == kLost || phase == kExit || phase == kBad) {
+      m.load_rest(Qin, idx, st, !fresh);
+      lsteps += unsigned(st.n_done - n0);
+      if (phase == kBad) {  // rint(L/dz) not usable: the reference raises here
+        label = e.label_inside;
+        ++bad;
+        steps += unsigned(m.rows);
+        write_outputs<M, kOut>(R, m, label);
+      } else {
+        range += (flags & 1u) ? 1 : 0;
+        rerr += (flags & 2u) ? 1 : 0;
+        m.lens_end(P, li, st, phase == kLost);
+        if (phase == kLost) {
+          label = e.label_inside;
+        } else {
+          int lens_at = -1;
+          label = walk(m, P, li + 1, &lens_at);
+          if (label == kQueued) {
+            enter = enter_lens(m, P, lens_at, nst);
+            if (!enter) {
+              label = P.el[lens_at].label_inside;
+              ++bad;
+            }
+          }
+        }
+        if (label != kQueued) {
+          steps += unsigned(m.rows);
+          band += (m.margin < double(kEdgeBand)) ? 1 : 0;
+          write_outputs<M, kOut>(R, m, label);
+        }
+      }
+      phase = kIdle;
+    }
+    push_lens<kTagNone>(Qnext, enter, m, nst);
+    tally_warp(S, label, P.n_labels);
+  };
+
+  {
+    const unsigned j = (unsigned(warp) * gridDim.x + blockIdx.x) * 32u + unsigned(lane);
+    if (j < n_in) take(j);
+  }
+  // phase A
+  for (bool exhausted = static_entries >= n_in; !exhausted;) {
+    run(kPersistService);
+    finalize();
+    const unsigned idle = __ballot_sync(kFull, phase == kIdle);
+    if (idle) {
+      unsigned b = 0;
+      if (lane == 0) b = atomicAdd(Qin.head, unsigned(__popc(idle)));
+      b = static_entries + __shfl_sync(kFull, b, 0);
+      exhausted = b + unsigned(__popc(idle)) >= n_in;
+      if (phase == kIdle && b + __popc(idle & lanes_lt) < n_in) take(b + __popc(idle & lanes_lt));
+    } else {
+      exhausted = static_entries + *(volatile unsigned*)Qin.head >= n_in;
+    }
+  }
+  // phase B (every warp of the CTA enters it, then the barriers below match)
+  for (;;) {
+    run(interval);
+    finalize();
+    const unsigned held = __ballot_sync(kFull, phase != kIdle);
+    if (lane == 0) s_wcount[warp] = __popc(held);
+    __syncthreads();
+    unsigned total = 0, base = 0, used = 0;
+#pragma unroll
+    for (int w = 0; w < kPersistThreads / 32; ++w) {
+      const unsigned c = s_wcount[w];
+      base += w < warp ? c : 0u;
+      total += c;
+      used += c ? 1u : 0u;
+    }
+    __syncthreads();
+    if (total == 0) break;
+    if ((total + 31) / 32 < used) {
+      if (phase != kIdle) {
+        SwapSlot& w = s_swap[base + __popc(held & lanes_lt)];
+        w.a = make_float4(m.x, m.y, m.vx, m.vy);
+        w.b = make_float4(m.cx, m.cy, m.cvx, m.cvy);
+        w.dt = st.dt;
+        w.snap = st.snap;
+        w.c = make_int4(st.n_done, st.n_total, n0, int(idx));
+        w.flags = flags | (fresh ? 0x80000000u : 0u);
+        w.phase = unsigned(phase);
+        w.margin = m.margin;
+      }
+      __syncthreads();
+      phase = kIdle;
+      if (threadIdx.x < total) {
+        const SwapSlot& w = s_swap[threadIdx.x];
+        m.x = w.a.x;
+        m.y = w.a.y;
+        m.vx = w.a.z;
+        m.vy = w.a.w;
+        m.cx = w.b.x;
+        m.cy = w.b.y;
+        m.cvx = w.b.z;
+        m.cvy = w.b.w;
+        st.dt = w.dt;
+        st.snap = w.snap;
+        st.n_done = w.c.x;
+        st.n_total = w.c.y;
+        n0 = w.c.z;
+        idx = unsigned(w.c.w);
+        flags = w.flags & 0x7fffffffu;
+        fresh = (w.flags >> 31) != 0;
+        phase = int(w.phase);
+        m.margin = w.margin;
+        derive();
+      }
+      __syncthreads();
+    }
   }
   stat_add(S, kStatSteps, steps);
   stat_add(S, kStatLensSteps, lsteps);

@@ -553,15 +553,6 @@ struct Mol32 {
   float cx, cy, cvx, cvy;  // rounding errors carried by the lens integration
   RowSink* sink;
 
-  // s += inc with the rounding error carried in c (Fast2Sum: |s| >= |inc + c|
-  // holds because one step changes x and v by far less than their size)
-  __device__ __forceinline__ static void accumulate(float& s, float& c, float inc) {
-    const float d = __fadd_rn(inc, c);
-    const float t = __fadd_rn(s, d);
-    c = __fadd_rn(d, -__fadd_rn(t, -s));
-    s = t;
-  }
-
   __device__ void row_out() {
     if (kRec) sink->put(x, y, zc, vx, vy, vz, ax, ay, 0.0, t);
   }
@@ -700,30 +691,50 @@ struct Mol32 {
       const float w = wforce<F, kStaged>(px, py, L, s_tab, flags, b);
       return kScaled ? __fmul_rn(kappa, w) : w;
     };
+    // The (x, y) pairs go through the packed FP32 instructions of sm_100+
+    // (FFMA2 / FADD2 / FMUL2): per component the same rounding as the scalar
+    // operations, half the instructions.  Increments are formed in full
+    // precision, then added once with the carried rounding error (the lens
+    // defocuses, so uncompensated rounding of x and v grows to micrometres at
+    // the detector).
+    const float2 p = make_float2(x, y), v = make_float2(vx, vy);
+    const float2 Hdt = make_float2(hdt, hdt), Dt = make_float2(dt, dt), G0 = make_float2(0.0f, -g);
     const float w1 = force(x, y);
-    const float l1x = __fmul_rn(w1, x), l1y = __fmaf_rn(w1, y, -g);
-    const float k2x = __fmaf_rn(hdt, l1x, vx), k2y = __fmaf_rn(hdt, l1y, vy);
-    const float p2x = __fmaf_rn(c2, vx, x), p2y = __fmaf_rn(c2, vy, y);
-    const float w2 = force(p2x, p2y);
-    const float l2x = __fmul_rn(w2, p2x), l2y = __fmaf_rn(w2, p2y, -g);
-    const float k3x = __fmaf_rn(hdt, l2x, vx), k3y = __fmaf_rn(hdt, l2y, vy);
-    const float p3x = __fmaf_rn(hdt, k2x, x), p3y = __fmaf_rn(hdt, k2y, y);
-    const float w3 = force(p3x, p3y);
-    const float l3x = __fmul_rn(w3, p3x), l3y = __fmaf_rn(w3, p3y, -g);
-    const float p4x = __fmaf_rn(dt, k3x, x), p4y = __fmaf_rn(dt, k3y, y);
-    const float w4 = force(p4x, p4y);
-    const float l4x = __fmul_rn(w4, p4x), l4y = __fmaf_rn(w4, p4y, -g);
-    const float sx = __fadd_rn(__fadd_rn(l1x, l2x), l3x);
-    const float sy = __fadd_rn(__fadd_rn(l1y, l2y), l3y);
-    // increments are formed in full precision, then added once with the
-    // carried rounding error (the lens defocuses, so uncompensated rounding of
-    // x and v grows to micrometres at the detector)
-    accumulate(x, cx, __fmaf_rn(dt26, sx, __fmul_rn(dt, vx)));
-    accumulate(y, cy, __fmaf_rn(dt26, sy, __fmul_rn(dt, vy)));
-    accumulate(vx, cvx, __fmul_rn(dt6, __fmaf_rn(2.0f, __fadd_rn(l2x, l3x), __fadd_rn(l1x, l4x))));
-    accumulate(vy, cvy, __fmul_rn(dt6, __fmaf_rn(2.0f, __fadd_rn(l2y, l3y), __fadd_rn(l1y, l4y))));
-    ax = l1x;
-    ay = l1y;
+    const float2 l1 = __ffma2_rn(make_float2(w1, w1), p, G0);
+    const float2 k2 = __ffma2_rn(Hdt, l1, v);
+    const float2 p2 = __ffma2_rn(make_float2(c2, c2), v, p);
+    const float w2 = force(p2.x, p2.y);
+    const float2 l2 = __ffma2_rn(make_float2(w2, w2), p2, G0);
+    const float2 k3 = __ffma2_rn(Hdt, l2, v);
+    const float2 p3 = __ffma2_rn(Hdt, k2, p);
+    const float w3 = force(p3.x, p3.y);
+    const float2 l3 = __ffma2_rn(make_float2(w3, w3), p3, G0);
+    const float2 p4 = __ffma2_rn(Dt, k3, p);
+    const float w4 = force(p4.x, p4.y);
+    const float2 l4 = __ffma2_rn(make_float2(w4, w4), p4, G0);
+    const float2 sum = __fadd2_rn(__fadd2_rn(l1, l2), l3);
+    const float2 dx = __ffma2_rn(make_float2(dt26, dt26), sum, __fmul2_rn(Dt, v));
+    const float2 dv = __fmul2_rn(make_float2(dt6, dt6),
+                                 __ffma2_rn(make_float2(2.0f, 2.0f), __fadd2_rn(l2, l3), __fadd2_rn(l1, l4)));
+    // s += inc with the rounding error carried in c, for both pairs (Fast2Sum:
+    // |s| >= |inc + c| holds because one step changes x and v by far less
+    // than their size)
+    auto neg = [](float2 a) { return make_float2(-a.x, -a.y); };
+    float2 cp = make_float2(cx, cy), cv = make_float2(cvx, cvy);
+    const float2 d1 = __fadd2_rn(dx, cp), t1 = __fadd2_rn(p, d1);
+    cp = __fadd2_rn(d1, neg(__fadd2_rn(t1, neg(p))));
+    const float2 d2 = __fadd2_rn(dv, cv), t2 = __fadd2_rn(v, d2);
+    cv = __fadd2_rn(d2, neg(__fadd2_rn(t2, neg(v))));
+    x = t1.x;
+    y = t1.y;
+    vx = t2.x;
+    vy = t2.y;
+    cx = cp.x;
+    cy = cp.y;
+    cvx = cv.x;
+    cvy = cv.y;
+    ax = l1.x;
+    ay = l1.y;
     const float r2 = __fmaf_rn(y, y, __fmul_rn(x, x));
     if (kOut) note(__fadd_rn(sqrtf(r2), -L.bore));
     return r2 > L.bore2;

@@ -142,7 +142,13 @@ class Tuning(ctypes.Structure):
         ("chunk_growth", ctypes.c_int32),
         ("chunk_max", ctypes.c_int32),
         ("front_waves", ctypes.c_int32),
+        ("lens_mode", ctypes.c_int32),
+        ("lens_interval", ctypes.c_int32),
     ]
+
+
+LENS_PERSISTENT = 0
+LENS_CHUNKED = 1
 
 
 class Sweep(ctypes.Structure):

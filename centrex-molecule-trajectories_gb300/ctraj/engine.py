@@ -78,8 +78,11 @@ class Engine:
         _abi.check(self.lib.ctraj_synchronize(self.ctx), self.lib)
 
     def set_tuning(self, chunk_first: int = 64, chunk_growth: int = 200, chunk_max: int = 1024,
-                   front_waves: int = 4):
-        t = _abi.Tuning(int(chunk_first), int(chunk_growth), int(chunk_max), int(front_waves))
+                   front_waves: int = 4, lens_mode: int = _abi.LENS_PERSISTENT, lens_interval: int = 256):
+        """ctraj_set_tuning: chunked-lens knobs, front grid, and the FP32 lens
+        pass (persistent or chunked) with its compaction interval."""
+        t = _abi.Tuning(int(chunk_first), int(chunk_growth), int(chunk_max), int(front_waves), int(lens_mode),
+                        int(lens_interval))
         _abi.check(self.lib.ctraj_set_tuning(self.ctx, ctypes.byref(t)), self.lib)
 
     def get_tuning(self) -> dict:

@@ -249,8 +249,9 @@ def test_results_do_not_depend_on_tuning(engine):
     xd, vd = (device_spec(d, r) for d, r in zip(source(), ("position", "velocity")))
     ref = engine.run(cb, 200_000, xdist=xd, vdist=vd, seed=9, outputs=True)
     try:
-        for t in (dict(chunk_first=16, chunk_growth=100, chunk_max=16, front_waves=1),
-                  dict(chunk_first=2048, chunk_growth=150, chunk_max=8192, front_waves=8)):
+        for t in (dict(chunk_first=16, chunk_growth=100, chunk_max=16, front_waves=1, lens_mode=1),
+                  dict(chunk_first=2048, chunk_growth=150, chunk_max=8192, front_waves=8, lens_mode=1),
+                  dict(lens_interval=1), dict(lens_interval=5000, front_waves=2)):
             engine.set_tuning(**t)
             r = engine.run(cb, 200_000, xdist=xd, vdist=vd, seed=9, outputs=True)
             np.testing.assert_array_equal(r.counts, ref.counts)
@@ -259,5 +260,9 @@ def test_results_do_not_depend_on_tuning(engine):
             assert r.molecule_steps == ref.molecule_steps
         with pytest.raises(ValueError):
             engine.set_tuning(chunk_first=0)
+        with pytest.raises(ValueError):
+            engine.set_tuning(lens_mode=2)
+        with pytest.raises(ValueError):
+            engine.set_tuning(lens_interval=0)
     finally:
         engine.set_tuning()
