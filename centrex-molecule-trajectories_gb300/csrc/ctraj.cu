@@ -405,11 +405,11 @@ int launch_persistent(ctraj_context* c, const Plan& P, const RunDev& R, int i, c
   unsigned* hist = c->lens_order.as<unsigned>();
   unsigned* order = hist + kOrderBuckets;
   const float scale = float(kOrderBuckets - 1) / (float(max_steps) + 1.0f);
-  const int grid = c->sm_count * 4;
+  const int grid = c->sm_count;
   CT_CUDA(cudaMemsetAsync(hist, 0, kOrderBuckets * sizeof(unsigned), s));
-  k_order_count<<<grid, 256, 0, s>>>(P, i, Qin, scale, hist);
+  k_order_count<<<grid, kOrderThreads, 0, s>>>(P, i, Qin, scale, hist);
   k_order_scan<<<1, kOrderBuckets, 0, s>>>(hist);
-  k_order_place<<<grid, 256, 0, s>>>(P, i, Qin, scale, hist, order);
+  k_order_place<<<grid, kOrderThreads, 0, s>>>(P, i, Qin, scale, hist, order);
   k<<<c->sm_count, kPersistThreads, smem, s>>>(P, R, i, Qin, Qnext, lens_args(P, i, true), order,
                                                 c->lens_interval);
   CT_CUDA(cudaGetLastError());

@@ -464,11 +464,29 @@ __device__ __forceinline__ int order_bucket(const ctraj_element& e, float vz, fl
   return u > 0.0f ? (u < float(kOrderBuckets - 1) ? int(u) : kOrderBuckets - 1) : 0;
 }
 
-__global__ void __launch_bounds__(256) k_order_count(const __grid_constant__ Plan P, const int li, const Queue Q,
-                                                     const float scale, unsigned* hist) {
-  const unsigned n = *Q.count;
-  for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
-    atomicAdd(hist + order_bucket(P.el[li], Q.vz[j], scale), 1u);
+// Each block takes a contiguous range of the queue and counts it in shared
+// memory first: the step counts of a beam cluster in a few buckets, where
+// global atomics from every thread would serialise.
+constexpr int kOrderThreads = 256;
+
+__device__ __forceinline__ void order_range(unsigned n, unsigned& lo, unsigned& hi) {
+  const unsigned per = (n + gridDim.x - 1) / gridDim.x;
+  lo = min(n, blockIdx.x * per);
+  hi = min(n, lo + per);
+}
+
+__global__ void __launch_bounds__(kOrderThreads) k_order_count(const __grid_constant__ Plan P, const int li,
+                                                               const Queue Q, const float scale, unsigned* hist) {
+  __shared__ unsigned h[kOrderBuckets];
+  for (int b = threadIdx.x; b < kOrderBuckets; b += blockDim.x) h[b] = 0;
+  __syncthreads();
+  unsigned lo, hi;
+  order_range(*Q.count, lo, hi);
+  for (unsigned j = lo + threadIdx.x; j < hi; j += blockDim.x)
+    atomicAdd(h + order_bucket(P.el[li], Q.vz[j], scale), 1u);
+  __syncthreads();
+  for (int b = threadIdx.x; b < kOrderBuckets; b += blockDim.x)
+    if (h[b]) atomicAdd(hist + b, h[b]);
 }
 
 __global__ void __launch_bounds__(kOrderBuckets) k_order_scan(unsigned* hist) {
@@ -486,11 +504,25 @@ __global__ void __launch_bounds__(kOrderBuckets) k_order_scan(unsigned* hist) {
   hist[i] = t[i] - own;
 }
 
-__global__ void __launch_bounds__(256) k_order_place(const __grid_constant__ Plan P, const int li, const Queue Q,
-                                                     const float scale, unsigned* cursor, unsigned* order) {
-  const unsigned n = *Q.count;
-  for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
-    order[atomicAdd(cursor + order_bucket(P.el[li], Q.vz[j], scale), 1u)] = j;
+// Same ranges as k_order_count: the block reserves its entries of every
+// bucket with one global atomic per bucket, then places them with
+// shared-memory atomics.
+__global__ void __launch_bounds__(kOrderThreads) k_order_place(const __grid_constant__ Plan P, const int li,
+                                                               const Queue Q, const float scale, unsigned* cursor,
+                                                               unsigned* order) {
+  __shared__ unsigned h[kOrderBuckets];
+  for (int b = threadIdx.x; b < kOrderBuckets; b += blockDim.x) h[b] = 0;
+  __syncthreads();
+  unsigned lo, hi;
+  order_range(*Q.count, lo, hi);
+  for (unsigned j = lo + threadIdx.x; j < hi; j += blockDim.x)
+    atomicAdd(h + order_bucket(P.el[li], Q.vz[j], scale), 1u);
+  __syncthreads();
+  for (int b = threadIdx.x; b < kOrderBuckets; b += blockDim.x)
+    h[b] = h[b] ? atomicAdd(cursor + b, h[b]) : 0u;
+  __syncthreads();
+  for (unsigned j = lo + threadIdx.x; j < hi; j += blockDim.x)
+    order[atomicAdd(h + order_bucket(P.el[li], Q.vz[j], scale), 1u)] = j;
 }
 
 // ---------------------------------------------------------------------------
