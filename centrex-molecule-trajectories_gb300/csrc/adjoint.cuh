@@ -37,6 +37,8 @@
 // adjoint (they do not change the dynamics) and are summed in the forward
 // pass.
 #pragma once
+#include <type_traits>
+
 #include "kernels.cuh"
 
 namespace ctraj {
@@ -82,10 +84,21 @@ __device__ __forceinline__ float exp_(float a) { return expf(a); }
 __device__ __forceinline__ double exp_(double a) { return exp(a); }
 __device__ __forceinline__ float log1p_(float a) { return log1pf(a); }
 __device__ __forceinline__ double log1p_(double a) { return log1p(a); }
+__device__ __forceinline__ unsigned to_uint_rz(float a) { return __float2uint_rz(a); }
+__device__ __forceinline__ unsigned to_uint_rz(double a) { return __double2uint_rz(a); }
 
 // log sigma(z) and sigma(-z) = d log sigma(z) / dz
 template <class T>
 __device__ __forceinline__ void log_sigmoid(T z, T& ls, T& dls) {
+  if (std::is_same<T, float>::value && z >= T(12)) {
+    // e = exp(-z) <= 6.2e-6: log1p(e) = e (1 - e/2) and e / (1 + e) = e (1 - e)
+    // up to relative terms e^2 / 3 < 1.3e-11, far below float precision
+    // (most bore tests of a molecule inside the lens are this far from the edge)
+    const T e = exp_(-z);
+    ls = -mul_(e, fma_(T(-0.5), e, T(1)));
+    dls = mul_(e, add_(T(1), -e));
+    return;
+  }
   const T e = exp_(z >= T(0) ? -z : z);  // in (0, 1]
   const T l = log1p_(e);
   ls = z >= T(0) ? -l : add_(z, -l);
@@ -94,9 +107,21 @@ __device__ __forceinline__ void log_sigmoid(T z, T& ls, T& dls) {
 
 // The soft test of an edge of radius R at (x, y): log weight ls and its
 // derivative d with respect to R.
+// Radius of a soft edge test: FP64 the IEEE square root; FP32 r2 * rsqrt(r2),
+// within 2 ulp (the IEEE square root cost a tenth of the soft lens pass).
+template <class T>
+__device__ __forceinline__ T soft_radius(T x, T y) {
+  const T r2 = fma_(y, y, mul_(x, x));
+  if constexpr (std::is_same<T, float>::value) {
+    return r2 > 0.0f ? mul_(r2, rsqrtf(r2)) : 0.0f;
+  } else {
+    return sqrt_(r2);
+  }
+}
+
 template <class T>
 __device__ __forceinline__ void soft_test(T x, T y, T R, T inv_w, T& ls, T& d) {
-  const T r = sqrt_(fma_(y, y, mul_(x, x)));
+  const T r = soft_radius(x, y);
   T dls;
   log_sigmoid(mul_(add_(R, -r), inv_w), ls, dls);
   d = mul_(dls, inv_w);
@@ -227,7 +252,7 @@ struct SoftMol {
   // soft edge test at radius R: returns sigma(-z) / w, the derivative of the
   // log weight with respect to R
   __device__ T check(T R, T inv_w) {
-    const T r = sqrt_(fma_(y, y, mul_(x, x)));
+    const T r = soft_radius(x, y);
     T ls, dls;
     log_sigmoid(mul_(add_(R, -r), inv_w), ls, dls);
     lw = add_(lw, ls);
@@ -269,19 +294,22 @@ struct SoftTape {
 // conversion per use would run on the FP64 pipe inside the step loop).
 template <class T>
 struct SoftK {
-  T beta, neg_s0, kappa, g, kb2, k1, nint;
+  T beta, neg_s0, kappa, g, kb2, k1;
   int n_int;
   __device__ explicit SoftK(const SoftPlan& S)
       : beta(T(S.beta)), neg_s0(T(-S.s0)), kappa(T(S.kappa)), g(T(S.g)), kb2(T(2.0 * S.kappa * S.beta)),
-        k1(T(S.kappa1)), nint(T(S.n_int)), n_int(S.n_int) {}
+        k1(T(S.kappa1)), n_int(S.n_int) {}
 };
 
 template <class T, bool kStaged>
 __device__ __forceinline__ void soft_poly(const SoftK<T>& C, const Coef4<T>* tab, T px, T py, T& P, T& Pp) {
   const T r2 = fma_(py, py, mul_(px, px));
   const T s = fma_(C.beta, r2, C.neg_s0);
-  // interval index, clamped (the end pieces extrapolate); NaN gives the last
-  const int i = s >= T(0) ? (s < C.nint ? int(s) : C.n_int - 1) : (s < T(0) ? 0 : C.n_int - 1);
+  // interval index, clamped (the end pieces extrapolate): truncation to
+  // unsigned sends s < 0 and NaN to 0, one conversion and a min on the
+  // step-to-step dependency chain (a compare-and-select clamp doubled the
+  // step's latency)
+  const unsigned i = min(to_uint_rz(s), unsigned(C.n_int - 1));
   const T u = add_(s, -T(i));
   const Coef4<T> q = tab[i];
   P = fma_(u, fma_(u, q.q2, q.q1), q.q0);
@@ -297,6 +325,52 @@ __device__ __forceinline__ void soft_step(const SoftK<T>& C, const Coef4<T>* tab
   const T g = C.g, kappa = C.kappa;
   T P, Pp;
   if (te) { te->x = x; te->y = y; te->vx = vx; te->vy = vy; }
+  if constexpr (std::is_same<T, float>::value) {
+    // FP32: the (x, y) pairs on the packed FP32 instructions (FFMA2 / FADD2 /
+    // FMUL2), per component the same rounding as the scalar path below
+    const float2 p = make_float2(x, y), v = make_float2(vx, vy);
+    const float2 Hdt = make_float2(hdt, hdt), Dt = make_float2(dt, dt), G0 = make_float2(0.0f, -g);
+    auto neg = [](float2 a) { return make_float2(-a.x, -a.y); };
+    soft_poly<T, kStaged>(C, tab, x, y, P, Pp);
+    if (te) { te->P[0] = P; te->Pp[0] = Pp; }
+    float w = mul_(kappa, P);
+    const float2 l1 = __ffma2_rn(make_float2(w, w), p, G0);
+    const float2 k2 = __ffma2_rn(Hdt, l1, v);
+    const float2 p2 = __ffma2_rn(make_float2(c2, c2), v, p);
+    soft_poly<T, kStaged>(C, tab, p2.x, p2.y, P, Pp);
+    if (te) { te->P[1] = P; te->Pp[1] = Pp; }
+    w = mul_(kappa, P);
+    const float2 l2 = __ffma2_rn(make_float2(w, w), p2, G0);
+    const float2 k3 = __ffma2_rn(Hdt, l2, v);
+    const float2 p3 = __ffma2_rn(Hdt, k2, p);
+    soft_poly<T, kStaged>(C, tab, p3.x, p3.y, P, Pp);
+    if (te) { te->P[2] = P; te->Pp[2] = Pp; }
+    w = mul_(kappa, P);
+    const float2 l3 = __ffma2_rn(make_float2(w, w), p3, G0);
+    const float2 p4 = __ffma2_rn(Dt, k3, p);
+    soft_poly<T, kStaged>(C, tab, p4.x, p4.y, P, Pp);
+    if (te) { te->P[3] = P; te->Pp[3] = Pp; }
+    w = mul_(kappa, P);
+    const float2 l4 = __ffma2_rn(make_float2(w, w), p4, G0);
+    const float2 sum = __fadd2_rn(__fadd2_rn(l1, l2), l3);
+    const float2 dx = __ffma2_rn(make_float2(dt26, dt26), sum, __fmul2_rn(Dt, v));
+    const float2 dv = __fmul2_rn(make_float2(dt6, dt6),
+                                 __ffma2_rn(make_float2(2.0f, 2.0f), __fadd2_rn(l2, l3), __fadd2_rn(l1, l4)));
+    float2 cp = make_float2(cx, cy), cv = make_float2(cvx, cvy);
+    const float2 d1 = __fadd2_rn(dx, cp), t1 = __fadd2_rn(p, d1);
+    cp = __fadd2_rn(d1, neg(__fadd2_rn(t1, neg(p))));
+    const float2 d2 = __fadd2_rn(dv, cv), t2 = __fadd2_rn(v, d2);
+    cv = __fadd2_rn(d2, neg(__fadd2_rn(t2, neg(v))));
+    x = t1.x;
+    y = t1.y;
+    vx = t2.x;
+    vy = t2.y;
+    cx = cp.x;
+    cy = cp.y;
+    cvx = cv.x;
+    cvy = cv.y;
+    return;
+  }
   soft_poly<T, kStaged>(C, tab, x, y, P, Pp);
   if (te) { te->P[0] = P; te->Pp[0] = Pp; }
   T w = mul_(kappa, P);
@@ -409,7 +483,7 @@ __device__ __forceinline__ void soft_step_adjoint(const SoftK<T>& C, const SoftT
 // d lw / d(x, y) of the soft bore test at (x, y): -sigma(-z)/w * (x, y)/r
 template <class T>
 __device__ __forceinline__ void check_adjoint(T R, T inv_w, T x, T y, T& lx, T& ly) {
-  const T r = sqrt_(fma_(y, y, mul_(x, x)));
+  const T r = soft_radius(x, y);
   T ls, dls;
   log_sigmoid(mul_(add_(R, -r), inv_w), ls, dls);
   if (r > T(0)) {
