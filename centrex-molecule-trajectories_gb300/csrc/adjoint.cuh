@@ -132,6 +132,7 @@ struct SoftPlan {
   int64_t n;                        // molecules of the whole run
   int64_t first, count;             // the molecules of this launch: first .. first + count - 1
   uint64_t seed, offset;
+  PhiloxKey key;                    // round keys of seed
   int ic_mode;
   int n_planes;                     // ballistic planes up to and including the lens entrance
   const double* normals;            // (5, n) unit normals n_vx, n_vy, n_vz, n_x, n_y (host mode)
@@ -210,7 +211,7 @@ struct SoftMol {
   __device__ void init(const SoftPlan& S, int64_t i) {
     T n0, n1, n2, n3, n4;
     if (S.ic_mode == CTRAJ_IC_DEVICE_DRAW) {
-      const Words8 w = molecule_words(S.offset + uint64_t(i), S.seed);
+      const Words8 w = molecule_words(S.offset + uint64_t(i), S.key);
       T n5;
       box_muller(w.w[0], w.w[1], n0, n1);
       box_muller(w.w[2], w.w[3], n2, n3);

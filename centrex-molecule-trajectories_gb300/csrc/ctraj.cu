@@ -575,6 +575,7 @@ int prepare(ctraj_context* c, const ctraj_run_args* a, Plan& P, RunDev& R) {
   R.n = a->n;
   R.rec_lens = -1;
   R.seed = a->seed;
+  R.key = philox_key(a->seed);
   R.offset = a->offset;
   R.ic_mode = a->ic_mode;
   R.xd = a->xdist;
@@ -1409,6 +1410,7 @@ int soft_plan(const ctraj_context* c, const ctraj_soft_args* a, const double* pr
   S.n_planes = np;
   S.n = a->n;
   S.seed = a->seed;
+  S.key = philox_key(a->seed);
   S.offset = a->offset;
   S.ic_mode = a->ic_mode;
   S.z_ic = a->xdist.p[2];
@@ -1886,6 +1888,7 @@ extern "C" int ctraj_run_noalloc(const ctraj_element* el, int32_t n_el, int32_t 
   std::memset(&R, 0, sizeof R);
   R.n = a->n;
   R.seed = a->seed;
+  R.key = philox_key(a->seed);
   R.offset = a->offset;
   R.ic_mode = a->ic_mode;
   R.xd = a->xdist;

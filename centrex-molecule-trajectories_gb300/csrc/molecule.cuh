@@ -345,7 +345,7 @@ struct Mol64 {
     margin = INFINITY;
     rows = 0;
     if (R.ic_mode == CTRAJ_IC_DEVICE_DRAW) {
-      const Words8 w = molecule_words(R.offset + uint64_t(i), R.seed);
+      const Words8 w = molecule_words(R.offset + uint64_t(i), R.key);
       double n0, n1, n2, n3, n4, n5;
       box_muller(w.w[0], w.w[1], n0, n1);
       box_muller(w.w[2], w.w[3], n2, n3);
@@ -563,7 +563,7 @@ struct Mol32 {
     rows = 0;
     double z_ic;
     if (R.ic_mode == CTRAJ_IC_DEVICE_DRAW) {
-      const Words8 w = molecule_words(R.offset + uint64_t(i), R.seed);
+      const Words8 w = molecule_words(R.offset + uint64_t(i), R.key);
       float n0, n1, n2, n3, n4, n5;
       box_muller(w.w[0], w.w[1], n0, n1);
       box_muller(w.w[2], w.w[3], n2, n3);

@@ -35,15 +35,29 @@ __host__ __device__ inline void philox_round(uint32_t& c0, uint32_t& c1, uint32_
   c3 = lo0;
 }
 
-__host__ __device__ inline Philox4 philox4x32_10(uint64_t ctr, uint32_t call, uint64_t key) {
-  uint32_t c0 = uint32_t(ctr), c1 = uint32_t(ctr >> 32), c2 = call, c3 = 0u;
-  uint32_t k0 = uint32_t(key), k1 = uint32_t(key >> 32);
-#pragma unroll
+// The ten round keys of a seed (the key plus r Weyl increments), computed on
+// the host once per launch and read from the kernel parameters, so that no
+// thread repeats the key schedule.
+struct PhiloxKey {
+  uint32_t k[20];  // round r: k[2r], k[2r + 1]
+};
+
+inline PhiloxKey philox_key(uint64_t seed) {
+  PhiloxKey K;
+  uint32_t k0 = uint32_t(seed), k1 = uint32_t(seed >> 32);
   for (int r = 0; r < 10; ++r) {
-    philox_round(c0, c1, c2, c3, k0, k1);
+    K.k[2 * r] = k0;
+    K.k[2 * r + 1] = k1;
     k0 += 0x9E3779B9u;
     k1 += 0xBB67AE85u;
   }
+  return K;
+}
+
+__host__ __device__ inline Philox4 philox4x32_10(uint64_t ctr, uint32_t call, const PhiloxKey& K) {
+  uint32_t c0 = uint32_t(ctr), c1 = uint32_t(ctr >> 32), c2 = call, c3 = 0u;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) philox_round(c0, c1, c2, c3, K.k[2 * r], K.k[2 * r + 1]);
   return Philox4{{c0, c1, c2, c3}};
 }
 
@@ -59,9 +73,17 @@ __device__ __forceinline__ double u01d(uint32_t w) {
 // ln U for U = (w + 1/2) 2^-32.  Above one half, U is close to 1 and a float
 // holds it only to 2^-25 absolute, which would make the Box-Muller radius
 // sqrt(-2 ln U) inaccurate near zero; there ln U = log1p(-V) with
-// V = 1 - U = (~w + 1/2) 2^-32 formed exactly from the integer.
+// V = 1 - U = (~w + 1/2) 2^-32 formed exactly from the integer.  Below one
+// half, U = 2^e m with m in [1, 2) and ln U = e ln 2 + log1p(m - 1) (m - 1
+// exact), so both halves take the same single log1pf and no lane diverges.
 __device__ __forceinline__ float log_u01f(uint32_t w) {
-  return (w < 0x80000000u) ? logf(u01f(w)) : log1pf(-u01f(~w));
+  const bool low = w < 0x80000000u;
+  const float u = u01f(low ? w : ~w);  // U, or V = 1 - U
+  const uint32_t bits = __float_as_uint(u);
+  const float e = float(int(bits >> 23) - 127);
+  const float m1 = __fadd_rn(__uint_as_float((bits & 0x007fffffu) | 0x3f800000u), -1.0f);
+  const float l = log1pf(low ? m1 : -u);
+  return low ? __fmaf_rn(e, 0.693147180559945309f, l) : l;
 }
 
 __device__ __forceinline__ double log_u01d(uint32_t w) {
@@ -93,9 +115,9 @@ struct Words8 {
   uint32_t w[8];
 };
 
-__device__ __forceinline__ Words8 molecule_words(uint64_t id, uint64_t seed) {
-  const Philox4 a = philox4x32_10(id, 0u, seed);
-  const Philox4 b = philox4x32_10(id, 1u, seed);
+__device__ __forceinline__ Words8 molecule_words(uint64_t id, const PhiloxKey& K) {
+  const Philox4 a = philox4x32_10(id, 0u, K);
+  const Philox4 b = philox4x32_10(id, 1u, K);
   return Words8{{a.v[0], a.v[1], a.v[2], a.v[3], b.v[0], b.v[1], b.v[2], b.v[3]}};
 }
 

@@ -9,6 +9,7 @@
 #include <cstdint>
 
 #include "ctraj.h"
+#include "philox.cuh"
 
 namespace ctraj {
 
@@ -97,6 +98,7 @@ __host__ __device__ inline LensArgs lens_args(const Plan& P, int li, bool staged
 struct RunDev {
   int64_t n;
   uint64_t seed;
+  PhiloxKey key;  // round keys of seed
   uint64_t offset;
   int ic_mode;
   int pad;
