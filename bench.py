@@ -607,6 +607,20 @@ def main():
                 "lens_ms_per_launch": lens_ms / args.steps, "front_ms_per_launch": front_ms / args.steps,
                 "traffic": LENS_DRAM_BYTES_PER_RUN, "traffic_unit": "bytes per lens pass (ncu, the k_lens_persist launch)",
                 "step_probe": probe}
+    # the lens pass is bound by its critical path, not by the FP32 pipe: the
+    # molecule with the most RK4 steps cannot finish before that many steps
+    # of one-warp latency (the step probe) at the clock seen in the timed region
+    max_steps = max(r.extra.get("max_lens_steps", 0) for r in results)
+    cyc = probe.get("one_warp_cycles_per_step") if probe else None
+    mhz = clocks.get("sm_mhz") if clocks else None
+    if max_steps and cyc and mhz:
+        floor_ms = max_steps * cyc / (mhz * 1e3)
+        roofline["critical_path"] = {
+            "max_lens_steps": int(max_steps), "one_warp_cycles_per_step": cyc, "sm_mhz": mhz,
+            "floor_ms": floor_ms, "lens_ms_per_launch": lens_ms / args.steps,
+            "frac": floor_ms / (lens_ms / args.steps),
+            "note": "latency floor of the slowest molecule (max_lens_steps x one-warp step latency); "
+                    "frac = floor / measured lens pass"}
     cpu = None if args.no_cpu or world > 1 else cpu_baseline(int(args.cpu_sample))
     r0 = results[-1]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

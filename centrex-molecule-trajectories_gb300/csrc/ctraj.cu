@@ -112,6 +112,7 @@ struct ctraj_context {
   int front_waves = 4;          // k_front grid in units of resident CTAs
   int lens_mode = CTRAJ_LENS_PERSISTENT;  // FP32 lens pass
   int lens_interval = 256;      // persistent mode: steps between CTA compactions
+  unsigned run_max_steps = 0;   // largest lens queue step bound of the last run
   bool timing = false;
   // before front, after front, before the first lens chunk, after the last one
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -426,6 +427,7 @@ template <bool k64, bool kOut, bool kRing = false>
 int launch_all(ctraj_context* c, const Plan& P, const RunDev& R0, Queue* q, int* launches) {
   using MolT = typename std::conditional<k64, Mol64<false>, Mol32<kOut, false>>::type;
   RunDev R = R0;  // ring recording fills in the staging buffers once the lens count is known
+  c->run_max_steps = 0;
   unsigned ring_slots = 0;
   const int64_t n = R.n;
   cudaStream_t s = c->stream;
@@ -448,6 +450,7 @@ int launch_all(ctraj_context* c, const Plan& P, const RunDev& R0, Queue* q, int*
     CT_CUDA(cudaStreamSynchronize(s));
     const unsigned count = c->host_max[0], max_steps = c->host_max[1];
     if (count == 0) break;  // no molecule reaches this lens, hence none reaches a later one
+    c->run_max_steps = std::max(c->run_max_steps, max_steps);
     if (c->timing && !started) CT_CUDA(cudaEventRecord(c->ev[2], s));
     started = true;
     CT_CUDA(cudaMemsetAsync(q[nxt].count, 0, kCtlWords * sizeof(unsigned), s));
@@ -876,6 +879,7 @@ static int run_impl(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* 
     stats->molecules = n;
     stats->molecule_steps = int64_t(hs[kStatSteps]);
     stats->lens_steps = int64_t(hs[kStatLensSteps]);
+    stats->max_lens_steps = int32_t(c->run_max_steps);
     stats->edge_band = (a->precision == 64 || out) ? int64_t(hs[kStatEdgeBand]) : -1;
     stats->table_range = int64_t(hs[kStatTableRange]);
     stats->bad_steps = int64_t(hs[kStatBadSteps]);

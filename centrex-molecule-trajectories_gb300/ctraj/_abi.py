@@ -133,6 +133,8 @@ class RunStats(ctypes.Structure):
         ("timed", ctypes.c_int32),
         ("front_ms", ctypes.c_float),
         ("lens_ms", ctypes.c_float),
+        ("max_lens_steps", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
 

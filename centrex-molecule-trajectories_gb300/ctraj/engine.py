@@ -218,6 +218,7 @@ class Engine:
             status = self.lib.ctraj_run_ring(self.ctx, ctypes.byref(a), ctypes.byref(rs), ctypes.byref(st))
         del keep
         _abi.check(status, self.lib)
+        res_extra["max_lens_steps"] = int(st.max_lens_steps)
         if st.timed:
             res_extra.update(front_ms=float(st.front_ms), lens_ms=float(st.lens_ms))
         return RunResult(counts=counts, labels=list(cb.labels), molecules=st.molecules,

@@ -212,6 +212,11 @@ typedef struct ctraj_run_stats {
   int32_t timed;            /* 1 when the *_ms fields below were measured     */
   float front_ms;           /* CUDA-event time of the ballistic front kernel  */
   float lens_ms;            /* CUDA-event time of all lens kernels            */
+  int32_t max_lens_steps;   /* ctraj_run: upper bound on the RK4 steps of the
+                               molecule with the most steps in a lens
+                               (rint(L/dz) + 2), the length of the lens pass's
+                               critical path; 0 from the other entry points   */
+  int32_t reserved;
 } ctraj_run_stats;
 
 /* ---- context -------------------------------------------------------------- */
