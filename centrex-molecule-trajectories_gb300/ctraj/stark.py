@@ -13,7 +13,14 @@ a(r) = -dW/dr / m, then a linear ``interp1d``.  This module supplies:
   reference accepts as ``ElectrostaticLens.a_interp`` and that the compiler
   uploads as a piecewise-cubic table;
 * :func:`reference_radial_table` -- the reference's own interp1d
-  construction (:194-209) fed from any W(E) instead of ``stark_potential``.
+  construction (:194-209) fed from any W(E) instead of ``stark_potential``;
+* :func:`stark_potential` -- the reference's Stark curve of a state
+  (stark_potential.py:9-88) for any Hamiltonian of the form H0 + E_z HE +
+  B_z HB (:class:`LinearHamiltonian`), with the eigensolves batched on the
+  GPU, and :func:`lens_table_from_hamiltonian`, the lens table the reference
+  builds from it when ``a_interp`` is None.  centrex_TlF, which supplies the
+  TlF matrices in the reference, is not available here: the caller brings
+  the matrices.
 """
 from __future__ import annotations
 
@@ -28,7 +35,8 @@ DEBYE = 1e-21 / LIGHT  # C m
 TLF_MASS = (204.38 + 19.00) * 1.67e-27  # kg, electrostatic_lens.py:44-46
 
 __all__ = ["DEBYE", "TLF_MASS", "TwoLevelStark", "StarkForce", "hexapole_force",
-           "reference_radial_table", "field_coefficient"]
+           "reference_radial_table", "field_coefficient", "LinearHamiltonian", "reorder_evecs",
+           "stark_potential", "lens_table_from_hamiltonian"]
 
 
 @dataclass(frozen=True)
@@ -140,3 +148,99 @@ def reference_radial_table(W, V: float, d: float, mass: float = TLF_MASS,
     V_stark = W(E_values)
     a_values = -np.gradient(V_stark, dr) / mass
     return interp1d(r_values, a_values)
+
+
+# ---------------------------------------------------------------------------
+# Stark curves from a Hamiltonian (stark_potential.py:9-88)
+# ---------------------------------------------------------------------------
+
+
+@dataclass
+class LinearHamiltonian:
+    """H(E, B) = H0 + E_z HE + B_z HB in rad/s (E in V/cm, B in T): the form of
+    the TlF ground-state Hamiltonian the reference diagonalises
+    (stark_potential.py:26-27; centrex_TlF's function is linear in the field
+    components).  Any basis and size; the matrices are Hermitian."""
+
+    H0: np.ndarray
+    HE: np.ndarray
+    HB: np.ndarray
+
+    def __post_init__(self):
+        self.H0, self.HE, self.HB = (np.asarray(a, dtype=np.complex128) for a in (self.H0, self.HE, self.HB))
+        n = self.H0.shape[0]
+        if any(a.shape != (n, n) for a in (self.H0, self.HE, self.HB)):
+            raise ValueError("H0, HE and HB must be square matrices of one size")
+
+    def __call__(self, E, B):
+        return self.H0 + E[2] * self.HE + B[2] * self.HB
+
+
+def reorder_evecs(V_in, E_in, V_ref):
+    """stark_potential.py:78-88: order eigenpairs so that index k follows the
+    reference vector k (largest overlap), E_out, V_out."""
+    overlap = np.abs(np.conj(V_in.T) @ V_ref)
+    index = np.argsort(np.argmax(overlap, axis=1))
+    return E_in[index], V_in[:, index]
+
+
+def stark_potential(state, Ezs, hamiltonian: LinearHamiltonian, basis=None, B: float = 1e-4,
+                    E_start: float = 100.0) -> np.ndarray:
+    """Stark energy (J) of ``state`` at the field magnitudes ``Ezs`` (V/cm),
+    stark_potential.py:9-67, on the GPU.
+
+    All the Hamiltonians H(Ez z^, B z^) are diagonalised in one batched
+    Hermitian eigensolve (cuSOLVER through torch.linalg.eigh, complex128), the
+    overlaps |V_i^H V_(i-1)| of consecutive eigenbases in one batched product
+    on the device.  The reference's adiabatic reordering (each step's
+    eigenpairs sorted by the reference vector they overlap most, the reference
+    being the previous step's reordered basis, reorder_evecs) is then a chain
+    of index permutations composed on the host: with perm the previous step's
+    order, the largest overlap of new vector k among the reordered columns is
+    column inv(perm)[argmax_c |V_i^H V_(i-1)|[k, c]].  The state is the
+    eigenvector at E = E_start V/cm (the reference's 100 V/cm and B = 1e-4 T)
+    with the largest |<state|v>| (centrex_TlF's find_closest_vector_idx).
+
+    ``state``: a state vector in the Hamiltonian's basis, or an object with
+    ``state_vector(basis)`` (centrex_TlF's State).  Needs a CUDA GPU.
+    """
+    import torch
+    from scipy.constants import hbar
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("stark_potential runs its eigensolves on a CUDA GPU; none is available")
+    H = hamiltonian
+    vec = np.asarray(state.state_vector(basis) if hasattr(state, "state_vector") else state, np.complex128)
+    Ezs = np.asarray(Ezs, dtype=np.float64)
+    n = H.H0.shape[0]
+    if vec.shape != (n,):
+        raise ValueError(f"state vector of length {vec.shape} for a {n}-state Hamiltonian")
+    dev = torch.device("cuda")
+    H0, HE, HB = (torch.as_tensor(a, device=dev) for a in (H.H0, H.HE, H.HB))
+    Ez = torch.as_tensor(Ezs, device=dev)
+    # H0 + E_z HE + B_z HB, in the reference's order of operations
+    Hs = (H0 + Ez[:, None, None] * HE) + B * HB
+    evals, evecs = torch.linalg.eigh(Hs)
+    _, V0 = torch.linalg.eigh((H0 + E_start * HE) + B * HB)
+    prev = torch.cat([V0[None], evecs[:-1]]) if Ezs.size else V0[None]
+    best = (evecs.mH @ prev).abs().argmax(dim=2).cpu().numpy()
+    E = evals.cpu().numpy()
+    out = np.empty_like(E)
+    inv = np.arange(n)
+    for i in range(Ezs.size):
+        order = np.argsort(inv[best[i]])
+        out[i] = E[i][order]
+        inv = np.empty(n, dtype=np.int64)
+        inv[order] = np.arange(n)
+    state_i = int(np.argmax(np.abs(np.conj(vec) @ V0.cpu().numpy())))
+    return out[:, state_i] * hbar
+
+
+def lens_table_from_hamiltonian(lens, state, hamiltonian: LinearHamiltonian, basis=None) -> interp1d:
+    """The lens's a(r) table as ``ElectrostaticLens.lens_acceleration`` builds it
+    when ``a_interp`` is None (electrostatic_lens.py:191-209): r grid, |E| =
+    2 V r / (d/2)^2, the Stark curve of ``state`` (``stark_potential``, E in
+    V/cm), a = -np.gradient(V_stark, dr) / mass, linear interp1d.  Assign the
+    result to ``lens.a_interp``."""
+    return reference_radial_table(lambda E: stark_potential(state, E / 100, hamiltonian, basis), V=lens.V,
+                                  d=lens.d, mass=lens.mass)
