@@ -292,7 +292,7 @@ def bench_sweep(eng, stream, flush, steps: int, warmup: int, device_name: str):
 
     from ctraj.distributions import device_spec
     from ctraj.sweep import config_beamlines, loop_sweep, run_sweep, sweep_beamline
-    from ctraj.tuning import autotune, candidates
+    from ctraj.tuning import autotune
     from ctraj.workloads import lens_beamline, source, sweep_configs
 
     cfg = sweep_configs()
@@ -311,8 +311,7 @@ def bench_sweep(eng, stream, flush, steps: int, warmup: int, device_name: str):
 
     for k in range(warmup):
         sweep(k)
-    tuned = autotune(eng, cb, cfg.total, {}, device_name=device_name, measure=measure, key_extra="|sweep",
-                     cands=candidates(chunked_only=True))
+    tuned = autotune(eng, cb, cfg.total, {}, device_name=device_name, measure=measure, key_extra="|sweep")
     for k in range(warmup):
         sweep(k)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

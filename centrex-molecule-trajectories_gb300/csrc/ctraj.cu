@@ -46,11 +46,15 @@ int fail(int code, const char* fmt, ...) {
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
-  int ensure(size_t want) {
+  // headroom_pct: when growing, allocate that much more, for buffers sized by
+  // a count that varies from run to run (a cudaFree/cudaMalloc in a run
+  // synchronizes the device)
+  int ensure(size_t want, size_t headroom_pct = 0) {
     if (want <= bytes) return CTRAJ_OK;
     if (p) cudaFree(p);
     p = nullptr;
     bytes = 0;
+    want += want / 100 * headroom_pct;
     cudaError_t e = cudaMalloc(&p, want);
     if (e != cudaSuccess) {
       p = nullptr;
@@ -106,6 +110,7 @@ struct ctraj_context {
   DevBuf rec_stage;             // ring recording: staged records of the recorded lens
   DevBuf ring_ent;              // ring recording: molecules stopped by the entrance test
   DevBuf lens_order;            // persistent lens pass: bucket counts | entrant order
+  DevBuf sweep_order;           // persistent sweep: per table bucket counts | entrant order
   int chunk = 64;               // RK4 steps of the first lens chunk (compaction interval)
   int chunk_growth = 200;       // percent: each chunk's length relative to the previous
   int chunk_max = 1024;         // longest chunk
@@ -401,16 +406,16 @@ int launch_persistent(ctraj_context* c, const Plan& P, const RunDev& R, int i, c
   }
   const size_t smem = (staged ? size_t(P.lf[i].n_int) * sizeof(float4) : 0) + kPersistThreads * sizeof(SwapSlot);
   CT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-  int st = c->lens_order.ensure((size_t(kOrderBuckets) + count) * sizeof(unsigned));
+  int st = c->lens_order.ensure((size_t(kOrderBuckets) + count) * sizeof(unsigned), 25);
   if (st) return st;
   unsigned* hist = c->lens_order.as<unsigned>();
   unsigned* order = hist + kOrderBuckets;
-  const float scale = float(kOrderBuckets - 1) / (float(max_steps) + 1.0f);
+  (void)max_steps;  // the ordering kernels read it from the queue
   const int grid = c->sm_count;
   CT_CUDA(cudaMemsetAsync(hist, 0, kOrderBuckets * sizeof(unsigned), s));
-  k_order_count<<<grid, kOrderThreads, 0, s>>>(P, i, Qin, scale, hist);
+  k_order_count<<<grid, kOrderThreads, 0, s>>>(P, i, Qin, hist);
   k_order_scan<<<1, kOrderBuckets, 0, s>>>(hist);
-  k_order_place<<<grid, kOrderThreads, 0, s>>>(P, i, Qin, scale, hist, order);
+  k_order_place<<<grid, kOrderThreads, 0, s>>>(P, i, Qin, hist, order);
   k<<<c->sm_count, kPersistThreads, smem, s>>>(P, R, i, Qin, Qnext, lens_args(P, i, true), order,
                                                 c->lens_interval);
   CT_CUDA(cudaGetLastError());
@@ -462,7 +467,7 @@ int launch_all(ctraj_context* c, const Plan& P, const RunDev& R0, Queue* q, int*
       R.rec_max = int(max_steps / unsigned(R.rec_stride)) + 3;
       const size_t recb = align256(size_t(count) * size_t(R.rec_max) * sizeof(float4));
       const size_t sb = align256(size_t(count) * 4);
-      int st = c->rec_stage.ensure(recb + 5 * sb + 2 * align256(size_t(count) * 8));
+      int st = c->rec_stage.ensure(recb + 5 * sb + 2 * align256(size_t(count) * 8), 25);
       if (st) return st;
       char* b = c->rec_stage.as<char>();
       R.rec = reinterpret_cast<float4*>(b);
@@ -656,6 +661,7 @@ int ctraj_destroy(ctraj_context* c) {
   c->rec_stage.release();
   c->ring_ent.release();
   c->lens_order.release();
+  c->sweep_order.release();
   if (c->sweep_exec) cudaGraphExecDestroy(c->sweep_exec);
   for (int t = 0; t < CTRAJ_MAX_TABLES; ++t) {
     if (c->side[t]) cudaStreamSynchronize(c->side[t]);
@@ -1063,7 +1069,30 @@ struct SweepLaunch {
   std::vector<int> chunks;
   unsigned long long* result = nullptr;  // device: per-configuration counts | totals | stats
   size_t result_bytes = 0;
+  bool persistent = false;               // one k_sweep_persist launch instead of the chunks
+  unsigned* order[CTRAJ_MAX_TABLES] = {};  // persistent: bucket counts then entrant order, per table
 };
+
+// The persistent sweep lens kernel of a force law; staged when every table fits.
+using SweepPersistKernel = void (*)(const Plan, const RunDev, const int, const SweepQueues, const int,
+                                    const SweepTabs, const LensArgs, const int);
+SweepPersistKernel sweep_persist_kernel(int force, bool staged) {
+  if (staged)
+    return force == kForceStark1 ? k_sweep_persist<kForceStark1, true> : k_sweep_persist<kForceStark2, true>;
+  return force == kForceStark1 ? k_sweep_persist<kForceStark1, false> : k_sweep_persist<kForceStark2, false>;
+}
+
+bool sweep_staged(const SweepLaunch& W) {
+  for (int t = 0; t < W.n_tab; ++t)
+    if (W.la[t].n_smem == 0) return false;
+  return true;
+}
+
+size_t sweep_persist_smem(const SweepLaunch& W) {
+  int max_int = 0;
+  for (int t = 0; t < W.n_tab; ++t) max_int = std::max(max_int, W.la[t].n_int);
+  return (sweep_staged(W) ? size_t(max_int) * sizeof(float4) : 0) + kPersistThreads * sizeof(SwapSlot);
+}
 
 // The whole sweep on c->stream (forking to one side stream per table).  Every
 // call ends with the result copied to c->sweep_host; the caller synchronizes.
@@ -1089,6 +1118,33 @@ int sweep_enqueue(ctraj_context* c, const Plan& P, const RunDev& R, const SweepL
     ++launches;
   }
   if (c->timing) CT_CUDA(record(c->ev[1]));
+  if (W.persistent && R.n > 0) {
+    SweepQueues Qs{};
+    SweepTabs T{};
+    for (int t = 0; t < W.n_tab; ++t) {
+      Qs.q[t] = W.qa[t];
+      unsigned* hist = W.order[t];
+      CT_CUDA(cudaMemsetAsync(hist, 0, kOrderBuckets * sizeof(unsigned), s));
+      k_order_count<<<c->sm_count, kOrderThreads, 0, s>>>(P, W.lens, W.qa[t], hist);
+      k_order_scan<<<1, kOrderBuckets, 0, s>>>(hist);
+      k_order_place<<<c->sm_count, kOrderThreads, 0, s>>>(P, W.lens, W.qa[t], hist, hist + kOrderBuckets);
+      CT_CUDA(cudaGetLastError());
+      launches += 3;
+      T.q[t] = W.la[t].q;
+      T.order[t] = hist + kOrderBuckets;
+      T.s0[t] = W.la[t].s0;
+      T.n_int[t] = W.la[t].n_int;
+    }
+    sweep_persist_kernel(P.lf[W.lens].force, sweep_staged(W))<<<c->sm_count, kPersistThreads,
+                                                                  sweep_persist_smem(W), s>>>(
+        P, R, W.lens, Qs, W.n_tab, T, W.la[0], c->lens_interval);
+    CT_CUDA(cudaGetLastError());
+    ++launches;
+    if (c->timing) CT_CUDA(record(c->ev[3]));
+    CT_CUDA(cudaMemcpyAsync(c->sweep_host, W.result, W.result_bytes, cudaMemcpyDeviceToHost, s));
+    c->sweep_launches = launches;
+    return CTRAJ_OK;
+  }
   CT_CUDA(cudaEventRecord(c->fork, s));
   for (int t = 0; t < W.n_tab && R.n > 0; ++t) {
     cudaStream_t st = c->side[t];
@@ -1203,6 +1259,17 @@ extern "C" int ctraj_run_sweep(ctraj_context* c, const ctraj_sweep* sw, const ct
   if ((st = ens(c->sweep_tables, tab_elems * sizeof(float4)))) return st;
   if ((st = ens(c->sweep_cfg, cfg_bytes + W.result_bytes))) return st;
   if ((st = ens(c->sweep_ctl, kSwCtlBytes))) return st;
+  W.persistent = c->lens_mode == CTRAJ_LENS_PERSISTENT;
+  if (W.persistent) {
+    size_t words_o = 0;
+    for (int t = 0; t < W.n_tab; ++t) words_o += kOrderBuckets + size_t(std::max<int64_t>(tab_n[t], 1));
+    if ((st = ens(c->sweep_order, words_o * sizeof(unsigned)))) return st;
+    size_t off = 0;
+    for (int t = 0; t < W.n_tab; ++t) {
+      W.order[t] = c->sweep_order.as<unsigned>() + off;
+      off += kOrderBuckets + size_t(std::max<int64_t>(tab_n[t], 1));
+    }
+  }
   for (int t = 0; t < W.n_tab; ++t) {
     const size_t cap = size_t(std::max<int64_t>(tab_n[t], 1));
     if ((st = ens(c->sweep_queue[2 * t], queue_bytes(cap, 32, true)))) return st;
@@ -1272,6 +1339,8 @@ extern "C" int ctraj_run_sweep(ctraj_context* c, const ctraj_sweep* sw, const ct
   put(sw->alpha, size_t(n_cfg) * 8);
   put(sw->table, size_t(n_cfg) * 4);
   put(W.chunks.data(), W.chunks.size() * sizeof(int));
+  put(&c->lens_mode, sizeof c->lens_mode);
+  put(&c->lens_interval, sizeof c->lens_interval);
   const bool same = key == c->sweep_key;
   cudaStream_t s = c->stream;
   if (!same) {
@@ -1318,6 +1387,9 @@ extern "C" int ctraj_run_sweep(ctraj_context* c, const ctraj_sweep* sw, const ct
     CT_CUDA(cudaFuncSetAttribute(sweep_lens_kernel(P.lf[lens].force, staged),
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   }
+  if (W.persistent)
+    CT_CUDA(cudaFuncSetAttribute(sweep_persist_kernel(P.lf[lens].force, sweep_staged(W)),
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(sweep_persist_smem(W))));
   c->timing = timing;
   if (sw->use_graph) {
     if (!c->sweep_exec) {
@@ -1521,8 +1593,8 @@ int soft_run(ctraj_context* c, const ctraj_soft_args* a, SoftPlan& S, int li, ct
       const size_t n_seg = (size_t(max_steps) + S.checkpoint - 1) / S.checkpoint + 1;
       const int max_seg = int(n_seg - 1);
       if (a->want_grad) {
-        if ((st = c->soft_ckpt.ensure(n_seg * 8 * cap * sizeof(T)))) return st;
-        if ((st = c->soft_seg.ensure(size_t(kSoftSegFields) * cap * size_t(max_seg) * sizeof(T)))) return st;
+        if ((st = c->soft_ckpt.ensure(n_seg * 8 * cap * sizeof(T), 25))) return st;
+        if ((st = c->soft_seg.ensure(size_t(kSoftSegFields) * cap * size_t(max_seg) * sizeof(T), 25))) return st;
       }
       grid = int((cap + kSoftThreads - 1) / kSoftThreads);
       kl<<<grid, kSoftThreads, tb, s>>>(S, Q, c->soft_table.as<Coef4<T>>(), c->soft_ckpt.as<T>(), cap, contrib,

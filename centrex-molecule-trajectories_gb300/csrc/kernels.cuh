@@ -457,11 +457,15 @@ __global__ void __launch_bounds__(kLensThreads, 2) k_lens_chunk(const __grid_con
 // result: molecules are independent and tallies are integer sums.
 constexpr int kOrderBuckets = 1024;
 
-// bucket 0 = most steps; scale = (kOrderBuckets - 1) / (largest step count + 1)
+// bucket 0 = most steps, for a queue whose largest step count is max_steps
 __device__ __forceinline__ int order_bucket(const ctraj_element& e, float vz, float scale) {
   const float dz = e.step_mode == CTRAJ_STEP_DT ? fabsf(vz) * float(e.p[2]) : float(e.p[1]);
   const float u = float(kOrderBuckets - 1) - (float(e.p[7]) / dz) * scale;  // NaN, -inf -> 0
   return u > 0.0f ? (u < float(kOrderBuckets - 1) ? int(u) : kOrderBuckets - 1) : 0;
+}
+
+__device__ __forceinline__ float order_scale(const Queue& Q) {
+  return float(kOrderBuckets - 1) / (float(*Q.max_steps) + 1.0f);
 }
 
 // Each block takes a contiguous range of the queue and counts it in shared
@@ -476,10 +480,11 @@ __device__ __forceinline__ void order_range(unsigned n, unsigned& lo, unsigned& 
 }
 
 __global__ void __launch_bounds__(kOrderThreads) k_order_count(const __grid_constant__ Plan P, const int li,
-                                                               const Queue Q, const float scale, unsigned* hist) {
+                                                               const Queue Q, unsigned* hist) {
   __shared__ unsigned h[kOrderBuckets];
   for (int b = threadIdx.x; b < kOrderBuckets; b += blockDim.x) h[b] = 0;
   __syncthreads();
+  const float scale = order_scale(Q);
   unsigned lo, hi;
   order_range(*Q.count, lo, hi);
   for (unsigned j = lo + threadIdx.x; j < hi; j += blockDim.x)
@@ -508,11 +513,11 @@ __global__ void __launch_bounds__(kOrderBuckets) k_order_scan(unsigned* hist) {
 // bucket with one global atomic per bucket, then places them with
 // shared-memory atomics.
 __global__ void __launch_bounds__(kOrderThreads) k_order_place(const __grid_constant__ Plan P, const int li,
-                                                               const Queue Q, const float scale, unsigned* cursor,
-                                                               unsigned* order) {
+                                                               const Queue Q, unsigned* cursor, unsigned* order) {
   __shared__ unsigned h[kOrderBuckets];
   for (int b = threadIdx.x; b < kOrderBuckets; b += blockDim.x) h[b] = 0;
   __syncthreads();
+  const float scale = order_scale(Q);
   unsigned lo, hi;
   order_range(*Q.count, lo, hi);
   for (unsigned j = lo + threadIdx.x; j < hi; j += blockDim.x)
@@ -526,8 +531,9 @@ __global__ void __launch_bounds__(kOrderThreads) k_order_place(const __grid_cons
 }
 
 // ---------------------------------------------------------------------------
-// k_lens_persist: one launch integrates a whole lens queue (FP32), one CTA
-// per SM, 16 warps.
+// Persistent lens pass: one launch integrates a whole lens queue (FP32), one
+// CTA per SM, 16 warps (k_lens_persist; k_sweep_persist runs it per Stark
+// table of a batched sweep).
 //
 // Phase A (molecules left in the queue): every kPersistService steps a warp
 // finalises its lanes whose molecule was lost or left the lens (exit snap,
@@ -548,36 +554,35 @@ struct SwapSlot {
   double dt, snap;
   int4 c;    // n_done, n_total, n0, idx
   unsigned flags, phase;
-  float margin, pad;
+  float margin;
+  int cfg;   // batched sweeps: configuration
 };
 
 constexpr int kPersistThreads = 512;
 constexpr int kPersistService = 16;
 
-template <class M, bool kOut, int F, bool kStaged>
-__global__ void __launch_bounds__(kPersistThreads, 1) k_lens_persist(const __grid_constant__ Plan P, const RunDev R,
-                                                                     const int li, const Queue Qin, const Queue Qnext,
-                                                                     const LensArgs L, const unsigned* order,
-                                                                     const int interval) {
-  extern __shared__ float4 s_dyn[];
-  __shared__ BlockTally S;
-  __shared__ unsigned s_wcount[kPersistThreads / 32];
-  const float4* s_tab = s_dyn;
-  SwapSlot* s_swap = reinterpret_cast<SwapSlot*>(s_dyn + (kStaged ? L.n_int : 0));
+struct PersistAcc {
+  unsigned long long steps = 0, lsteps = 0, band = 0, bad = 0, range = 0, rerr = 0;
+};
+
+// One CTA's share of a persistent pass over Qin.  The first static_entries
+// queue positions are dealt out interleaved across CTAs (entry (w * grid +
+// b) * 32 + lane to lane `lane` of warp w of CTA b); the rest are taken in
+// order by the lanes that become idle.  kSweep: molecules carry their
+// configuration (Queue::cfg), whose beta and kappa scale the unscaled table,
+// and tallies are also kept per configuration.  Every thread of the CTA
+// calls it; it returns with all of the CTA's molecules finalised.
+template <class M, bool kOut, int F, bool kStaged, bool kSweep>
+__device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, const int li, const Queue& Qin,
+                                             const Queue& Qnext, const LensArgs& L, const unsigned* order,
+                                             const int interval, const unsigned static_entries,
+                                             const float4* s_tab, SwapSlot* s_swap, unsigned* s_wcount,
+                                             BlockTally& S, PersistAcc& acc) {
   const unsigned n_in = *(volatile unsigned*)Qin.count;
-  if (n_in == 0) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned lanes_lt = (1u << lane) - 1u;
-  // each warp's first 32 entries are fixed and interleaved across CTAs, so
-  // that a short queue spreads over all SMs; the rest are taken in order
-  const unsigned static_entries = gridDim.x * kPersistThreads;
-  tally_init(S);
-  if (kStaged)
-    for (int k = threadIdx.x; k < L.n_int; k += blockDim.x) s_dyn[k] = __ldg(L.q + k);
-  __syncthreads();
   const ctraj_element& e = P.el[li];
   const bool classic = e.scheme == CTRAJ_RK4_CLASSIC;
-  unsigned long long steps = 0, lsteps = 0, band = 0, bad = 0, range = 0, rerr = 0;
 
   M m;
   LensStep st, nst;
@@ -585,7 +590,8 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_lens_persist(const __gri
   int phase = kIdle;
   unsigned flags = 0;
   float dt = 0.f, hdt = 0.f, c2 = 0.f, dt6 = 0.f, dt26 = 0.f;
-  int n0 = 0;
+  int n0 = 0, cfg = 0;
+  float beta = 0.f, kappa = 1.f;
   bool fresh = false;
   unsigned idx = 0;
 
@@ -595,11 +601,16 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_lens_persist(const __gri
     c2 = classic ? hdt : dt;
     dt6 = dt * (1.0f / 6.0f);
     dt26 = float(st.dt * st.dt / 6.0);
+    if (kSweep) {
+      beta = __ldg(R.cfg_beta + cfg);
+      kappa = __ldg(R.cfg_kappa + cfg);
+    }
   };
   auto take = [&](unsigned j) {  // queue position j
     idx = order ? __ldg(order + j) : j;
     flags = 0;
     m.load_state(Qin, idx, P, st);
+    if (kSweep) cfg = Qin.cfg[idx];
     bool ok = true;
     fresh = st.n_total < 0;
     if (fresh) {  // step setup deferred by the front kernel
@@ -614,7 +625,7 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_lens_persist(const __gri
     if (!__any_sync(kFull, phase == kRun)) return;
     for (int k = 0; k < n_steps; ++k) {
       if (phase == kRun) {
-        bool lost = m.template lens_step<F, kStaged>(L, dt, hdt, c2, dt6, dt26, s_tab, flags);
+        bool lost = m.template lens_step<F, kStaged, kSweep>(L, dt, hdt, c2, dt6, dt26, s_tab, flags, beta, kappa);
         if (F == kForceRadial && (flags & 2u)) lost = true;
         ++st.n_done;
         if (lost) phase = kLost;
@@ -630,15 +641,15 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_lens_persist(const __gri
     bool enter = false;
     if (phase == kLost || phase == kExit || phase == kBad) {
       m.load_rest(Qin, idx, st, !fresh);
-      lsteps += unsigned(st.n_done - n0);
+      acc.lsteps += unsigned(st.n_done - n0);
       if (phase == kBad) {  // rint(L/dz) not usable: the reference raises here
         label = e.label_inside;
-        ++bad;
-        steps += unsigned(m.rows);
+        ++acc.bad;
+        acc.steps += unsigned(m.rows);
         write_outputs<M, kOut>(R, m, label);
       } else {
-        range += (flags & 1u) ? 1 : 0;
-        rerr += (flags & 2u) ? 1 : 0;
+        acc.range += (flags & 1u) ? 1 : 0;
+        acc.rerr += (flags & 2u) ? 1 : 0;
         m.lens_end(P, li, st, phase == kLost);
         if (phase == kLost) {
           label = e.label_inside;
@@ -649,28 +660,29 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_lens_persist(const __gri
             enter = enter_lens(m, P, lens_at, nst);
             if (!enter) {
               label = P.el[lens_at].label_inside;
-              ++bad;
+              ++acc.bad;
             }
           }
         }
         if (label != kQueued) {
-          steps += unsigned(m.rows);
-          band += (m.margin < double(kEdgeBand)) ? 1 : 0;
+          acc.steps += unsigned(m.rows);
+          acc.band += (m.margin < double(kEdgeBand)) ? 1 : 0;
           write_outputs<M, kOut>(R, m, label);
         }
       }
       phase = kIdle;
     }
-    push_lens<kTagNone>(Qnext, enter, m, nst);
+    push_lens<kSweep ? kTagCarry : kTagNone>(Qnext, enter, m, nst, cfg);
     tally_warp(S, label, P.n_labels);
+    if (kSweep) tally_cfg(R, cfg, label, P.n_labels);
   };
 
   {
     const unsigned j = (unsigned(warp) * gridDim.x + blockIdx.x) * 32u + unsigned(lane);
-    if (j < n_in) take(j);
+    if (j < min(n_in, static_entries)) take(j);
   }
   // phase A
-  for (bool exhausted = static_entries >= n_in; !exhausted;) {
+  for (bool exhausted = static_entries >= n_in && static_entries > 0; !exhausted;) {
     run(kPersistService);
     finalize();
     const unsigned idle = __ballot_sync(kFull, phase == kIdle);
@@ -712,6 +724,7 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_lens_persist(const __gri
         w.flags = flags | (fresh ? 0x80000000u : 0u);
         w.phase = unsigned(phase);
         w.margin = m.margin;
+        w.cfg = cfg;
       }
       __syncthreads();
       phase = kIdle;
@@ -735,18 +748,105 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_lens_persist(const __gri
         fresh = (w.flags >> 31) != 0;
         phase = int(w.phase);
         m.margin = w.margin;
+        cfg = w.cfg;
         derive();
       }
       __syncthreads();
     }
   }
-  stat_add(S, kStatSteps, steps);
-  stat_add(S, kStatLensSteps, lsteps);
-  stat_add(S, kStatEdgeBand, band);
-  stat_add(S, kStatBadSteps, bad);
-  stat_add(S, kStatTableRange, range);
-  stat_add(S, kStatRangeError, rerr);
-  tally_flush(S, R, P.n_labels);
+}
+
+__device__ __forceinline__ void persist_flush(BlockTally& S, const RunDev& R, int n_labels, const PersistAcc& a) {
+  stat_add(S, kStatSteps, a.steps);
+  stat_add(S, kStatLensSteps, a.lsteps);
+  stat_add(S, kStatEdgeBand, a.band);
+  stat_add(S, kStatBadSteps, a.bad);
+  stat_add(S, kStatTableRange, a.range);
+  stat_add(S, kStatRangeError, a.rerr);
+  tally_flush(S, R, n_labels);
+}
+
+template <class M, bool kOut, int F, bool kStaged>
+__global__ void __launch_bounds__(kPersistThreads, 1) k_lens_persist(const __grid_constant__ Plan P, const RunDev R,
+                                                                     const int li, const Queue Qin, const Queue Qnext,
+                                                                     const LensArgs L, const unsigned* order,
+                                                                     const int interval) {
+  extern __shared__ float4 s_dyn[];
+  __shared__ BlockTally S;
+  __shared__ unsigned s_wcount[kPersistThreads / 32];
+  SwapSlot* s_swap = reinterpret_cast<SwapSlot*>(s_dyn + (kStaged ? L.n_int : 0));
+  if (*(volatile unsigned*)Qin.count == 0) return;
+  tally_init(S);
+  if (kStaged)
+    for (int k = threadIdx.x; k < L.n_int; k += blockDim.x) s_dyn[k] = __ldg(L.q + k);
+  __syncthreads();
+  PersistAcc acc;
+  // a short queue spreads over all SMs through the interleaved first entries
+  persist_pass<M, kOut, F, kStaged, false>(P, R, li, Qin, Qnext, L, order, interval, gridDim.x * kPersistThreads,
+                                           s_dyn, s_swap, s_wcount, S, acc);
+  persist_flush(S, R, P.n_labels, acc);
+}
+
+// Batched sweep: the Stark tables' lens queues in one launch.  Each CTA
+// starts on a table, chosen so that CTAs are spread over the tables in
+// proportion to their queues, and when that queue is used up moves on to the
+// next table with molecules left, staging its table.
+struct SweepTabs {
+  const float4* q[CTRAJ_MAX_TABLES];
+  const unsigned* order[CTRAJ_MAX_TABLES];
+  float s0[CTRAJ_MAX_TABLES];
+  int n_int[CTRAJ_MAX_TABLES];
+};
+
+template <int F, bool kStaged>
+__global__ void __launch_bounds__(kPersistThreads, 1) k_sweep_persist(const __grid_constant__ Plan P, const RunDev R,
+                                                                      const int li,
+                                                                      const __grid_constant__ SweepQueues Qs,
+                                                                      const int n_tab,
+                                                                      const __grid_constant__ SweepTabs T,
+                                                                      const LensArgs L0, const int interval) {
+  using M = Mol32<false, false>;
+  extern __shared__ float4 s_dyn[];
+  __shared__ BlockTally S;
+  __shared__ unsigned s_wcount[kPersistThreads / 32];
+  __shared__ int s_left;
+  int max_int = 0;
+  for (int t = 0; t < n_tab; ++t) max_int = max(max_int, T.n_int[t]);
+  SwapSlot* s_swap = reinterpret_cast<SwapSlot*>(s_dyn + (kStaged ? max_int : 0));
+  tally_init(S);
+  // first table: the one whose share of the queued molecules holds this CTA's
+  unsigned total = 0;
+  for (int t = 0; t < n_tab; ++t) total += *(volatile unsigned*)Qs.q[t].count;
+  const float pos = (float(blockIdx.x) + 0.5f) / float(gridDim.x) * float(total);
+  int t0 = n_tab - 1;
+  for (unsigned cum = 0, t = 0; t < unsigned(n_tab); ++t) {
+    cum += *(volatile unsigned*)Qs.q[t].count;
+    if (pos < float(cum)) {
+      t0 = int(t);
+      break;
+    }
+  }
+  PersistAcc acc;
+  for (int k = 0; k < n_tab; ++k) {
+    const int t = (t0 + k) % n_tab;
+    const Queue& Q = Qs.q[t];
+    __syncthreads();  // the previous table's last reads of s_dyn / s_left are done
+    if (threadIdx.x == 0) s_left = *(volatile unsigned*)Q.head < *(volatile unsigned*)Q.count;
+    __syncthreads();
+    if (!s_left) continue;
+    if (kStaged)
+      for (int j = threadIdx.x; j < T.n_int[t]; j += blockDim.x) s_dyn[j] = __ldg(T.q[t] + j);
+    __syncthreads();
+    LensArgs L = L0;
+    L.q = T.q[t];
+    L.s0 = T.s0[t];
+    L.n_int = T.n_int[t];
+    L.n_smem = kStaged ? T.n_int[t] : 0;
+    // no interleaved first entries: each CTA takes from its table's queue in order
+    persist_pass<M, false, F, kStaged, true>(P, R, li, Q, Q, L, T.order[t], interval, 0u, s_dyn, s_swap, s_wcount,
+                                            S, acc);
+  }
+  persist_flush(S, R, P.n_labels, acc);
 }
 
 // ---------------------------------------------------------------------------

@@ -4,8 +4,8 @@ The knobs (``ctraj_set_tuning``): which FP32 lens pass runs (one persistent
 launch that refills lanes and compacts the last molecules every
 ``lens_interval`` steps, or chunked launches), the length of the first lens
 chunk, the growth of later chunks and their maximum (how often molecules still
-inside a lens are compacted into full warps in chunked mode, which FP64 runs,
-ring recording and sweeps always use), and the size of the front kernel's grid.
+inside a lens are compacted into full warps in chunked mode, which FP64 runs
+and ring recording always use), and the size of the front kernel's grid.
 The best setting depends on the beamline: how fast molecules are lost inside
 the lens and how long the survivors stay.  ``autotune`` times every candidate
 on the actual workload with CUDA events (kernel time of the front and lens
@@ -23,15 +23,13 @@ from pathlib import Path
 DEFAULT = dict(chunk_first=64, chunk_growth=200, chunk_max=1024, front_waves=4, lens_mode=0, lens_interval=256)
 
 
-def candidates(chunked_only: bool = False):
-    """Knob settings to try.  ``chunked_only``: the chunk knobs alone, for
-    workloads whose lens pass is always chunked (batched sweeps)."""
+def candidates():
+    """Knob settings to try: the chunked lens pass with each chunk schedule,
+    the persistent one with each compaction interval, the front grid."""
     out = []
     for cf, g, cm in itertools.product((32, 64, 128), (150, 200, 300), (256, 512, 1024, 2048)):
         if cm >= cf:
             out.append(dict(DEFAULT, chunk_first=cf, chunk_growth=g, chunk_max=cm, lens_mode=1))
-    if chunked_only:
-        return out
     for iv in (64, 128, 256, 512, 1024):
         out.append(dict(DEFAULT, lens_interval=iv))
     for fw in (1, 2, 8):

@@ -244,11 +244,12 @@ int ctraj_set_beamline(ctraj_context* ctx, const ctraj_element* elements,
  *   chunk_growth  each chunk is this many percent of the previous  default 200
  *   chunk_max     upper limit of a chunk's steps                  default 1024
  *   front_waves   k_front grid = front_waves x resident CTAs     default 4
- *   lens_mode     FP32 lens pass: CTRAJ_LENS_PERSISTENT (one launch, lanes
- *                 refilled, the last molecules compacted within each CTA) or
+ *   lens_mode     FP32 lens pass of runs and sweeps: CTRAJ_LENS_PERSISTENT
+ *                 (one launch, lanes refilled, the last molecules compacted
+ *                 within each CTA; a sweep's Stark tables share the launch) or
  *                 CTRAJ_LENS_CHUNKED (launches of chunk_* steps, compacted in
- *                 between).  FP64 runs, ring recording and sweeps are always
- *                 chunked.  Results do not depend on it.    default persistent
+ *                 between).  FP64 runs and ring recording are always chunked.
+ *                 Results do not depend on it.              default persistent
  *   lens_interval persistent mode: RK4 steps between the CTA's compactions
  *                 once the lens queue is empty                   default 256 */
 enum { CTRAJ_LENS_PERSISTENT = 0, CTRAJ_LENS_CHUNKED = 1 };

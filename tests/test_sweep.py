@@ -124,6 +124,29 @@ def test_graph_replay_equals_direct_launches(engine):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_persistent_and_chunked_sweeps_agree(engine, use_graph):
+    """The one-launch persistent lens pass (default) and the chunked one give
+    the same per-configuration counts and steps: the same molecules through
+    the same arithmetic, in another order."""
+    from ctraj.sweep import run_sweep
+
+    cfg = small_configs(10_000, 40_000, seed=5)
+    bl = lens_beamline()
+    xs, vs = _specs()
+    try:
+        engine.set_tuning(lens_mode=1)
+        chunked = run_sweep(bl, cfg, xdist=xs, vdist=vs, seed=4, use_graph=use_graph, engine=engine)
+        for interval in (256, 7):
+            engine.set_tuning(lens_interval=interval)
+            pers = run_sweep(bl, cfg, xdist=xs, vdist=vs, seed=4, use_graph=use_graph, engine=engine)
+            np.testing.assert_array_equal(pers.counts, chunked.counts)
+            assert pers.molecule_steps == chunked.molecule_steps and pers.lens_steps == chunked.lens_steps
+    finally:
+        engine.set_tuning()
+
+
+@pytest.mark.gpu
 def test_sweep_matches_fp64_oracle_on_host_ics(engine):
     from ctraj.distributions import host_draw
     from ctraj.sweep import run_sweep
