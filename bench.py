@@ -54,6 +54,22 @@ FLOP_PER_BALLISTIC_STEP = 12
 # profiles/k_lens_persist_lens_beamline_1e7.md (the queue is read once; the
 # table and the molecule state stay on chip)
 LENS_DRAM_BYTES_PER_RUN = 10.9e6
+# Shared-memory wavefronts per warp table lookup (one LDS.128 per lane, random
+# intervals: ~2.3 bank-conflicted wavefronts in each of the 4 eight-lane
+# phases), from l1tex__data_pipe_lsu_wavefronts_mem_shared_op_ld of the same
+# capture: 1.91e8 wavefronts for 1.43e8 lane-steps x 4 lookups at 27.2 lanes
+# per warp instruction.  One wavefront per cycle per SM is the roof for the
+# throughput-bound phases of a lens pass.
+SHARED_WAVEFRONTS_PER_LOOKUP = 9.1
+LOOKUPS_PER_RK4_STEP = 4
+
+
+def shared_roof(lens_steps_per_s: float, sms: int, mhz: float) -> dict:
+    roof = sms * mhz * 1e6 * 32 / (LOOKUPS_PER_RK4_STEP * SHARED_WAVEFRONTS_PER_LOOKUP)
+    return {"bound": "shared-memory wavefronts (force-table lookups)", "unit": "RK4 lane-steps/s",
+            "wavefronts_per_lookup": SHARED_WAVEFRONTS_PER_LOOKUP, "lookups_per_step": LOOKUPS_PER_RK4_STEP,
+            "roof": roof, "achieved": lens_steps_per_s, "frac": lens_steps_per_s / roof,
+            "note": "1 shared-memory wavefront per cycle per SM; wavefronts per lookup from ncu"}
 WORKLOAD = ("lens beamline: aperture r=6mm@0.30m, hexapole lens z0=0.80m L=0.60m R=17.5mm V=30kV "
             "(4096-knot Stark spline, a=h*6.7GHz, d=4.2D), RK4 dt=1us, detection@3.0m; "
             "x,y~N(0,1.5mm) vx,vy~N(0,20m/s) vz~N(184,16m/s)")
@@ -80,7 +96,7 @@ def parse():
                         "or a ring-recording run (--molecules)")
     p.add_argument("--sweep-scale", type=float, default=1.0, help="molecule counts of --profile sweep x this")
     p.add_argument("--lens-mode", choices=["persistent", "chunked"], default="persistent",
-                   help="--profile lens: the FP32 lens pass to run (ctraj_tuning.lens_mode)")
+                   help="--profile lens/sweep: the FP32 lens pass to run (ctraj_tuning.lens_mode)")
     return p.parse_args()
 
 
@@ -319,13 +335,15 @@ def bench_sweep(eng, stream, flush, steps: int, warmup: int, device_name: str):
     for k in range(steps):
         flush.zero_()
         ev0.record(stream)
-        r = sweep(100 + k)
+        r = sweep(100 + k, timing=True)
         ev1.record(stream)
         ev1.synchronize()
         times.append(ev0.elapsed_time(ev1))
         res.append(r)
     sweep_ms = sum(times) / steps
     msteps = sum(r.molecule_steps for r in res) / steps
+    lsteps = sum(r.lens_steps for r in res) / steps
+    lens_ms = sum(r.extra["lens_ms"] for r in res) / steps
     # the loop of plain runs, on the same seed as the last sweep: counts must agree
     eng.set_tuning(**plain_tuning)
     cbs = config_beamlines(bl, cfg)
@@ -344,6 +362,10 @@ def bench_sweep(eng, stream, flush, steps: int, warmup: int, device_name: str):
             "loop_of_plain_runs_ms": loop_ms, "speedup_vs_loop": loop_ms / sweep_ms,
             "loop_count_difference": {"max_per_config": int(diff.max()), "total": int(diff.sum())},
             "tuning": tuned["tuning"], "tuning_cached": tuned.get("cached", False),
+            "lens_ms": lens_ms, "lens_steps": lsteps,
+            # at the GB300's maximum SM clock (the sweep runs outside the sampled region)
+            "roofline": shared_roof(lsteps / (lens_ms / 1e3), torch.cuda.get_device_properties(0).multi_processor_count,
+                                    2070.0),
             "timing": "CUDA events on the launching stream around ctraj_run_sweep (counts back on the host), "
                       "L2 flushed before each; loop timed with perf_counter"}
 
@@ -620,6 +642,9 @@ def main():
             "frac": floor_ms / (lens_ms / args.steps),
             "note": "latency floor of the slowest molecule (max_lens_steps x one-warp step latency); "
                     "frac = floor / measured lens pass"}
+    if mhz:
+        roofline["shared_memory"] = shared_roof(lens_steps / (lens_ms / 1e3), torch.cuda.get_device_properties(
+            local).multi_processor_count, mhz)
     cpu = None if args.no_cpu or world > 1 else cpu_baseline(int(args.cpu_sample))
     r0 = results[-1]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
