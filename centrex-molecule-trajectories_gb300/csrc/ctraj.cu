@@ -384,10 +384,12 @@ LensKernel lens_kernel(int force, bool staged) {
 // The persistent FP32 lens pass of lens element i over queue Qin (count
 // entries, at most max_steps steps each): order the entrants longest first,
 // then one k_lens_persist launch, one CTA per SM.
+// The persistent FP32 lens pass of lens element i over queue Qin: order the
+// entrants longest first into `order_buf` (kOrderBuckets + the queue's
+// entries), then one k_lens_persist launch, one CTA per SM.
 template <bool kOut>
-int launch_persistent(ctraj_context* c, const Plan& P, const RunDev& R, int i, const Queue& Qin, const Queue& Qnext,
-                      unsigned count, unsigned max_steps, int* launches) {
-  cudaStream_t s = c->stream;
+int enqueue_persistent(const Plan& P, const RunDev& R, int i, const Queue& Qin, const Queue& Qnext,
+                       unsigned* order_buf, int sms, int interval, cudaStream_t s, int* launches) {
   using M = Mol32<kOut, false>;
   using PK = void (*)(const Plan, const RunDev, const int, const Queue, const Queue, const LensArgs,
                       const unsigned*, const int);
@@ -406,21 +408,25 @@ int launch_persistent(ctraj_context* c, const Plan& P, const RunDev& R, int i, c
   }
   const size_t smem = (staged ? size_t(P.lf[i].n_int) * sizeof(float4) : 0) + kPersistThreads * sizeof(SwapSlot);
   CT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-  int st = c->lens_order.ensure((size_t(kOrderBuckets) + count) * sizeof(unsigned), 25);
-  if (st) return st;
-  unsigned* hist = c->lens_order.as<unsigned>();
+  unsigned* hist = order_buf;
   unsigned* order = hist + kOrderBuckets;
-  (void)max_steps;  // the ordering kernels read it from the queue
-  const int grid = c->sm_count;
   CT_CUDA(cudaMemsetAsync(hist, 0, kOrderBuckets * sizeof(unsigned), s));
-  k_order_count<<<grid, kOrderThreads, 0, s>>>(P, i, Qin, hist);
+  k_order_count<<<sms, kOrderThreads, 0, s>>>(P, i, Qin, hist);
   k_order_scan<<<1, kOrderBuckets, 0, s>>>(hist);
-  k_order_place<<<grid, kOrderThreads, 0, s>>>(P, i, Qin, hist, order);
-  k<<<c->sm_count, kPersistThreads, smem, s>>>(P, R, i, Qin, Qnext, lens_args(P, i, true), order,
-                                                c->lens_interval);
+  k_order_place<<<sms, kOrderThreads, 0, s>>>(P, i, Qin, hist, order);
+  k<<<sms, kPersistThreads, smem, s>>>(P, R, i, Qin, Qnext, lens_args(P, i, true), order, interval);
   CT_CUDA(cudaGetLastError());
   *launches += 4;
   return CTRAJ_OK;
+}
+
+template <bool kOut>
+int launch_persistent(ctraj_context* c, const Plan& P, const RunDev& R, int i, const Queue& Qin, const Queue& Qnext,
+                      unsigned count, int* launches) {
+  int st = c->lens_order.ensure((size_t(kOrderBuckets) + count) * sizeof(unsigned), 25);
+  if (st) return st;
+  return enqueue_persistent<kOut>(P, R, i, Qin, Qnext, c->lens_order.as<unsigned>(), c->sm_count,
+                                  c->lens_interval, c->stream, launches);
 }
 
 // k_front, then for each lens: read the lens queue's size and largest
@@ -483,7 +489,7 @@ int launch_all(ctraj_context* c, const Plan& P, const RunDev& R0, Queue* q, int*
     }
     if constexpr (!k64 && !kRing) {
       if (c->lens_mode == CTRAJ_LENS_PERSISTENT) {
-        int st = launch_persistent<kOut>(c, P, R, i, q[cur], q[nxt], count, max_steps, launches);
+        int st = launch_persistent<kOut>(c, P, R, i, q[cur], q[nxt], count, launches);
         if (st) return st;
         c->host_max[2 + i] = 0;  // no continuation queue
         std::swap(cur, nxt);
@@ -1695,9 +1701,10 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[CTRAJ_NOALLOC_S
 // Layout: control words (queue counters, tallies, stats) | per-chunk queue
 // counters | FP32 lens tables | three lens queues.
 constexpr size_t kNaCtl = 0;
-constexpr size_t kNaChunk = 4096;
-constexpr size_t kNaTables = kNaChunk + size_t(kMaxChunks) * kCtlWords * sizeof(unsigned);
-constexpr size_t kNaQueues = kNaTables + size_t(CTRAJ_NOALLOC_MAX_INTERVALS) * sizeof(float4);
+constexpr size_t kNaTables = 4096;
+constexpr size_t kNaOrder = kNaTables + size_t(CTRAJ_NOALLOC_MAX_INTERVALS) * sizeof(float4);
+constexpr size_t kNaQueues =
+    kNaOrder + ((size_t(kOrderBuckets) + CTRAJ_NOALLOC_MAX_MOLECULES) * sizeof(unsigned) + 255) / 256 * 256;
 
 std::mutex g_noalloc_mu;
 void* g_noalloc_ptr[64] = {};
@@ -1838,8 +1845,8 @@ int noalloc_plan(const ctraj_element* el, int n_el, int n_labels, const ctraj_fo
 
 // The launch sequence of launch_all (FP32), on the scratch's queues.
 template <bool kOut>
-int noalloc_launch(const Plan& P, const RunDev& R, Queue* q, unsigned* chunk_ctl, cudaStream_t s,
-                   int* launches, unsigned* leftover) {
+int noalloc_launch(const Plan& P, const RunDev& R, Queue* q, unsigned* order_buf, cudaStream_t s,
+                   int* launches) {
   int dev = 0, sms = 0;
   CT_CUDA(cudaGetDevice(&dev));
   CT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -1852,46 +1859,17 @@ int noalloc_launch(const Plan& P, const RunDev& R, Queue* q, unsigned* chunk_ctl
     CT_CUDA(cudaGetLastError());
     ++*launches;
   }
-  int cur = 0, alt = 1, nxt = 2;
+  int cur = 0, nxt = 1;
   for (int i = 0; i < P.n_el && n > 0; ++i) {
     if (P.el[i].type != CTRAJ_ELECTROSTATIC_LENS) continue;
-    unsigned head[2] = {0, 0};  // count, largest remaining step count
-    CT_CUDA(cudaMemcpyAsync(head, q[cur].count, sizeof head, cudaMemcpyDeviceToHost, s));
+    unsigned count = 0;
+    CT_CUDA(cudaMemcpyAsync(&count, q[cur].count, sizeof count, cudaMemcpyDeviceToHost, s));
     CT_CUDA(cudaStreamSynchronize(s));
-    if (head[0] == 0) break;
+    if (count == 0) break;
     CT_CUDA(cudaMemsetAsync(q[nxt].count, 0, kCtlWords * sizeof(unsigned), s));
-    const bool staged = P.lf[i].n_smem > 0;
-    const size_t smem = staged ? size_t(P.lf[i].n_int) * sizeof(float4) : 0;
-    LensKernel kl = lens_kernel<false, kOut>(P.lf[i].force, staged);
-    CT_CUDA(cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    const int64_t per_launch = int64_t(blocks_per_sm(kl, kLensThreads, smem)) * sms;
-    const int grid =
-        int(std::max<int64_t>(1, std::min<int64_t>(per_launch, (head[0] + kLensThreads - 1) / kLensThreads)));
-    int lens_chunks[kMaxChunks];
-    int nc = 0;
-    for (int64_t done = 0, len = 64; done < int64_t(head[1]) || nc == 0; len = std::min<int64_t>(2 * len, 1024)) {
-      if (nc == kMaxChunks) return fail(CTRAJ_ESTEPS, "lens element %d needs more than %d chunks", i, kMaxChunks);
-      lens_chunks[nc++] = int(len);
-      done += len;
-    }
-    CT_CUDA(cudaMemsetAsync(chunk_ctl, 0, size_t(nc) * kCtlWords * sizeof(unsigned), s));
-    const LensArgs la = lens_args(P, i, true);
-    Queue in = q[cur];
-    for (int k = 0; k < nc; ++k) {
-      Queue out = q[alt];
-      out.count = chunk_ctl + size_t(k) * kCtlWords;
-      out.max_steps = out.count + 1;
-      out.head = out.count + 2;
-      kl<<<grid, kLensThreads, smem, s>>>(P, R, i, in, out, q[nxt], lens_chunks[k], la);
-      CT_CUDA(cudaGetLastError());
-      ++*launches;
-      in = out;
-      std::swap(cur, alt);
-    }
-    unsigned left = 0;
-    CT_CUDA(cudaMemcpyAsync(&left, in.count, sizeof left, cudaMemcpyDeviceToHost, s));
-    CT_CUDA(cudaStreamSynchronize(s));
-    *leftover += left;
+    // the persistent pass finishes every molecule: nothing stays inside the lens
+    int st = enqueue_persistent<kOut>(P, R, i, q[cur], q[nxt], order_buf, sms, 256, s, launches);
+    if (st) return st;
     std::swap(cur, nxt);
   }
   return CTRAJ_OK;
@@ -1943,7 +1921,7 @@ extern "C" int ctraj_run_noalloc(const ctraj_element* el, int32_t n_el, int32_t 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const size_t cap = CTRAJ_NOALLOC_MAX_MOLECULES;
   const size_t qb = queue_bytes(cap, 32);
-  if (kNaQueues + 3 * qb > CTRAJ_NOALLOC_SCRATCH_BYTES) return fail(CTRAJ_ENOMEM, "scratch layout too large");
+  if (kNaQueues + 2 * qb > CTRAJ_NOALLOC_SCRATCH_BYTES) return fail(CTRAJ_ENOMEM, "scratch layout too large");
   Plan P;
   if ((st = noalloc_plan(el, n_el, n_labels, tabs, n_tab, a, reinterpret_cast<float4*>(scratch + kNaTables), s, P)))
     return st;
@@ -1951,8 +1929,8 @@ extern "C" int ctraj_run_noalloc(const ctraj_element* el, int32_t n_el, int32_t 
   unsigned long long* counts = reinterpret_cast<unsigned long long*>(scratch + kNaCtl + 256);
   unsigned long long* dstats = reinterpret_cast<unsigned long long*>(scratch + kNaCtl + 256 + 8 * (CTRAJ_MAX_LABELS + 1));
   // queues are handed over in DevBuf form so the same layout code places the arrays
-  Queue q[3];
-  for (int k = 0; k < 3; ++k) {
+  Queue q[2];
+  for (int k = 0; k < 2; ++k) {
     DevBuf view;
     view.p = scratch + kNaQueues + size_t(k) * qb;
     view.bytes = qb;
@@ -1984,16 +1962,14 @@ extern "C" int ctraj_run_noalloc(const ctraj_element* el, int32_t n_el, int32_t 
     R.out_final = a->out_final;
   }
   int launches = 0;
-  unsigned leftover = 0;
-  unsigned* chunk_ctl = reinterpret_cast<unsigned*>(scratch + kNaChunk);
-  st = out ? noalloc_launch<true>(P, R, q, chunk_ctl, s, &launches, &leftover)
-           : noalloc_launch<false>(P, R, q, chunk_ctl, s, &launches, &leftover);
+  unsigned* order_buf = reinterpret_cast<unsigned*>(scratch + kNaOrder);
+  st = out ? noalloc_launch<true>(P, R, q, order_buf, s, &launches)
+           : noalloc_launch<false>(P, R, q, order_buf, s, &launches);
   if (st) return st;
   unsigned long long hc[CTRAJ_MAX_LABELS + 1], hs[kStatCount];
   CT_CUDA(cudaMemcpyAsync(hc, counts, sizeof hc, cudaMemcpyDeviceToHost, s));
   CT_CUDA(cudaMemcpyAsync(hs, dstats, sizeof hs, cudaMemcpyDeviceToHost, s));
   CT_CUDA(cudaStreamSynchronize(s));
-  if (leftover) return fail(CTRAJ_ECUDA, "internal error: %u molecules left inside a lens", leftover);
   for (int k = 0; k <= n_labels; ++k) a->counts[k] = int64_t(hc[k]);
   if (stats) {
     std::memset(stats, 0, sizeof *stats);

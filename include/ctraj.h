@@ -460,9 +460,10 @@ int ctraj_soft_transmission(ctraj_context* ctx, const ctraj_soft_args* args,
  * Allocation-free run.  This entry point has no counterpart in the reference.
  *
  * ctraj_run_noalloc propagates molecules exactly as ctraj_run does (same
- * kernels, same results molecule by molecule) but needs no context and
- * allocates no device memory: its scratch (lens queues, queue counters,
- * tallies, the FP32 lens tables) lives in one file-scope __device__ array of
+ * kernels -- the persistent lens pass with the default compaction interval --
+ * same results molecule by molecule) but needs no context and allocates no
+ * device memory: its scratch (lens queues, queue counters, tallies, the FP32
+ * lens tables, the lens-entrant order) lives in one file-scope __device__ array of
  * CTRAJ_NOALLOC_SCRATCH_BYTES that every GPU which loads libctraj.so holds
  * until the process exits.  It is for callers that cannot allocate device
  * memory while they run: an application that hands this library a fixed
