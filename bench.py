@@ -463,6 +463,7 @@ def bench_large(eng, stream, flush, n_total: int = 1_000_000_000, chunk: int = 1
     cb = compile_beamline(lens_beamline())
     xd, vd = source()
     xs, vs = device_spec(xd, "position"), device_spec(vd, "velocity")
+    eng.set_tuning()  # default knobs (persistent lens pass), not the sweep's
     ring = HBMRing(capacity_rows=200_000_000, capacity_molecules=20_000_000, stride=50)
     run_streamed(cb, 2_000_000, chunk=chunk, xdist=xs, vdist=vs, seed=1, ring=ring, engine=eng)  # warm-up
     ring.reset()

@@ -387,7 +387,7 @@ LensKernel lens_kernel(int force, bool staged) {
 // The persistent FP32 lens pass of lens element i over queue Qin: order the
 // entrants longest first into `order_buf` (kOrderBuckets + the queue's
 // entries), then one k_lens_persist launch, one CTA per SM.
-template <bool kOut>
+template <bool kOut, bool kRing = false>
 int enqueue_persistent(const Plan& P, const RunDev& R, int i, const Queue& Qin, const Queue& Qnext,
                        unsigned* order_buf, int sms, int interval, cudaStream_t s, int* launches) {
   using M = Mol32<kOut, false>;
@@ -397,13 +397,16 @@ int enqueue_persistent(const Plan& P, const RunDev& R, int i, const Queue& Qin, 
   PK k;
   switch (P.lf[i].force) {
     case kForceStark2:
-      k = staged ? k_lens_persist<M, kOut, kForceStark2, true> : k_lens_persist<M, kOut, kForceStark2, false>;
+      k = staged ? k_lens_persist<M, kOut, kForceStark2, true, kRing>
+                 : k_lens_persist<M, kOut, kForceStark2, false, kRing>;
       break;
     case kForceStark1:
-      k = staged ? k_lens_persist<M, kOut, kForceStark1, true> : k_lens_persist<M, kOut, kForceStark1, false>;
+      k = staged ? k_lens_persist<M, kOut, kForceStark1, true, kRing>
+                 : k_lens_persist<M, kOut, kForceStark1, false, kRing>;
       break;
     default:
-      k = staged ? k_lens_persist<M, kOut, kForceRadial, true> : k_lens_persist<M, kOut, kForceRadial, false>;
+      k = staged ? k_lens_persist<M, kOut, kForceRadial, true, kRing>
+                 : k_lens_persist<M, kOut, kForceRadial, false, kRing>;
       break;
   }
   const size_t smem = (staged ? size_t(P.lf[i].n_int) * sizeof(float4) : 0) + kPersistThreads * sizeof(SwapSlot);
@@ -420,13 +423,13 @@ int enqueue_persistent(const Plan& P, const RunDev& R, int i, const Queue& Qin, 
   return CTRAJ_OK;
 }
 
-template <bool kOut>
+template <bool kOut, bool kRing = false>
 int launch_persistent(ctraj_context* c, const Plan& P, const RunDev& R, int i, const Queue& Qin, const Queue& Qnext,
                       unsigned count, int* launches) {
   int st = c->lens_order.ensure((size_t(kOrderBuckets) + count) * sizeof(unsigned), 25);
   if (st) return st;
-  return enqueue_persistent<kOut>(P, R, i, Qin, Qnext, c->lens_order.as<unsigned>(), c->sm_count,
-                                  c->lens_interval, c->stream, launches);
+  return enqueue_persistent<kOut, kRing>(P, R, i, Qin, Qnext, c->lens_order.as<unsigned>(), c->sm_count,
+                                         c->lens_interval, c->stream, launches);
 }
 
 // k_front, then for each lens: read the lens queue's size and largest
@@ -487,9 +490,9 @@ int launch_all(ctraj_context* c, const Plan& P, const RunDev& R0, Queue* q, int*
       CT_CUDA(cudaMemsetAsync(R.rec_n, 0, sb, s));
       ring_slots = count;
     }
-    if constexpr (!k64 && !kRing) {
+    if constexpr (!k64) {
       if (c->lens_mode == CTRAJ_LENS_PERSISTENT) {
-        int st = launch_persistent<kOut>(c, P, R, i, q[cur], q[nxt], count, launches);
+        int st = launch_persistent<kOut, kRing>(c, P, R, i, q[cur], q[nxt], count, launches);
         if (st) return st;
         c->host_max[2 + i] = 0;  // no continuation queue
         std::swap(cur, nxt);

@@ -572,7 +572,7 @@ struct PersistAcc {
 // configuration (Queue::cfg), whose beta and kappa scale the unscaled table,
 // and tallies are also kept per configuration.  Every thread of the CTA
 // calls it; it returns with all of the CTA's molecules finalised.
-template <class M, bool kOut, int F, bool kStaged, bool kSweep>
+template <class M, bool kOut, int F, bool kStaged, bool kSweep, bool kRing = false>
 __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, const int li, const Queue& Qin,
                                              const Queue& Qnext, const LensArgs& L, const unsigned* order,
                                              const int interval, const unsigned static_entries,
@@ -590,10 +590,12 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
   int phase = kIdle;
   unsigned flags = 0;
   float dt = 0.f, hdt = 0.f, c2 = 0.f, dt6 = 0.f, dt26 = 0.f;
-  int n0 = 0, cfg = 0;
+  int n0 = 0, cfg = 0;  // cfg: the configuration (kSweep) or the record slot (kRing)
   float beta = 0.f, kappa = 1.f;
   bool fresh = false;
   unsigned idx = 0;
+  const bool rec_on = kRing && li == R.rec_lens;
+  int to_rec = 0;  // ring recording: steps to the next staged record
 
   auto derive = [&]() {
     dt = float(st.dt);
@@ -610,7 +612,13 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
     idx = order ? __ldg(order + j) : j;
     flags = 0;
     m.load_state(Qin, idx, P, st);
-    if (kSweep) cfg = Qin.cfg[idx];
+    if (kSweep || kRing) cfg = Qin.cfg[idx];
+    if constexpr (kRing) {
+      if (rec_on) {  // the entrance state opens the record
+        to_rec = R.rec_stride - st.n_done % R.rec_stride;
+        if (st.n_done == 0) R.rec[size_t(cfg) * R.rec_max] = make_float4(m.x, m.y, m.vx, m.vy);
+      }
+    }
     bool ok = true;
     fresh = st.n_total < 0;
     if (fresh) {  // step setup deferred by the front kernel
@@ -628,6 +636,12 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
         bool lost = m.template lens_step<F, kStaged, kSweep>(L, dt, hdt, c2, dt6, dt26, s_tab, flags, beta, kappa);
         if (F == kForceRadial && (flags & 2u)) lost = true;
         ++st.n_done;
+        if constexpr (kRing) {
+          if (rec_on && --to_rec == 0) {
+            to_rec = R.rec_stride;
+            R.rec[size_t(cfg) * R.rec_max + st.n_done / R.rec_stride] = make_float4(m.x, m.y, m.vx, m.vy);
+          }
+        }
         if (lost) phase = kLost;
         else if (st.n_done == st.n_total) phase = kExit;
       }
@@ -641,6 +655,23 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
     bool enter = false;
     if (phase == kLost || phase == kExit || phase == kBad) {
       m.load_rest(Qin, idx, st, !fresh);
+      if constexpr (kRing) {
+        if (rec_on) {  // close the record (the state after the losing step) before the exit snap
+          int n_rec = 0;
+          if (phase == kLost) {
+            const int s = R.rec_stride, k = st.n_done;
+            if (k % s != 0) R.rec[size_t(cfg) * R.rec_max + k / s + 1] = make_float4(m.x, m.y, m.vx, m.vy);
+            n_rec = k / s + 1 + (k % s != 0 ? 1 : 0);
+            R.rec_last[cfg] = k;
+          }
+          R.rec_n[cfg] = n_rec;  // 0: left the lens (or unusable step count), not recorded
+          if (fresh) {
+            R.rec_id[cfg] = m.id;
+            R.rec_t0[cfg] = m.t;
+            R.rec_vz[cfg] = m.vz;
+          }
+        }
+      }
       acc.lsteps += unsigned(st.n_done - n0);
       if (phase == kBad) {  // rint(L/dz) not usable: the reference raises here
         label = e.label_inside;
@@ -672,7 +703,7 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
       }
       phase = kIdle;
     }
-    push_lens<kSweep ? kTagCarry : kTagNone>(Qnext, enter, m, nst, cfg);
+    push_lens<(kSweep || kRing) ? kTagCarry : kTagNone>(Qnext, enter, m, nst, cfg);
     tally_warp(S, label, P.n_labels);
     if (kSweep) tally_cfg(R, cfg, label, P.n_labels);
   };
@@ -749,6 +780,7 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
         phase = int(w.phase);
         m.margin = w.margin;
         cfg = w.cfg;
+        if (kRing && rec_on) to_rec = R.rec_stride - st.n_done % R.rec_stride;
         derive();
       }
       __syncthreads();
@@ -766,7 +798,7 @@ __device__ __forceinline__ void persist_flush(BlockTally& S, const RunDev& R, in
   tally_flush(S, R, n_labels);
 }
 
-template <class M, bool kOut, int F, bool kStaged>
+template <class M, bool kOut, int F, bool kStaged, bool kRing = false>
 __global__ void __launch_bounds__(kPersistThreads, 1) k_lens_persist(const __grid_constant__ Plan P, const RunDev R,
                                                                      const int li, const Queue Qin, const Queue Qnext,
                                                                      const LensArgs L, const unsigned* order,
@@ -782,8 +814,8 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_lens_persist(const __gri
   __syncthreads();
   PersistAcc acc;
   // a short queue spreads over all SMs through the interleaved first entries
-  persist_pass<M, kOut, F, kStaged, false>(P, R, li, Qin, Qnext, L, order, interval, gridDim.x * kPersistThreads,
-                                           s_dyn, s_swap, s_wcount, S, acc);
+  persist_pass<M, kOut, F, kStaged, false, kRing>(P, R, li, Qin, Qnext, L, order, interval,
+                                                  gridDim.x * kPersistThreads, s_dyn, s_swap, s_wcount, S, acc);
   persist_flush(S, R, P.n_labels, acc);
 }
 

@@ -5,7 +5,7 @@ launch that refills lanes and compacts the last molecules every
 ``lens_interval`` steps, or chunked launches), the length of the first lens
 chunk, the growth of later chunks and their maximum (how often molecules still
 inside a lens are compacted into full warps in chunked mode, which FP64 runs
-and ring recording always use), and the size of the front kernel's grid.
+always use), and the size of the front kernel's grid.
 The best setting depends on the beamline: how fast molecules are lost inside
 the lens and how long the survivors stay.  ``autotune`` times every candidate
 on the actual workload with CUDA events (kernel time of the front and lens

@@ -248,8 +248,8 @@ int ctraj_set_beamline(ctraj_context* ctx, const ctraj_element* elements,
  *                 (one launch, lanes refilled, the last molecules compacted
  *                 within each CTA; a sweep's Stark tables share the launch) or
  *                 CTRAJ_LENS_CHUNKED (launches of chunk_* steps, compacted in
- *                 between).  FP64 runs and ring recording are always chunked.
- *                 Results do not depend on it.              default persistent
+ *                 between).  FP64 runs are always chunked.  Results (and ring
+ *                 records) do not depend on it.             default persistent
  *   lens_interval persistent mode: RK4 steps between the CTA's compactions
  *                 once the lens queue is empty                   default 256 */
 enum { CTRAJ_LENS_PERSISTENT = 0, CTRAJ_LENS_CHUNKED = 1 };

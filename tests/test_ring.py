@@ -102,6 +102,31 @@ def test_small_ring_keeps_the_latest_complete_records(engine):
     assert small.counts() == (2 * n_rows, 2 * n_mol)
 
 
+def test_ring_is_the_same_in_both_lens_modes(engine):
+    """The persistent lens pass (default) and the chunked one record the same
+    molecules with the same rows."""
+    from ctraj.ring import HBMRing
+
+    cb = compile_beamline(lens_beamline())
+    xs, vs = _specs()
+    n = 30_000
+    out = []
+    try:
+        for mode in (0, 1):
+            engine.set_tuning(lens_mode=mode)
+            ring = HBMRing(capacity_rows=150_000, capacity_molecules=15_000, stride=STRIDE)
+            r = engine.run(cb, n, xdist=xs, vdist=vs, seed=8, ring=ring)
+            out.append((r.counts, {rec.molecule: (rec.label, rec.rows) for rec in ring.read()}, ring.counts()))
+    finally:
+        engine.set_tuning()
+    (c0, m0, k0), (c1, m1, k1) = out
+    np.testing.assert_array_equal(c0, c1)
+    assert k0 == k1 and m0.keys() == m1.keys() and m0
+    for mol, (label, rows) in m0.items():
+        assert m1[mol][0] == label
+        np.testing.assert_array_equal(m1[mol][1], rows)
+
+
 def test_ring_argument_checks(engine):
     from ctraj.ring import HBMRing
 
