@@ -742,6 +742,10 @@ __global__ void __launch_bounds__(kSoftThreads) k_soft_compose(const __grid_cons
     const SoftLensSteps<T> L(S, m.vz);
     const int n_seg = (L.N + S.checkpoint - 1) / S.checkpoint;
     T lx = T(0), ly = T(0), lvx = T(0), lvy = T(0), gV = T(0);
+    // unrolled so that the next segments' loads are issued while this one's
+    // products wait (a thread walks its segments in order; the maps are read
+    // once each)
+#pragma unroll 4
     for (int sg = n_seg - 1; sg >= 0; --sg) {
       const T* o = seg_out + size_t(b) * size_t(max_seg) + size_t(sg);
       const T lo[4] = {lx, ly, lvx, lvy};
