@@ -12,9 +12,15 @@ One step = one full propagation of all molecules (ctraj_run).
 Metric: molecule-steps/s = sum over molecules of len(trajectory.t) - 1 (the
 reference's trajectory rows after the initial one), counted on the device.
 
-`value` times ctraj_run with CUDA events on its stream (L2 flushed between
-steps).  `e2e` times the public drop-in TrajectorySimulator.run_simulation
-(host Beamline / Distribution objects in, Counter out) with perf_counter.
+`value` times the K runs as one pipelined ctraj_run_batch with CUDA events on
+the engine's stream (runs alternate between two lanes, so one run's ballistic
+front overlaps the previous run's lens pass; L2 flushed before every run
+inside the timed region); `sequential` times the same runs one ctraj_run at a
+time (L2 flushed between them), and those runs give the front / lens split
+and the roofline.  `e2e` times the public drop-in TrajectorySimulator
+(host Beamline / Distribution objects in, Counters out) with perf_counter:
+run_simulations over the K batches, and (run_simulation_loop) one
+run_simulation per batch.
 `cpu_baseline` and --impl reference time the FP64 C restatement of the
 reference (oracle/) on the host cores on a bounded sample of the same workload.
 For N > 1 (torchrun) every rank propagates its own 1e7 molecules on disjoint
@@ -547,6 +553,8 @@ def main():
                      device_name=torch.cuda.get_device_name(local))
     for k in range(args.warmup):
         step(seed=k)
+    eng.run_batch(cb, n, list(range(max(2, args.warmup))), precision=32, xdist=xs, vdist=vs, offset=rank * n,
+                  l2_flush_bytes=flush.numel())
     peak = fp32_peak(local)
     probe = step_probe(local, bl)
 
@@ -555,63 +563,107 @@ def main():
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
+    seeds = [1000 + k for k in range(args.steps)]
     times, results = [], []
     with Clocks(local) as clk:
+        # the K runs one at a time: the front / lens-pass split and the roofline
         for k in range(args.steps):
             flush.zero_()
             ev0.record(stream)
-            r = step(seed=1000 + k)
+            r = step(seed=seeds[k])
             ev1.record(stream)
             ev1.synchronize()
             times.append(ev0.elapsed_time(ev1))
             results.append(r)
         torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        # the headline: the same K runs as one pipelined batch, the L2 flush
+        # written on the lane's stream before every run inside the timed region
+        ev0.record(stream)
+        batch = eng.run_batch(cb, n, seeds, precision=32, xdist=xs, vdist=vs, offset=rank * n,
+                              l2_flush_bytes=flush.numel())
+        ev1.record(stream)
+        ev1.synchronize()
+        batch_ms = ev0.elapsed_time(ev1)
+        torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
+    for a, b in zip(results, batch):  # the batch must reproduce the single runs
+        if list(a.counts) != list(b.counts) or a.molecule_steps != b.molecule_steps:
+            raise RuntimeError("ctraj_run_batch differs from ctraj_run on the same seeds")
     clocks = clk.summary()
-    total_ms = sum(times)
-    steps = sum(r.molecule_steps for r in results)
+    seq_ms = sum(times)
+    total_ms = batch_ms
+    steps = sum(r.molecule_steps for r in batch)
     lens_steps = sum(r.lens_steps for r in results)
     lens_ms = sum(r.extra["lens_ms"] for r in results)
     front_ms = sum(r.extra["front_ms"] for r in results)
     if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+        t = torch.tensor([total_ms, seq_ms], dtype=torch.float64, device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         s = torch.tensor([steps], dtype=torch.float64, device="cuda")
         dist.all_reduce(s, op=dist.ReduceOp.SUM)
-        total_ms, steps_all = float(t.item()), float(s.item())
+        total_ms, seq_ms, steps_all = float(t[0].item()), float(t[1].item()), float(s.item())
     else:
         steps_all = float(steps)
     value = steps_all / (total_ms / 1e3)
+    sequential = {"value": steps_all / (seq_ms / 1e3), "ms_per_step": seq_ms / args.steps,
+                  "api": "ctraj_run once per step (Engine.run), L2 flushed between steps outside the events"}
 
     # end to end through the public drop-in API
     e2e = None
     if not args.no_e2e:
         sim = TrajectorySimulator(device=local)
+        names = [f"run{k}" for k in range(args.steps)]
         for k in range(max(1, args.warmup)):
             sim.run_simulation(bl, "warm", vdist=vdist, xdist=xdist, N_traj=n, seed=k)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        e2e_steps = 0
-        for k in range(args.steps):
-            sim.run_simulation(bl, f"run{k}", vdist=vdist, xdist=xdist, N_traj=n, seed=2000 + k)
-            e2e_steps += sim.last_run.molecule_steps
-        e2e_s = time.perf_counter() - t0
+        sim.run_simulations(bl, names[:2], vdist=vdist, xdist=xdist, N_traj=n, seeds=[0, 1])
         tab = cb.tables[0]
-        h2d = (tab.knots.nbytes + tab.coef.nbytes + (tab.knots.size - 1) * 16
-               + ctypes.sizeof(cb.elements))
+        upload = (tab.knots.nbytes + tab.coef.nbytes + (tab.knots.size - 1) * 16
+                  + ctypes.sizeof(cb.elements))
         d2h = 8 * (len(cb.labels) + 1) + 64
-        if world > 1:
-            t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
-            s = torch.tensor([e2e_steps], dtype=torch.float64, device="cuda")
-            dist.all_reduce(s, op=dist.ReduceOp.SUM)
-            e2e_steps = float(s.item())
-        e2e = {"value": e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+
+        def timed(fn):
+            torch.cuda.synchronize()
+            if world > 1:
+                dist.barrier()
+            t0 = time.perf_counter()
+            got = fn()
+            el = time.perf_counter() - t0
+            if world > 1:
+                t = torch.tensor([el], dtype=torch.float64, device="cuda")
+                dist.all_reduce(t, op=dist.ReduceOp.MAX)
+                el = float(t.item())
+                s = torch.tensor([got], dtype=torch.float64, device="cuda")
+                dist.all_reduce(s, op=dist.ReduceOp.SUM)
+                got = float(s.item())
+            return got / el, el
+
+        def loop():
+            tot = 0
+            for k in range(args.steps):
+                sim.run_simulation(bl, names[k], vdist=vdist, xdist=xdist, N_traj=n, seed=2000 + k)
+                tot += sim.last_run.molecule_steps
+            return tot
+
+        def pipelined():
+            sim.run_simulations(bl, names, vdist=vdist, xdist=xdist, N_traj=n,
+                                seeds=[2000 + k for k in range(args.steps)])
+            return sum(r.molecule_steps for r in sim.last_runs)
+
+        v_loop, s_loop = timed(loop)
+        v_pipe, s_pipe = timed(pipelined)
+        # run_simulations compiles and uploads the beamline once per call for
+        # each of the two lanes; run_simulation once per call
+        e2e = {"value": v_pipe, "unit": UNIT, "h2d_bytes_per_step": int(round(2 * upload / args.steps)),
                "d2h_bytes_per_step": int(d2h),
-               "api": "ctraj.TrajectorySimulator.run_simulation(beamline, run_name, vdist, xdist, N_traj=1e7)",
-               "ms_per_step": e2e_s / args.steps * 1e3}
+               "api": "ctraj.TrajectorySimulator.run_simulations(beamline, run_names, vdist, xdist, N_traj=1e7): "
+                      "the loop of run_simulation over K batches as one pipelined call",
+               "ms_per_step": s_pipe / args.steps * 1e3,
+               "run_simulation_loop": {"value": v_loop, "ms_per_step": s_loop / args.steps * 1e3,
+                                       "h2d_bytes_per_step": int(upload), "d2h_bytes_per_step": int(d2h),
+                                       "api": "ctraj.TrajectorySimulator.run_simulation once per batch"}}
 
     if rank != 0:
         return
@@ -653,12 +705,16 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
             "data": "synthetic: Philox-4x32-10 initial conditions drawn on the device",
             "config": {"workload": WORKLOAD, "molecules_per_gpu": n, "precision": "fp32",
-                       "l2": "flushed between steps (256 MiB write outside the timed events)",
+                       "pipelining": "ctraj_run_batch: the K runs alternate between two lanes (contexts with "
+                                     "their own streams and buffers, one host thread each); a run's front "
+                                     "overlaps the other lane's lens pass",
+                       "l2": "flushed before every run: 256 MiB written on the run's lane stream inside the "
+                             "timed region (pipelined batch); between steps outside the events (sequential)",
                        "parallelism": f"replicas x{world}",
                        "tuning": tuned["tuning"], "tuning_cached": tuned.get("cached", False)},
-            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "sweep": sweep,
-            "adjoint": adjoint, "large": large,
-            "gpu_launches": int(sum(r.kernels for r in results)),
+            "e2e": e2e, "sequential": sequential, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+            "sweep": sweep, "adjoint": adjoint, "large": large,
+            "gpu_launches": int(sum(r.kernels for r in batch)),
             "molecule_steps_per_step": steps / args.steps, "counts_last_step": r0.counter_dict()}
     print(json.dumps(line), flush=True)
     eng.close()

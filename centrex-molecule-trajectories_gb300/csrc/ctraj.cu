@@ -15,6 +15,8 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <system_error>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -137,6 +139,12 @@ struct ctraj_context {
   cudaGraphExec_t sweep_exec = nullptr;
   std::vector<char> sweep_key;  // inputs the captured graph was built from
   int sweep_launches = 0;
+  // pipelined batches (ctraj_run_batch): the second lane's context, a copy of
+  // this one's beamline, tables and tuning as of generation peer_generation
+  ctraj_context* peer = nullptr;
+  uint64_t peer_generation = ~uint64_t(0);
+  DevBuf l2_flush;              // scratch written before each run of a batch
+  cudaEvent_t batch_ev = nullptr;
 };
 
 namespace ctraj {
@@ -691,6 +699,10 @@ int ctraj_destroy(ctraj_context* c) {
   c->soft_seg.release();
   for (auto& ev : c->ev)
     if (ev) cudaEventDestroy(ev);
+  if (c->peer) ctraj_destroy(c->peer);
+  cudaSetDevice(c->device);
+  c->l2_flush.release();
+  if (c->batch_ev) cudaEventDestroy(c->batch_ev);
   if (c->host_max) cudaFreeHost(c->host_max);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
@@ -916,6 +928,107 @@ static int run_impl(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* 
 
 int ctraj_run(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* stats) {
   return run_impl(c, a, stats, nullptr);
+}
+
+// One lane of a pipelined batch: runs lane, lane + 2, ... on context x.
+struct BatchLane {
+  int status = CTRAJ_OK;
+  int run = -1;
+  std::string error;
+};
+
+static void batch_lane(ctraj_context* x, const ctraj_run_args* a, int32_t n_runs, int lane,
+                       ctraj_run_stats* stats, uint64_t flush, BatchLane* out) {
+  int st = CTRAJ_OK;
+  int k = lane;
+  if (cudaSetDevice(x->device) != cudaSuccess) st = fail(CTRAJ_ECUDA, "cudaSetDevice(%d) failed", x->device);
+  if (!st && flush) st = x->l2_flush.ensure(size_t(flush));
+  for (; !st && k < n_runs; k += 2) {
+    if (flush) {
+      const cudaError_t e = cudaMemsetAsync(x->l2_flush.p, k & 0xff, size_t(flush), x->stream);
+      if (e != cudaSuccess) st = fail(CTRAJ_ECUDA, "L2 flush: %s", cudaGetErrorString(e));
+    }
+    if (!st) st = run_impl(x, a + k, stats ? stats + k : nullptr, nullptr);
+    if (st) break;
+  }
+  if (st) {
+    out->status = st;
+    out->run = k;
+    out->error = g_error;
+  }
+}
+
+// The second lane's context: same device, and the beamline, tables and
+// tuning of c (copied again whenever c's generation moved).
+static int batch_peer(ctraj_context* c) {
+  if (!c->peer) {
+    int st = ctraj_create(c->device, &c->peer);
+    if (st) return st;
+    c->peer_generation = ~uint64_t(0);
+  }
+  ctraj_context* p = c->peer;
+  if (c->peer_generation != c->generation) {
+    p->elements = c->elements;
+    p->n_labels = c->n_labels;
+    p->have_beamline = c->have_beamline;
+    for (int t = 0; t < CTRAJ_MAX_TABLES; ++t) {
+      p->tables[t].kind = c->tables[t].kind;
+      p->tables[t].n = c->tables[t].n;
+      p->tables[t].knots = c->tables[t].knots;
+      p->tables[t].coef = c->tables[t].coef;
+      p->tables[t].values = c->tables[t].values;
+      p->tables[t].uploaded = false;
+    }
+    p->lens_tables_dirty = true;
+    p->chunk = c->chunk;
+    p->chunk_growth = c->chunk_growth;
+    p->chunk_max = c->chunk_max;
+    p->front_waves = c->front_waves;
+    p->lens_mode = c->lens_mode;
+    p->lens_interval = c->lens_interval;
+    ++p->generation;
+    c->peer_generation = c->generation;
+  }
+  return CTRAJ_OK;
+}
+
+int ctraj_run_batch(ctraj_context* c, const ctraj_run_args* a, int32_t n_runs, ctraj_run_stats* stats,
+                    uint64_t l2_flush_bytes) {
+  if (!c) return fail(CTRAJ_EINVAL, "ctx is NULL");
+  if (n_runs < 0 || (n_runs > 0 && !a)) return fail(CTRAJ_EINVAL, "bad batch (n_runs %d)", n_runs);
+  if (l2_flush_bytes > (uint64_t(1) << 34)) return fail(CTRAJ_EINVAL, "l2_flush_bytes above 16 GiB");
+  if (n_runs == 0) return CTRAJ_OK;
+  CT_CUDA(cudaSetDevice(c->device));
+  BatchLane lanes[2];
+  if (n_runs == 1) {
+    batch_lane(c, a, 1, 0, stats, l2_flush_bytes, &lanes[0]);
+  } else {
+    int st = batch_peer(c);
+    if (st) return st;
+    if (!c->batch_ev) CT_CUDA(cudaEventCreateWithFlags(&c->batch_ev, cudaEventDisableTiming));
+    if (!c->peer->batch_ev) CT_CUDA(cudaEventCreateWithFlags(&c->peer->batch_ev, cudaEventDisableTiming));
+    // the batch starts after the work already queued on ctx's stream
+    CT_CUDA(cudaEventRecord(c->batch_ev, c->stream));
+    CT_CUDA(cudaStreamWaitEvent(c->peer->stream, c->batch_ev, 0));
+    bool threaded = true;
+    std::thread second;
+    try {
+      second = std::thread(batch_lane, c->peer, a, n_runs, 1, stats, l2_flush_bytes, &lanes[1]);
+    } catch (const std::system_error&) {
+      threaded = false;  // no thread to be had: the lanes run one after the other
+    }
+    batch_lane(c, a, n_runs, 0, stats, l2_flush_bytes, &lanes[0]);
+    if (threaded) second.join();
+    else batch_lane(c->peer, a, n_runs, 1, stats, l2_flush_bytes, &lanes[1]);
+    // and later work on ctx's stream after all of it
+    CT_CUDA(cudaEventRecord(c->peer->batch_ev, c->peer->stream));
+    CT_CUDA(cudaStreamWaitEvent(c->stream, c->peer->batch_ev, 0));
+  }
+  const BatchLane* bad = nullptr;
+  for (const BatchLane& l : lanes)
+    if (l.status && (!bad || l.run < bad->run)) bad = &l;
+  if (bad) return fail(bad->status, "batch run %d: %s", bad->run, bad->error.c_str());
+  return CTRAJ_OK;
 }
 
 int ctraj_plane(ctraj_context* c, const ctraj_run_args* a, const int64_t* ids, int64_t n_ids, double z_plane,

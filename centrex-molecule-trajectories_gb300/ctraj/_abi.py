@@ -238,6 +238,8 @@ SIGNATURES = {
     "ctraj_set_beamline": (ctypes.c_int, [_P, ctypes.POINTER(Element), ctypes.c_int32, ctypes.c_int32]),
     "ctraj_set_force_table": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(ForceTable)]),
     "ctraj_run": (ctypes.c_int, [_P, ctypes.POINTER(RunArgs), ctypes.POINTER(RunStats)]),
+    "ctraj_run_batch": (ctypes.c_int, [_P, ctypes.POINTER(RunArgs), ctypes.c_int32, ctypes.POINTER(RunStats),
+                                       ctypes.c_uint64]),
     "ctraj_record": (ctypes.c_int, [_P, ctypes.POINTER(RunArgs), _P, ctypes.c_int64, ctypes.c_int32,
                                     ctypes.c_int32, _P, _P]),
     "ctraj_run_sweep": (ctypes.c_int, [_P, ctypes.POINTER(Sweep), ctypes.POINTER(RunArgs), _P,

@@ -226,6 +226,48 @@ class Engine:
                          edge_band=st.edge_band, table_range=st.table_range, kernels=st.kernels,
                          label=label, final=final, rows=rows, margin=margin, extra=res_extra)
 
+    def run_batch(self, cb: CompiledBeamline, n: int, seeds, precision: int = 32, ics=None, xdist=None,
+                  vdist=None, offset: int = 0, g: float = G, timing: bool = False,
+                  l2_flush_bytes: int = 0) -> list:
+        """ctraj_run_batch: one run per entry of ``seeds`` (with device draws) or
+        of ``ics`` (a list of (6, n) arrays or tensors), pipelined over two
+        lanes; result k equals ``run(cb, n, seed=seeds[k], ...)``."""
+        self.load(cb)
+        if ics is not None:
+            ics_list = list(ics)
+            seeds = list(seeds) if seeds is not None else [0] * len(ics_list)
+            if len(seeds) != len(ics_list):
+                raise ValueError("seeds and ics must have the same length")
+        else:
+            seeds = list(seeds)
+            ics_list = [None] * len(seeds)
+        n_runs = len(seeds)
+        nl = len(cb.labels)
+        args = (_abi.RunArgs * max(n_runs, 1))()
+        stats = (_abi.RunStats * max(n_runs, 1))()
+        counts = [np.zeros(nl + 1, np.int64) for _ in range(n_runs)]
+        keep = []
+        for k in range(n_runs):
+            a, kk = self._args(n, precision, ics_list[k], xdist, vdist, seeds[k], offset, g)
+            a.timing = 1 if timing else 0
+            a.counts = counts[k].ctypes.data
+            args[k] = a
+            keep.append(kk)
+        status = self.lib.ctraj_run_batch(self.ctx, args, n_runs, stats, int(l2_flush_bytes))
+        del keep
+        _abi.check(status, self.lib)
+        out = []
+        for k in range(n_runs):
+            st = stats[k]
+            extra = {"max_lens_steps": int(st.max_lens_steps)}
+            if st.timed:
+                extra.update(front_ms=float(st.front_ms), lens_ms=float(st.lens_ms))
+            out.append(RunResult(counts=counts[k], labels=list(cb.labels), molecules=st.molecules,
+                                 molecule_steps=st.molecule_steps, lens_steps=st.lens_steps,
+                                 edge_band=st.edge_band, table_range=st.table_range, kernels=st.kernels,
+                                 extra=extra))
+        return out
+
     def plane(self, cb: CompiledBeamline, n: int, ids, z: float, precision: int = 32, ics=None, xdist=None,
               vdist=None, seed: int = 0, offset: int = 0, g: float = G) -> np.ndarray:
         """ctraj_plane: (len(ids), 8) x, y, z, vx, vy, vz, status, 0 of molecules `ids` of a run

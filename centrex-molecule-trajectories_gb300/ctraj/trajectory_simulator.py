@@ -162,6 +162,50 @@ class TrajectorySimulator:
         self.result = SimulationResult(self.counter, beamline, xdist, vdist, molecules, replay)
         self.results[run_name] = SimulationResult(self.counter, beamline, xdist, vdist, molecules, replay)
 
+    def run_simulations(self, beamline, run_names, vdist=CeNTREXVelocityDistribution(),
+                        xdist=CeNTREXPositionDistribution(), N_traj: int = 1000, n_jobs=1, *,
+                        seeds=None, precision: int | None = None, g: float = G):
+        """The caller's loop ``for name in run_names: run_simulation(beamline,
+        name, ...)`` as one call: every batch of N_traj molecules is its own run
+        (own seed, own Counter under results[name]), and the runs are pipelined
+        on the device (ctraj_run_batch), so one batch's ballistic front overlaps
+        the previous batch's lens pass.  Trajectories are not kept
+        (apertures_of_interest empty); last_runs holds the per-batch RunResults
+        and last_run the last one."""
+        names = list(run_names)
+        n = simulated_count(N_traj, n_jobs)
+        prec = precision or self.precision
+        if seeds is None:
+            seeds = [int.from_bytes(os.urandom(8), "little") for _ in names]
+        seeds = list(seeds)
+        if len(seeds) != len(names):
+            raise ValueError("one seed per run name")
+        cb = compile_beamline(beamline)
+        eng = default_engine(self.device)
+        xs, vs = device_spec(xdist, "position"), device_spec(vdist, "velocity")
+        ics = None
+        if (xs is None or vs is None) and n > 0:
+            n_loops = 100 * n_jobs
+            per = n // n_loops
+            ics = []
+            for _ in names:
+                chunks = []
+                for _ in range(n_loops):
+                    v = np.asarray(vdist.draw(per), dtype=np.float64).reshape(3, per)
+                    x = np.asarray(xdist.draw(per), dtype=np.float64).reshape(3, per)
+                    chunks.append(np.vstack((x, v)))
+                ics.append(np.ascontiguousarray(np.hstack(chunks)))
+        runs = eng.run_batch(cb, n, seeds, precision=prec, ics=ics, xdist=xs, vdist=vs, g=g)
+        self.last_runs = runs
+        for k, (name, res) in enumerate(zip(names, runs)):
+            self.last_run = res
+            self.counter = Counter()
+            self.counter.counter_dict = res.counter_dict()
+            replay = dict(device=self.device, cb=cb, n=n, precision=prec, ics=None if ics is None else ics[k],
+                          xdist=xs, vdist=vs, seed=seeds[k], g=g, ids=np.zeros(0, np.int64))
+            self.result = SimulationResult(self.counter, beamline, xdist, vdist, [], replay)
+            self.results[name] = self.result
+
     @staticmethod
     def _max_rows(cb, beamline, vz) -> int:
         """Trajectory rows a molecule can need (Trajectory.__init__, molecule.py:115-128)."""

@@ -279,6 +279,25 @@ int ctraj_run(ctraj_context* ctx, const ctraj_run_args* args,
               ctraj_run_stats* stats);
 
 /*
+ * n_runs independent runs, each exactly as ctraj_run(ctx, &args[k], &stats[k])
+ * (same counts, stats and outputs), pipelined over two lanes: runs 0, 2, 4, ...
+ * on ctx, runs 1, 3, 5, ... on a second context the call keeps inside ctx
+ * (same device and beamline, tables and tuning copied from ctx, its own
+ * stream, queues and events), each lane driven by its own host thread.  The
+ * ballistic front of one lane's run overlaps the other lane's lens pass,
+ * whose last molecules leave most SMs idle.  Replaces the caller's loop of one
+ * run_simulation per batch of molecules.  Work already queued on ctx's stream
+ * is ordered before the batch, and everything the batch does is ordered before
+ * later work on ctx's stream.  l2_flush_bytes > 0 writes a context-owned
+ * scratch buffer of that many bytes on the lane's stream before each run
+ * (benchmarks: no run finds the previous run's data in L2).  stats may be
+ * NULL.  Returns the status of the first run (by index) that failed; later
+ * runs of the other lane may have completed.
+ */
+int ctraj_run_batch(ctraj_context* ctx, const ctraj_run_args* args, int32_t n_runs,
+                    ctraj_run_stats* stats, uint64_t l2_flush_bytes);
+
+/*
  * Trajectory recording (trajectory_simulator.py:75-76 keeps full Trajectory
  * objects, molecule.py:111-167).  Re-propagates the molecules whose indices
  * are in ids (same ICs as the run that produced them: same seed/offset or the
