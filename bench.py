@@ -95,11 +95,12 @@ def parse():
     p.add_argument("--no-adjoint", action="store_true", help="skip the gradient measurement")
     p.add_argument("--no-large", action="store_true", help="skip the 1e9-molecule streamed run and the Adam tuning")
     p.add_argument("--profile", nargs="?", const="lens", default=None,
-                   choices=["lens", "sweep", "adjoint", "ring"],
+                   choices=["lens", "sweep", "adjoint", "ring", "batch"],
                    help="only run one workload --steps times with the default launch knobs (the commands "
                         "the ncu captures under profiles/ use): the lens beamline (--molecules), the "
                         "batched sweep (counts scaled by --sweep-scale), the gradient at 1e6 molecules, "
-                        "or a ring-recording run (--molecules)")
+                        "a ring-recording run (--molecules), or (batch) --steps lens-beamline runs as one "
+                        "pipelined ctraj_run_batch")
     p.add_argument("--sweep-scale", type=float, default=1.0, help="molecule counts of --profile sweep x this")
     p.add_argument("--lens-mode", choices=["persistent", "chunked"], default="persistent",
                    help="--profile lens/sweep: the FP32 lens pass to run (ctraj_tuning.lens_mode)")
@@ -139,6 +140,12 @@ def run_profile(args):
             prob = SoftProblem.from_beamline(lens_beamline(), n=1_000_000, aperture="A1", seed=k)
             o = soft_transmission(prob, prob.initial_params(), engine=eng, timing=True)
             out = {"loss": o.loss, "grad": o.grad.tolist(), "kernels": o.kernels, **o.extra}
+        elif args.profile == "batch":  # the headline: --steps runs as one pipelined batch
+            rs = eng.run_batch(cb, n, list(range(args.steps)), xdist=xs, vdist=vs)
+            for j, r in enumerate(rs):
+                print(json.dumps({"run": j, "profile": "batch", "kernels": r.kernels,
+                                  "molecule_steps": r.molecule_steps, "counts": r.counter_dict()}), flush=True)
+            break
         else:
             ring = None
             if args.profile == "ring":
