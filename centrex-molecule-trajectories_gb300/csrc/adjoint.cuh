@@ -307,11 +307,17 @@ __device__ __forceinline__ void soft_poly(const SoftK<T>& C, const Coef4<T>* tab
   const T r2 = fma_(py, py, mul_(px, px));
   const T s = fma_(C.beta, r2, C.neg_s0);
   // interval index, clamped (the end pieces extrapolate): truncation to
-  // unsigned sends s < 0 and NaN to 0, one conversion and a min on the
-  // step-to-step dependency chain (a compare-and-select clamp doubled the
-  // step's latency)
-  const unsigned i = min(to_uint_rz(s), unsigned(C.n_int - 1));
-  const T u = add_(s, -T(i));
+  // unsigned sends s < 0 and NaN to 0; in FP32 the same index and offset come
+  // from table_interval without the conversion unit (a compare-and-select
+  // clamp doubled the step's latency; max / min instructions do not)
+  unsigned i;
+  T u;
+  if constexpr (std::is_same<T, float>::value) {
+    table_interval(s, unsigned(C.n_int - 1), __int2float_rn(C.n_int - 1), i, u);
+  } else {
+    i = min(to_uint_rz(s), unsigned(C.n_int - 1));
+    u = add_(s, -T(i));
+  }
   const Coef4<T> q = tab[i];
   P = fma_(u, fma_(u, q.q2, q.q1), q.q0);
   Pp = fma_(mul_(T(2), u), q.q2, q.q1);

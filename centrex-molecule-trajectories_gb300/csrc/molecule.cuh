@@ -205,6 +205,25 @@ __device__ inline int mesh_nearest32(const LensF& L, const ElemF& f, float px, f
 }
 
 // ---------------------------------------------------------------------------
+// FP32 table interval: i = min(trunc_to_unsigned(s), last) and u = s - i, as
+// the truncating float-to-unsigned conversion and its inverse give them
+// (negative and NaN s -> interval 0; u keeps s's own offset), without the
+// conversion unit: 2^23 + max(s, 0) rounded toward -inf is 2^23 + floor(s)
+// for s < 2^23 (the spacing of floats in [2^23, 2^24) is 1), so floor(s)
+// sits in the low mantissa bits and 2^23 subtracts back exactly; larger s
+// and infinity land on the clamp.  Bit-identical to the conversions, on
+// FP32 / integer pipes instead of the conversion pipe.  The soft-transmission
+// kernels use it (their step is 4 % faster with it); the lens kernels keep
+// the conversions, which measured as fast or faster there.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void table_interval(const float s, const unsigned last, const float last_f,
+                                               unsigned& i, float& u) {
+  const float t = __fadd_rd(fmaxf(s, 0.0f), 8388608.0f);
+  i = min(__float_as_uint(t) - 0x4B000000u, last);
+  u = __fadd_rn(s, -fminf(__fadd_rn(t, -8388608.0f), last_f));
+}
+
+// ---------------------------------------------------------------------------
 // FP32 force: w such that a_perp = w * (x, y)
 // ---------------------------------------------------------------------------
 // kStaged: the whole table is in shared memory (s_tab); otherwise it is read
