@@ -60,13 +60,14 @@ FLOP_PER_BALLISTIC_STEP = 12
 # profiles/k_lens_persist_lens_beamline_1e7.md (the queue is read once; the
 # table and the molecule state stay on chip)
 LENS_DRAM_BYTES_PER_RUN = 10.9e6
-# Shared-memory wavefronts per warp table lookup (one LDS.128 per lane, random
-# intervals: ~2.3 bank-conflicted wavefronts in each of the 4 eight-lane
-# phases), from l1tex__data_pipe_lsu_wavefronts_mem_shared_op_ld of the same
-# capture: 1.91e8 wavefronts for 1.43e8 lane-steps x 4 lookups at 27.2 lanes
-# per warp instruction.  One wavefront per cycle per SM is the roof for the
-# throughput-bound phases of a lens pass.
-SHARED_WAVEFRONTS_PER_LOOKUP = 9.1
+# Shared-memory wavefronts per warp table lookup (the bench table goes to the
+# kernels in the 8-byte linear form: one LDS.64 per lane, random intervals,
+# bank-conflicted), from l1tex__data_pipe_lsu_wavefronts_mem_shared_op_ld of the
+# k_lens_persist capture in profiles/k_lens_persist_lens_beamline_1e7.md:
+# 1.14e8 wavefronts for 1.43e8 lane-steps x 4 lookups at 27.15 lanes per warp
+# instruction (the 16-byte quadratic form took 9.1).  One wavefront per cycle
+# per SM is the roof for the throughput-bound phases of a lens pass.
+SHARED_WAVEFRONTS_PER_LOOKUP = 5.4
 LOOKUPS_PER_RK4_STEP = 4
 
 
@@ -280,8 +281,8 @@ def fp32_peak(device: int):
 
 def step_probe(device: int, bl):
     """The production FP32 lens step in a loop: cycles per step of a lone warp
-    (latency floor) and lane-steps/s at 2 x 512 threads per SM (throughput
-    without queue, compaction or loss effects)."""
+    (latency floor) and lane-steps/s at 512 threads per SM, as the persistent
+    lens pass runs (throughput without queue, compaction or loss effects)."""
     import numpy as np
     import torch
 
@@ -291,10 +292,14 @@ def step_probe(device: int, bl):
     F = lens.a_interp
     h = (F.knots[-1] - F.knots[0]) / (len(F.knots) - 1)
     kappa = 2.0 * F.alpha / F.mass
-    q = np.zeros((len(F.coef), 4), np.float32)
-    q[:, 0] = -kappa * F.coef[:, 2]
-    q[:, 1] = -kappa * 2.0 * F.coef[:, 1] * h
-    q[:, 2] = -kappa * 3.0 * F.coef[:, 0] * h * h
+    # the lens kernels' layout for this table (kForceStark2Lin): per knot
+    # interval four linear quarter-interval pieces (w, dw) in two float4
+    a = -kappa * F.coef[:, 2]
+    b = -kappa * 2.0 * F.coef[:, 1] * h
+    c = -kappa * 3.0 * F.coef[:, 0] * h * h
+    w = [a + (k / 4) * (b + (k / 4) * c) for k in range(5)]
+    pieces = np.stack([x for k in range(4) for x in (w[k], w[k + 1] - w[k])], axis=1)  # (n_int, 8)
+    q = np.ascontiguousarray(pieces.astype(np.float32).reshape(-1, 4))  # 2 float4 per interval
     qd = torch.from_numpy(q).to(f"cuda:{device}")
     lib = ctypes.CDLL(str(PEAK_OUT))
     lib.ctraj_peak_step.restype = ctypes.c_int
@@ -302,9 +307,9 @@ def step_probe(device: int, bl):
                                     ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     sms = torch.cuda.get_device_properties(device).multi_processor_count
     out = {}
-    for key, blocks, threads in (("one_warp", 1, 32), ("full", 2 * sms, 512)):
+    for key, blocks, threads in (("one_warp", 1, 32), ("full", sms, 512)):
         cyc, lps = ctypes.c_double(), ctypes.c_double()
-        rc = lib.ctraj_peak_step(ctypes.c_void_p(qd.data_ptr()), len(q), ctypes.c_float(F.alpha / h), 4096,
+        rc = lib.ctraj_peak_step(ctypes.c_void_p(qd.data_ptr()), len(q), ctypes.c_float(4.0 * F.alpha / h), 4096,
                                  blocks, threads, ctypes.byref(cyc), ctypes.byref(lps))
         out[key] = (cyc.value, lps.value) if rc == 0 else (None, None)
     return {"one_warp_cycles_per_step": out["one_warp"][0],

@@ -153,6 +153,9 @@ namespace {
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 constexpr int kMaxStagedIntervals = 6144;  // 96 KiB of float4 per CTA
+// a kForceStark2Lin table (two float4 of pieces per knot interval) is staged
+// up to 128 KiB: with the persistent pass's 40 KiB of swap slots one CTA per SM
+constexpr int kMaxStagedLinear = 8192;
 constexpr int kMaxChunks = 16384;          // lens chunks per lens (CTRAJ_MAX_LENS_STEPS / 1024 < this)
 
 // Queue layout inside one buffer of capacity cap (SoA, each array 256-byte
@@ -191,9 +194,54 @@ size_t queue_bytes(size_t cap, int precision, bool with_cfg = false) {
   return layout_queue(nullptr, cap, precision, nullptr, nullptr, with_cfg);
 }
 
+// FP32 Stark tables of field order 2 reach the lens kernels as linear pieces
+// on quarter intervals (kForceStark2Lin: one 8-byte lookup instead of a
+// 16-byte quadratic) when both hold:
+//  * accuracy: linear interpolation of the quadratic w(u) = a + b u + c u^2
+//    of an interval over its quarters departs from it by at most |c| / 64;
+//    that must stay below kLinearTolerance of the largest |w| (the 4096-knot
+//    hexapole table: 4.0e-7);
+//  * coverage: the table starts at or below |E| = 0 and reaches |E| at
+//    kLinearCover times the bore radius, so a molecule inside the bore (and
+//    every RK4 stage point of its next step) looks up inside the table, where
+//    the quadratic form would need no extrapolation either; beyond the last
+//    knot a piece extrapolates linearly;
+// and the pieces (2 float4 per interval) fit the 128 KiB staging limit.
+// Otherwise the 16-byte quadratic (kForceStark2), exact per interval.
+constexpr double kLinearTolerance = 1e-6;
+constexpr double kLinearCover = 1.2;
+constexpr int kLinearPieces = 4;  // per knot interval
+
+bool stark_linear(int kind, int n_knots, const double* knots, const double* coef, const ctraj_element& e) {
+  if (kind != CTRAJ_TABLE_STARK_SPLINE || e.field_order != 2 || n_knots < 2) return false;
+  const int n_int = n_knots - 1;
+  if (2 * n_int > kMaxStagedLinear) return false;
+  const double h = (knots[n_int] - knots[0]) / double(n_int), alpha = e.p[6];
+  const double rc = 0.5 * e.p[0] * kLinearCover;
+  if (!(alpha >= 0.0) || !(knots[0] <= 0.0) || !(alpha * rc * rc <= knots[n_int])) return false;
+  double cmax = 0.0, wmax = 0.0;
+  for (int j = 0; j < n_int; ++j) {
+    const double* cj = coef + size_t(j) * 4;
+    const double a = cj[2], b = 2.0 * cj[1] * h, c = 3.0 * cj[0] * h * h;
+    cmax = std::max(cmax, std::fabs(c));
+    wmax = std::max(wmax, std::max(std::fabs(a), std::fabs(a + b + c)));
+  }
+  return std::isfinite(cmax) && cmax / double(4 * kLinearPieces * kLinearPieces) <= kLinearTolerance * wmax;
+}
+
+// Float4 `half` (0 or 1) of a kForceStark2Lin knot interval: the quadratic
+// a + b u + c u^2 (u in [0, 1]) as linear pieces over the quarters, each
+// (w at the piece's start, its rise across it), two pieces per float4.
+float4 stark_pieces(double a, double b, double c, int half) {
+  auto w = [&](int k) { const double u = 0.25 * k; return a + u * (b + u * c); };
+  const int k = 2 * half;
+  return make_float4(float(w(k)), float(w(k + 1) - w(k)), float(w(k + 1)), float(w(k + 2) - w(k + 1)));
+}
+
 int lens_force_kind(const ctraj_context* c, const ctraj_element& e) {
   const HostTable& t = c->tables[e.table];
   if (t.kind == CTRAJ_TABLE_RADIAL_LINEAR) return kForceRadial;
+  if (stark_linear(t.kind, t.n, t.knots.data(), t.coef.data(), e)) return kForceStark2Lin;
   return e.field_order == 1 ? kForceStark1 : kForceStark2;
 }
 
@@ -218,8 +266,9 @@ int build_lens_tables(ctraj_context* c) {
     const HostTable& t = c->tables[e.table];
     const double x0 = t.knots[0], h = (t.knots[t.n - 1] - t.knots[0]) / double(t.n - 1);
     const int n_int = t.n - 1;
+    const bool lin = lens_force_kind(c, e) == kForceStark2Lin;
     c->lens_offset[i] = host.size();
-    c->lens_n_int[i] = n_int;
+    c->lens_n_int[i] = lin ? 2 * n_int : n_int;  // float4 entries
     (void)x0;
     if (t.kind == CTRAJ_TABLE_RADIAL_LINEAR) {
       for (int j = 0; j < n_int; ++j)
@@ -229,12 +278,19 @@ int build_lens_tables(ctraj_context* c) {
       const double kappa = e.field_order == 1 ? alpha / mass : 2.0 * alpha / mass;
       for (int j = 0; j < n_int; ++j) {
         const double* cj = &t.coef[size_t(j) * 4];
-        host.push_back(make_float4(float(-kappa * cj[2]), float(-kappa * 2.0 * cj[1] * h),
-                                   float(-kappa * 3.0 * cj[0] * h * h), 0.f));
+        const double qa = -kappa * cj[2], qb = -kappa * 2.0 * cj[1] * h, qc = -kappa * 3.0 * cj[0] * h * h;
+        if (lin) {
+          host.push_back(stark_pieces(qa, qb, qc, 0));
+          host.push_back(stark_pieces(qa, qb, qc, 1));
+        } else {
+          host.push_back(make_float4(float(qa), float(qb), float(qc), 0.f));
+        }
       }
     }
     // the whole table goes to shared memory when it takes at most 96 KiB
-    c->lens_n_smem[i] = n_int <= kMaxStagedIntervals ? n_int : 0;
+    // (128 KiB in the linear form)
+    const int entries = c->lens_n_int[i];
+    c->lens_n_smem[i] = entries <= (lin ? kMaxStagedLinear : kMaxStagedIntervals) ? entries : 0;
   }
   if (!host.empty()) {
     int st = c->lens_tables.ensure(host.size() * sizeof(float4));
@@ -319,8 +375,9 @@ int build_plan(ctraj_context* c, const ctraj_run_args* a, Plan& P) {
         L.s0 = float(x0 / h);
         L.r_max = float(t.knots[t.n - 1]);
       } else {
-        L.beta = float(e.p[6] / h);
-        L.s0 = float(x0 / h);
+        const double scale = L.force == kForceStark2Lin ? double(kLinearPieces) : 1.0;  // pieces
+        L.beta = float(scale * e.p[6] / h);
+        L.s0 = float(scale * x0 / h);
         L.r_max = INFINITY;
       }
     }
@@ -378,6 +435,7 @@ LensKernel lens_kernel32(int force) {
   using M = Mol32<kOut, false>;
   switch (force) {
     case kForceStark2: return k_lens_chunk<M, kOut, kForceStark2, false, kStaged, false, kRing>;
+    case kForceStark2Lin: return k_lens_chunk<M, kOut, kForceStark2Lin, false, kStaged, false, kRing>;
     case kForceStark1: return k_lens_chunk<M, kOut, kForceStark1, false, kStaged, false, kRing>;
     default: return k_lens_chunk<M, kOut, kForceRadial, false, kStaged, false, kRing>;
   }
@@ -407,6 +465,10 @@ int enqueue_persistent(const Plan& P, const RunDev& R, int i, const Queue& Qin, 
     case kForceStark2:
       k = staged ? k_lens_persist<M, kOut, kForceStark2, true, kRing>
                  : k_lens_persist<M, kOut, kForceStark2, false, kRing>;
+      break;
+    case kForceStark2Lin:
+      k = staged ? k_lens_persist<M, kOut, kForceStark2Lin, true, kRing>
+                 : k_lens_persist<M, kOut, kForceStark2Lin, false, kRing>;
       break;
     case kForceStark1:
       k = staged ? k_lens_persist<M, kOut, kForceStark1, true, kRing>
@@ -1919,21 +1981,24 @@ int noalloc_plan(const ctraj_element* el, int n_el, int n_labels, const ctraj_fo
       return fail(CTRAJ_EINVAL, "lens element %d: field_order must be 1 or 2", i);
     if (P.first_lens == n_el) P.first_lens = i;
     const int n_int = t.n_knots - 1;
-    if (offset + size_t(n_int) > size_t(CTRAJ_NOALLOC_MAX_INTERVALS))
-      return fail(CTRAJ_EINVAL, "lens tables exceed %d intervals", CTRAJ_NOALLOC_MAX_INTERVALS);
+    const bool lin = stark_linear(t.kind, t.n_knots, t.knots, t.coef, e);
+    const int entries = lin ? 2 * n_int : n_int;  // float4
+    if (offset + size_t(entries) > size_t(CTRAJ_NOALLOC_MAX_INTERVALS))
+      return fail(CTRAJ_EINVAL, "lens tables exceed %d entries", CTRAJ_NOALLOC_MAX_INTERVALS);
     const double x0 = t.knots[0], h = (t.knots[t.n_knots - 1] - t.knots[0]) / double(n_int);
     const double alpha = e.p[6], mass = e.p[5];
     const double kappa = e.field_order == 1 ? alpha / mass : 2.0 * alpha / mass;
-    for (int j0 = 0; j0 < n_int; j0 += 256) {
-      const int m = std::min(256, n_int - j0);
+    for (int j0 = 0; j0 < entries; j0 += 256) {
+      const int m = std::min(256, entries - j0);
       for (int j = 0; j < m; ++j) {
         const int k = j0 + j;
         if (t.kind == CTRAJ_TABLE_RADIAL_LINEAR) {
           buf[j] = make_float4(float(t.values[k]), float(t.values[k + 1] - t.values[k]), 0.f, 0.f);
         } else {
-          const double* ck = &t.coef[size_t(k) * 4];
-          buf[j] = make_float4(float(-kappa * ck[2]), float(-kappa * 2.0 * ck[1] * h),
-                               float(-kappa * 3.0 * ck[0] * h * h), 0.f);
+          const int iv = lin ? k / 2 : k;
+          const double* ck = &t.coef[size_t(iv) * 4];
+          const double qa = -kappa * ck[2], qb = -kappa * 2.0 * ck[1] * h, qc = -kappa * 3.0 * ck[0] * h * h;
+          buf[j] = lin ? stark_pieces(qa, qb, qc, k % 2) : make_float4(float(qa), float(qb), float(qc), 0.f);
         }
       }
       // pageable source: the call returns once buf has been staged, so buf can be refilled
@@ -1941,20 +2006,21 @@ int noalloc_plan(const ctraj_element* el, int n_el, int n_labels, const ctraj_fo
     }
     LensF& L = P.lf[i];
     L.q = dev_tables + offset;
-    L.n_int = n_int;
-    L.n_smem = n_int <= kMaxStagedIntervals ? n_int : 0;
+    L.n_int = entries;
+    L.n_smem = entries <= (lin ? kMaxStagedLinear : kMaxStagedIntervals) ? entries : 0;
     if (t.kind == CTRAJ_TABLE_RADIAL_LINEAR) {
       L.force = kForceRadial;
       L.beta = float(1.0 / h);
       L.s0 = float(x0 / h);
       L.r_max = float(t.knots[t.n_knots - 1]);
     } else {
-      L.force = e.field_order == 1 ? kForceStark1 : kForceStark2;
-      L.beta = float(alpha / h);
-      L.s0 = float(x0 / h);
+      L.force = lin ? kForceStark2Lin : (e.field_order == 1 ? kForceStark1 : kForceStark2);
+      const double scale = lin ? double(kLinearPieces) : 1.0;  // pieces
+      L.beta = float(scale * alpha / h);
+      L.s0 = float(scale * x0 / h);
       L.r_max = INFINITY;
     }
-    offset += size_t(n_int);
+    offset += size_t(entries);
   }
   return CTRAJ_OK;
 }

@@ -984,6 +984,8 @@ __device__ __forceinline__ bool step_any(M& m, const Plan& P, int li, const floa
   switch (P.lf[li].force) {
     case kForceStark2:
       return m.template lens_step<kForceStark2, false>(L, dt, hdt, c2, dt6, dt26, nullptr, flags);
+    case kForceStark2Lin:
+      return m.template lens_step<kForceStark2Lin, false>(L, dt, hdt, c2, dt6, dt26, nullptr, flags);
     case kForceStark1:
       return m.template lens_step<kForceStark1, false>(L, dt, hdt, c2, dt6, dt26, nullptr, flags);
     default:

@@ -235,6 +235,16 @@ template <int F, bool kStaged>
 __device__ __forceinline__ float wforce(float px, float py, const LensArgs& L, const float4* s_tab,
                                         unsigned& flags, const float beta) {
   const float r2 = __fmaf_rn(py, py, __fmul_rn(px, px));
+  if (F == kForceStark2Lin) {
+    // one 8-byte lookup: ~6 bank-conflicted shared-memory wavefronts per warp
+    // instead of ~9 for the 16-byte quadratic entry
+    const float s = __fmaf_rn(beta, r2, -L.s0);
+    const unsigned i = min(__float2uint_rz(s), unsigned(2 * L.n_int - 1));
+    const float u = __fadd_rn(s, -__uint2float_rn(i));
+    const float2 q = kStaged ? reinterpret_cast<const float2*>(s_tab)[i]
+                             : __ldg(reinterpret_cast<const float2*>(L.q) + i);
+    return __fmaf_rn(u, q.y, q.x);
+  }
   float s, r = 0.0f;
   if (F == kForceStark2) {
     s = __fmaf_rn(beta, r2, -L.s0);

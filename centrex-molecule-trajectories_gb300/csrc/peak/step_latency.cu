@@ -33,7 +33,7 @@ __global__ void __launch_bounds__(512) k_step_loop(LensArgs L, int steps, float 
   int lost = 0;
   const long long t0 = clock64();
   for (int n = 0; n < steps; ++n)
-    lost += m.template lens_step<ctraj::kForceStark2, true>(L, dt, hdt, dt, dt6, dt26, s_tab, flags);
+    lost += m.template lens_step<ctraj::kForceStark2Lin, true>(L, dt, hdt, dt, dt6, dt26, s_tab, flags);
   const long long t1 = clock64();
   if (threadIdx.x == 0) cyc[blockIdx.x] = t1 - t0;
   out[blockIdx.x * blockDim.x + threadIdx.x] = m.x + m.y + m.vx + m.vy + float(lost + int(flags));
@@ -41,11 +41,12 @@ __global__ void __launch_bounds__(512) k_step_loop(LensArgs L, int steps, float 
 
 }  // namespace
 
-// q: FP32 table (n_int float4, the lens kernel's layout) in device memory.
+// q: FP32 Stark table in the lens kernels' linear layout (n_int float4 of two
+// (w, dw) quarter-interval pieces; beta counts quarter intervals) in device memory.
 // Returns 0 and the mean clock64 cycles per step and lane-steps per second.
 extern "C" int ctraj_peak_step(const void* q, int n_int, float beta, int steps, int blocks, int threads,
                                double* cycles_per_step, double* lane_steps_per_s) {
-  if (!q || n_int < 1 || n_int > 6144 || steps < 1 || blocks < 1 || threads < 32 || threads > 512) return -1;
+  if (!q || n_int < 1 || n_int > 8192 || steps < 1 || blocks < 1 || threads < 32 || threads > 512) return -1;
   LensArgs L{};
   L.q = static_cast<const float4*>(q);
   L.beta = beta;

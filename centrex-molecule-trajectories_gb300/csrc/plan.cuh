@@ -17,6 +17,11 @@ enum : int {
   kForceStark2 = 0,  // W(E) table, |E| = alpha r^2
   kForceStark1 = 1,  // W(E) table, |E| = alpha r
   kForceRadial = 2,  // a(r) linear table
+  // W(E) table, |E| = alpha r^2, whose derivative is tabulated as linear
+  // pieces on quarter intervals (float2 (w, dw) entries, two per float4;
+  // n_int counts the float4): chosen by the host when that is accurate and
+  // the table covers the bore
+  kForceStark2Lin = 3,
 };
 
 // FP32 constants of one element.
@@ -29,11 +34,13 @@ struct ElemF {
 
 // FP32 constants of one lens (indexed by element).
 struct LensF {
-  const float4* q;  // per interval: stark (q0, q1, q2, 0) scaled by -kappa; radial (y_j, y_{j+1}-y_j, 0, 0)
-  float beta;       // table coordinate s = beta * r^n - s0 (stark) or r * beta (radial, beta = 1/h)
+  const float4* q;  // per interval: stark (q0, q1, q2, 0) scaled by -kappa; stark2lin two float4
+                    // of two pieces (w, dw, w, dw) scaled by -kappa; radial (y_j, y_{j+1}-y_j, 0, 0)
+  float beta;       // table coordinate s = beta * r^n - s0 (stark; stark2lin in quarter intervals)
+                    // or r * beta (radial, beta = 1/h)
   float s0;
   float r_max;      // radial: last knot; lookups above it are errors
-  int n_int;        // intervals in the table
+  int n_int;        // float4 entries of the table (intervals; stark2lin 2 per interval)
   int n_smem;       // leading intervals staged in shared memory
   int force;        // kForce*
   int cols;         // honeycomb: q = cell centres (x, y, 0, 0), n_int = cells, cols = cells per row
