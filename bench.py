@@ -301,18 +301,26 @@ def step_probe(device: int, bl):
     pieces = np.stack([x for k in range(4) for x in (w[k], w[k + 1] - w[k])], axis=1)  # (n_int, 8)
     q = np.ascontiguousarray(pieces.astype(np.float32).reshape(-1, 4))  # 2 float4 per interval
     qd = torch.from_numpy(q).to(f"cuda:{device}")
+    # the exact quadratic form (kForceStark2), for the latency comparison
+    qq = np.zeros((len(F.coef), 4), np.float32)
+    qq[:, 0], qq[:, 1], qq[:, 2] = a, b, c
+    qqd = torch.from_numpy(qq).to(f"cuda:{device}")
     lib = ctypes.CDLL(str(PEAK_OUT))
     lib.ctraj_peak_step.restype = ctypes.c_int
     lib.ctraj_peak_step.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_int, ctypes.c_int,
-                                    ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+                                    ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                    ctypes.POINTER(ctypes.c_double)]
     sms = torch.cuda.get_device_properties(device).multi_processor_count
     out = {}
-    for key, blocks, threads in (("one_warp", 1, 32), ("full", sms, 512)):
+    runs = (("one_warp", qd, len(q), 4.0, 1, 1, 32), ("full", qd, len(q), 4.0, 1, sms, 512),
+            ("one_warp_quadratic", qqd, len(qq), 1.0, 0, 1, 32))
+    for key, table, n_int, scale, linear, blocks, threads in runs:
         cyc, lps = ctypes.c_double(), ctypes.c_double()
-        rc = lib.ctraj_peak_step(ctypes.c_void_p(qd.data_ptr()), len(q), ctypes.c_float(4.0 * F.alpha / h), 4096,
-                                 blocks, threads, ctypes.byref(cyc), ctypes.byref(lps))
+        rc = lib.ctraj_peak_step(ctypes.c_void_p(table.data_ptr()), n_int, ctypes.c_float(scale * F.alpha / h),
+                                 linear, 4096, blocks, threads, ctypes.byref(cyc), ctypes.byref(lps))
         out[key] = (cyc.value, lps.value) if rc == 0 else (None, None)
     return {"one_warp_cycles_per_step": out["one_warp"][0],
+            "one_warp_cycles_per_step_quadratic_table": out["one_warp_quadratic"][0],
             "isolated_lane_steps_per_s": out["full"][1],
             "isolated_tflops": None if out["full"][1] is None else out["full"][1] * FLOP_PER_RK4_STEP / 1e12}
 

@@ -969,6 +969,9 @@ static int run_impl(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* 
     stats->molecule_steps = int64_t(hs[kStatSteps]);
     stats->lens_steps = int64_t(hs[kStatLensSteps]);
     stats->max_lens_steps = int32_t(c->run_max_steps);
+    if (a->precision == 32)
+      for (int i = 0; i < P.n_el; ++i)
+        stats->linear_tables += P.el[i].type == CTRAJ_ELECTROSTATIC_LENS && P.lf[i].force == kForceStark2Lin;
     stats->edge_band = (a->precision == 64 || out) ? int64_t(hs[kStatEdgeBand]) : -1;
     stats->table_range = int64_t(hs[kStatTableRange]);
     stats->bad_steps = int64_t(hs[kStatBadSteps]);

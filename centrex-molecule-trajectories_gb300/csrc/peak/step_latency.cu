@@ -14,6 +14,7 @@ namespace {
 
 using ctraj::LensArgs;
 
+template <int F>
 __global__ void __launch_bounds__(512) k_step_loop(LensArgs L, int steps, float dt, long long* cyc,
                                                    float* out) {
   extern __shared__ float4 s_tab[];
@@ -33,7 +34,7 @@ __global__ void __launch_bounds__(512) k_step_loop(LensArgs L, int steps, float 
   int lost = 0;
   const long long t0 = clock64();
   for (int n = 0; n < steps; ++n)
-    lost += m.template lens_step<ctraj::kForceStark2Lin, true>(L, dt, hdt, dt, dt6, dt26, s_tab, flags);
+    lost += m.template lens_step<F, true>(L, dt, hdt, dt, dt6, dt26, s_tab, flags);
   const long long t1 = clock64();
   if (threadIdx.x == 0) cyc[blockIdx.x] = t1 - t0;
   out[blockIdx.x * blockDim.x + threadIdx.x] = m.x + m.y + m.vx + m.vy + float(lost + int(flags));
@@ -41,12 +42,15 @@ __global__ void __launch_bounds__(512) k_step_loop(LensArgs L, int steps, float 
 
 }  // namespace
 
-// q: FP32 Stark table in the lens kernels' linear layout (n_int float4 of two
-// (w, dw) quarter-interval pieces; beta counts quarter intervals) in device memory.
+// q: FP32 Stark table in device memory, in one of the lens kernels' layouts:
+// linear = 1: n_int float4 of two (w, dw) quarter-interval pieces, beta in
+// quarter intervals (kForceStark2Lin); linear = 0: one (a, b, c, 0) quadratic
+// per interval (kForceStark2).
 // Returns 0 and the mean clock64 cycles per step and lane-steps per second.
-extern "C" int ctraj_peak_step(const void* q, int n_int, float beta, int steps, int blocks, int threads,
-                               double* cycles_per_step, double* lane_steps_per_s) {
+extern "C" int ctraj_peak_step(const void* q, int n_int, float beta, int linear, int steps, int blocks,
+                               int threads, double* cycles_per_step, double* lane_steps_per_s) {
   if (!q || n_int < 1 || n_int > 8192 || steps < 1 || blocks < 1 || threads < 32 || threads > 512) return -1;
+  auto kernel = linear ? k_step_loop<ctraj::kForceStark2Lin> : k_step_loop<ctraj::kForceStark2>;
   LensArgs L{};
   L.q = static_cast<const float4*>(q);
   L.beta = beta;
@@ -65,15 +69,15 @@ extern "C" int ctraj_peak_step(const void* q, int n_int, float beta, int steps, 
     return -3;
   }
   const size_t smem = size_t(n_int) * sizeof(float4);
-  cudaFuncSetAttribute(k_step_loop, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   cudaStream_t s;
   cudaEvent_t e0, e1;
   cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  k_step_loop<<<blocks, threads, smem, s>>>(L, 32, 1e-6f, cyc, out);
+  kernel<<<blocks, threads, smem, s>>>(L, 32, 1e-6f, cyc, out);
   cudaEventRecord(e0, s);
-  k_step_loop<<<blocks, threads, smem, s>>>(L, steps, 1e-6f, cyc, out);
+  kernel<<<blocks, threads, smem, s>>>(L, steps, 1e-6f, cyc, out);
   cudaEventRecord(e1, s);
   cudaError_t err = cudaEventSynchronize(e1);
   float ms = 0.f;

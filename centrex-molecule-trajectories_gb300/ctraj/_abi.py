@@ -134,7 +134,7 @@ class RunStats(ctypes.Structure):
         ("front_ms", ctypes.c_float),
         ("lens_ms", ctypes.c_float),
         ("max_lens_steps", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("linear_tables", ctypes.c_int32),
     ]
 
 

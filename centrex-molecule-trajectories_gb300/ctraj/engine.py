@@ -219,6 +219,7 @@ class Engine:
         del keep
         _abi.check(status, self.lib)
         res_extra["max_lens_steps"] = int(st.max_lens_steps)
+        res_extra["linear_tables"] = int(st.linear_tables)
         if st.timed:
             res_extra.update(front_ms=float(st.front_ms), lens_ms=float(st.lens_ms))
         return RunResult(counts=counts, labels=list(cb.labels), molecules=st.molecules,
@@ -259,7 +260,7 @@ class Engine:
         out = []
         for k in range(n_runs):
             st = stats[k]
-            extra = {"max_lens_steps": int(st.max_lens_steps)}
+            extra = {"max_lens_steps": int(st.max_lens_steps), "linear_tables": int(st.linear_tables)}
             if st.timed:
                 extra.update(front_ms=float(st.front_ms), lens_ms=float(st.lens_ms))
             out.append(RunResult(counts=counts[k], labels=list(cb.labels), molecules=st.molecules,

@@ -216,7 +216,9 @@ typedef struct ctraj_run_stats {
                                molecule with the most steps in a lens
                                (rint(L/dz) + 2), the length of the lens pass's
                                critical path; 0 from the other entry points   */
-  int32_t reserved;
+  int32_t linear_tables;    /* ctraj_run: lens elements whose FP32 run used the
+                               8-byte linear form of their Stark table (the
+                               host's accuracy and coverage test passed)     */
 } ctraj_run_stats;
 
 /* ---- context -------------------------------------------------------------- */
@@ -504,7 +506,7 @@ int ctraj_soft_transmission(ctraj_context* ctx, const ctraj_soft_args* args,
  * the GPU (from two host threads, or on two streams) race: serialize them.
  */
 #define CTRAJ_NOALLOC_MAX_MOLECULES 131072
-#define CTRAJ_NOALLOC_MAX_INTERVALS 16384 /* FP32 table intervals over all lenses + honeycomb cells */
+#define CTRAJ_NOALLOC_MAX_INTERVALS 16384 /* FP32 table entries over all lenses (one per knot interval, two in the linear Stark form) + honeycomb cells */
 #define CTRAJ_NOALLOC_SCRATCH_BYTES (32u << 20)
 int ctraj_run_noalloc(const ctraj_element* elements, int32_t n_elements,
                       int32_t n_labels, const ctraj_force_table* tables,

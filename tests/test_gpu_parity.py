@@ -266,3 +266,16 @@ def test_results_do_not_depend_on_tuning(engine):
             engine.set_tuning(lens_interval=0)
     finally:
         engine.set_tuning()
+
+
+@pytest.mark.parametrize("case, linear", [("config1", 1), ("kat_lens", 0)])
+def test_stark_table_form(engine, case, linear):
+    """The 4096-knot hexapole table goes to the FP32 lens kernels as quarter-
+    interval linear pieces (accurate to 4e-7 of its largest force); the coarse
+    known-answer table (6.5e-6) keeps the exact quadratic.  Both are held to
+    the FP32 tolerance by test_fp32_within_tolerance; FP64 never uses pieces."""
+    fx = fixtures.load(case)
+    cb = compile_beamline(fixtures.build_beamline(fx))
+    n = fx["ics"].shape[1]
+    assert engine.run(cb, n, precision=32, ics=fx["ics"]).extra["linear_tables"] == linear
+    assert engine.run(cb, n, precision=64, ics=fx["ics"]).extra["linear_tables"] == 0
