@@ -213,8 +213,9 @@ __device__ inline int mesh_nearest32(const LensF& L, const ElemF& f, float px, f
 // sits in the low mantissa bits and 2^23 subtracts back exactly; larger s
 // and infinity land on the clamp.  Bit-identical to the conversions, on
 // FP32 / integer pipes instead of the conversion pipe.  The soft-transmission
-// kernels use it (their step is 4 % faster with it); the lens kernels keep
-// the conversions, which measured as fast or faster there.
+// kernels (4 % faster) and the linear-table lens lookups (one warp's step
+// 323 -> 231 cycles) use it; the quadratic-table lookups keep the
+// conversions, which measured as fast there.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void table_interval(const float s, const unsigned last, const float last_f,
                                                unsigned& i, float& u) {
@@ -239,8 +240,11 @@ __device__ __forceinline__ float wforce(float px, float py, const LensArgs& L, c
     // one 8-byte lookup: ~6 bank-conflicted shared-memory wavefronts per warp
     // instead of ~9 for the 16-byte quadratic entry
     const float s = __fmaf_rn(beta, r2, -L.s0);
-    const unsigned i = min(__float2uint_rz(s), unsigned(2 * L.n_int - 1));
-    const float u = __fadd_rn(s, -__uint2float_rn(i));
+    // (the interval without the conversion unit: one warp's RK4 step 231
+    // instead of 323 cycles, bit-identical)
+    unsigned i;
+    float u;
+    table_interval(s, unsigned(2 * L.n_int - 1), __int2float_rn(2 * L.n_int - 1), i, u);
     const float2 q = kStaged ? reinterpret_cast<const float2*>(s_tab)[i]
                              : __ldg(reinterpret_cast<const float2*>(L.q) + i);
     return __fmaf_rn(u, q.y, q.x);

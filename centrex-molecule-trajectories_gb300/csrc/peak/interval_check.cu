@@ -1,5 +1,5 @@
 // Check of the FP32 table-interval computation of the soft-transmission
-// kernels (table_interval in molecule.cuh) against the truncating float-to-unsigned
+// kernels and the linear-table lens lookups (table_interval in molecule.cuh) against the truncating float-to-unsigned
 // conversion and its inverse it replaces, over generated arguments: random
 // bit patterns (negative, NaN, infinite, subnormal and huge values), quarter
 // steps across the table and the neighbours of every integer.

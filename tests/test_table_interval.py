@@ -1,5 +1,6 @@
-"""The FP32 soft-transmission kernels locate a molecule's table interval
-without the float-to-integer conversion unit (table_interval in
+"""The FP32 soft-transmission kernels and the lens kernels' linear-table
+lookups locate a molecule's table interval without the float-to-integer
+conversion unit (table_interval in
 csrc/molecule.cuh); the interval and the offset in it must equal, bit for
 bit, what the truncating conversion and its inverse give, for every kind of
 argument."""
@@ -10,7 +11,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("last", [0, 15, 4094, 6143])
+@pytest.mark.parametrize("last", [0, 15, 4094, 6143, 16379])
 def test_table_interval_equals_the_conversions(last):
     from ctraj.build import build_peak_library
 
