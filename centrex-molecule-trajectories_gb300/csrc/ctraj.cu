@@ -1241,6 +1241,9 @@ std::vector<int> sweep_chunks(const ctraj_context* c, int64_t est) {
 
 LensKernel sweep_lens_kernel(int force, bool staged) {
   using M = Mol32<false, false>;
+  if (force == kForceStark2Lin)
+    return staged ? k_lens_chunk<M, false, kForceStark2Lin, false, true, true>
+                  : k_lens_chunk<M, false, kForceStark2Lin, false, false, true>;
   if (staged)
     return force == kForceStark1 ? k_lens_chunk<M, false, kForceStark1, false, true, true>
                                  : k_lens_chunk<M, false, kForceStark2, false, true, true>;
@@ -1257,6 +1260,8 @@ struct SweepLaunch {
   unsigned long long* result = nullptr;  // device: per-configuration counts | totals | stats
   size_t result_bytes = 0;
   bool persistent = false;               // one k_sweep_persist launch instead of the chunks
+  int force = kForceStark2;              // the lens's force law; kForceStark2Lin when every table
+                                         // passes the linear form's test at its largest voltage
   unsigned* order[CTRAJ_MAX_TABLES] = {};  // persistent: bucket counts then entrant order, per table
 };
 
@@ -1264,6 +1269,8 @@ struct SweepLaunch {
 using SweepPersistKernel = void (*)(const Plan, const RunDev, const int, const SweepQueues, const int,
                                     const SweepTabs, const LensArgs, const int);
 SweepPersistKernel sweep_persist_kernel(int force, bool staged) {
+  if (force == kForceStark2Lin)
+    return staged ? k_sweep_persist<kForceStark2Lin, true> : k_sweep_persist<kForceStark2Lin, false>;
   if (staged)
     return force == kForceStark1 ? k_sweep_persist<kForceStark1, true> : k_sweep_persist<kForceStark2, true>;
   return force == kForceStark1 ? k_sweep_persist<kForceStark1, false> : k_sweep_persist<kForceStark2, false>;
@@ -1322,7 +1329,7 @@ int sweep_enqueue(ctraj_context* c, const Plan& P, const RunDev& R, const SweepL
       T.s0[t] = W.la[t].s0;
       T.n_int[t] = W.la[t].n_int;
     }
-    sweep_persist_kernel(P.lf[W.lens].force, sweep_staged(W))<<<c->sm_count, kPersistThreads,
+    sweep_persist_kernel(W.force, sweep_staged(W))<<<c->sm_count, kPersistThreads,
                                                                   sweep_persist_smem(W), s>>>(
         P, R, W.lens, Qs, W.n_tab, T, W.la[0], c->lens_interval);
     CT_CUDA(cudaGetLastError());
@@ -1338,7 +1345,7 @@ int sweep_enqueue(ctraj_context* c, const Plan& P, const RunDev& R, const SweepL
     CT_CUDA(cudaStreamWaitEvent(st, c->fork, 0));
     const bool staged = W.la[t].n_smem > 0;
     const size_t smem = staged ? size_t(W.la[t].n_int) * sizeof(float4) : 0;
-    LensKernel kl = sweep_lens_kernel(P.lf[W.lens].force, staged);
+    LensKernel kl = sweep_lens_kernel(W.force, staged);
     const int grid = blocks_per_sm(kl, kLensThreads, smem) * c->sm_count;
     Queue in = W.qa[t];
     for (size_t k = 0; k < W.chunks.size(); ++k) {
@@ -1428,6 +1435,28 @@ extern "C" int ctraj_run_sweep(ctraj_context* c, const ctraj_sweep* sw, const ct
     }
     tab_n[dense_of[id]] += sw->n_molecules[k];
   }
+  // the table form: linear pieces when every table passes the test with the
+  // largest field coefficient any of its configurations uses
+  W.force = e.field_order == 1 ? kForceStark1 : kForceStark2;
+  if (e.field_order == 2) {
+    double alpha_max[CTRAJ_MAX_TABLES];
+    std::fill(alpha_max, alpha_max + CTRAJ_MAX_TABLES, 0.0);
+    bool lin = true;
+    for (int k = 0; k < n_cfg; ++k) {
+      const int d = dense_of[sw->table[k]];
+      if (!(sw->alpha[k] >= 0.0)) lin = false;
+      alpha_max[d] = std::max(alpha_max[d], sw->alpha[k]);
+    }
+    for (int t = 0; t < W.n_tab && lin; ++t) {
+      const HostTable& ht = c->tables[tab_id[t]];
+      ctraj_element ex = e;
+      ex.p[6] = alpha_max[t];
+      lin = stark_linear(ht.kind, ht.n, ht.knots.data(), ht.coef.data(), ex);
+    }
+    if (lin) W.force = kForceStark2Lin;
+  }
+  const bool lin = W.force == kForceStark2Lin;
+  const double piece_scale = lin ? double(kLinearPieces) : 1.0;  // table coordinate units per knot interval
 
   // buffers (grow-only); any reallocation invalidates a captured graph
   bool moved = false;
@@ -1438,7 +1467,7 @@ extern "C" int ctraj_run_sweep(ctraj_context* c, const ctraj_sweep* sw, const ct
   size_t tab_off[CTRAJ_MAX_TABLES], tab_elems = 0;
   for (int t = 0; t < W.n_tab; ++t) {
     tab_off[t] = tab_elems;
-    tab_elems += size_t(c->tables[tab_id[t]].n - 1);
+    tab_elems += size_t(c->tables[tab_id[t]].n - 1) * (lin ? 2 : 1);
   }
   const size_t words = size_t(n_cfg) * (nl + 1);
   const size_t cfg_bytes = align256(size_t(n_cfg + 1) * 8) + 3 * align256(size_t(n_cfg) * 4);
@@ -1504,10 +1533,10 @@ extern "C" int ctraj_run_sweep(ctraj_context* c, const ctraj_sweep* sw, const ct
     L = lens_args(P, lens, true);
     L.q = c->sweep_tables.as<float4>(tab_off[t] * sizeof(float4));
     L.beta = 0.f;  // per configuration
-    L.s0 = float(ht.knots[0] / h);
+    L.s0 = float(piece_scale * ht.knots[0] / h);
     L.r_max = INFINITY;
-    L.n_int = ht.n - 1;
-    L.n_smem = L.n_int <= kMaxStagedIntervals ? L.n_int : 0;
+    L.n_int = (ht.n - 1) * (lin ? 2 : 1);  // float4 entries
+    L.n_smem = L.n_int <= (lin ? kMaxStagedLinear : kMaxStagedIntervals) ? L.n_int : 0;
   }
   W.chunks = sweep_chunks(c, sweep_step_estimate(e, a));
 
@@ -1528,17 +1557,25 @@ extern "C" int ctraj_run_sweep(ctraj_context* c, const ctraj_sweep* sw, const ct
   put(W.chunks.data(), W.chunks.size() * sizeof(int));
   put(&c->lens_mode, sizeof c->lens_mode);
   put(&c->lens_interval, sizeof c->lens_interval);
+  put(&W.force, sizeof W.force);
   const bool same = key == c->sweep_key;
   cudaStream_t s = c->stream;
   if (!same) {
-    // unscaled tables: W'(E) = q.x + q.y u + q.z u^2 in interval j, u = (E - E_j) / h
+    // unscaled tables: W'(E) = q.x + q.y u + q.z u^2 in interval j, u = (E - E_j) / h,
+    // or its quarter-interval linear pieces
     std::vector<float4> host(tab_elems);
     for (int t = 0; t < W.n_tab; ++t) {
       const HostTable& ht = c->tables[tab_id[t]];
       const double h = (ht.knots[ht.n - 1] - ht.knots[0]) / double(ht.n - 1);
       for (int j = 0; j < ht.n - 1; ++j) {
         const double* cj = &ht.coef[size_t(j) * 4];
-        host[tab_off[t] + j] = make_float4(float(cj[2]), float(2.0 * cj[1] * h), float(3.0 * cj[0] * h * h), 0.f);
+        const double qa = cj[2], qb = 2.0 * cj[1] * h, qc = 3.0 * cj[0] * h * h;
+        if (lin) {
+          host[tab_off[t] + 2 * j] = stark_pieces(qa, qb, qc, 0);
+          host[tab_off[t] + 2 * j + 1] = stark_pieces(qa, qb, qc, 1);
+        } else {
+          host[tab_off[t] + j] = make_float4(float(qa), float(qb), float(qc), 0.f);
+        }
       }
     }
     // per configuration: first molecule, beta = alpha / h, kappa = -(n alpha / m) (n = field order)
@@ -1554,7 +1591,7 @@ extern "C" int ctraj_run_sweep(ctraj_context* c, const ctraj_sweep* sw, const ct
       const HostTable& ht = c->tables[id];
       const double h = (ht.knots[ht.n - 1] - ht.knots[0]) / double(ht.n - 1);
       const double alpha = sw->alpha[k];
-      h_beta[k] = float(alpha / h);
+      h_beta[k] = float(piece_scale * alpha / h);
       h_kappa[k] = float(-(e.field_order == 1 ? alpha / mass : 2.0 * alpha / mass));
       h_table[k] = dense_of[id];
     }
@@ -1571,11 +1608,11 @@ extern "C" int ctraj_run_sweep(ctraj_context* c, const ctraj_sweep* sw, const ct
   for (int t = 0; t < W.n_tab; ++t) {
     const bool staged = W.la[t].n_smem > 0;
     const size_t smem = staged ? size_t(W.la[t].n_int) * sizeof(float4) : 0;
-    CT_CUDA(cudaFuncSetAttribute(sweep_lens_kernel(P.lf[lens].force, staged),
+    CT_CUDA(cudaFuncSetAttribute(sweep_lens_kernel(W.force, staged),
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   }
   if (W.persistent)
-    CT_CUDA(cudaFuncSetAttribute(sweep_persist_kernel(P.lf[lens].force, sweep_staged(W)),
+    CT_CUDA(cudaFuncSetAttribute(sweep_persist_kernel(W.force, sweep_staged(W)),
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(sweep_persist_smem(W))));
   c->timing = timing;
   if (sw->use_graph) {
