@@ -237,8 +237,9 @@ __device__ __forceinline__ float wforce(float px, float py, const LensArgs& L, c
                                         unsigned& flags, const float beta) {
   const float r2 = __fmaf_rn(py, py, __fmul_rn(px, px));
   if (F == kForceStark2Lin) {
-    // one 8-byte lookup: ~6 bank-conflicted shared-memory wavefronts per warp
-    // instead of ~9 for the 16-byte quadratic entry
+    // quarter-interval piece (w, dw): one 8-byte lookup, ~5.4 bank-conflicted
+    // shared-memory wavefronts per warp instead of ~9 for the 16-byte
+    // quadratic entry; s counts pieces, the table holds 2 * n_int of them
     const float s = __fmaf_rn(beta, r2, -L.s0);
     // (the interval without the conversion unit: one warp's RK4 step 231
     // instead of 323 cycles, bit-identical)
