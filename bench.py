@@ -59,7 +59,7 @@ FLOP_PER_BALLISTIC_STEP = 12
 # one run of this workload, from the ncu capture summarised in
 # profiles/k_lens_persist_lens_beamline_1e7.md (the queue is read once; the
 # table and the molecule state stay on chip)
-LENS_DRAM_BYTES_PER_RUN = 10.9e6
+LENS_DRAM_BYTES_PER_RUN = 10.98e6
 # Shared-memory wavefronts per warp table lookup (the bench table goes to the
 # kernels in the 8-byte linear form: one LDS.64 per lane, random intervals,
 # bank-conflicted), from l1tex__data_pipe_lsu_wavefronts_mem_shared_op_ld of the
