@@ -1,4 +1,4 @@
-// libctraj_peak.so: measures the FP32 FMA throughput of the current GPU, the
+// libctraj_probes.so (bench_kernels/): measures the FP32 FMA throughput of the current GPU, the
 // denominator of the lens kernel's roofline fraction (the lens RK4 is bound by
 // the FP32 CUDA-core pipe, not by HBM or tensor cores).
 //

@@ -1,4 +1,4 @@
-// Check of the FP32 table-interval computation of the soft-transmission
+// Part of libctraj_probes.so (bench_kernels/).  Check of the FP32 table-interval computation of the soft-transmission
 // kernels and the linear-table lens lookups (table_interval in molecule.cuh) against the truncating float-to-unsigned
 // conversion and its inverse it replaces, over generated arguments: random
 // bit patterns (negative, NaN, infinite, subnormal and huge values), quarter

@@ -1,4 +1,4 @@
-// Part of libctraj_peak.so: the production FP32 lens RK4 step
+// Part of libctraj_probes.so (bench_kernels/): the production FP32 lens RK4 step
 // (Mol32::lens_step with the table staged in shared memory) run in a loop on
 // a fixed set of molecules, timed with clock64 and CUDA events.
 //

@@ -59,35 +59,6 @@ def build_library(force: bool = False, verbose: bool = False, extra: list[str] |
     return OUT
 
 
-PEAK_SRC = sorted((CSRC / "peak").glob("*.cu"))
-PEAK_OUT = PKG / "_lib" / "libctraj_peak.so"
-
-
-def build_peak_library(force: bool = False) -> Path:
-    """Measurement probes used by bench.py: FP32 peak (roofline denominator)
-    and the lens RK4 step's latency and throughput."""
-    deps = PEAK_SRC + headers()
-    if not force and PEAK_OUT.exists() and all(p.stat().st_mtime <= PEAK_OUT.stat().st_mtime for p in deps):
-        return PEAK_OUT
-    PEAK_OUT.parent.mkdir(parents=True, exist_ok=True)
-    tmp = PEAK_OUT.with_name(PEAK_OUT.name + f".tmp{os.getpid()}")
-    subprocess.run([nvcc(), *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", f"-I{INCLUDE}",
-                    f"-I{CSRC}", *map(str, PEAK_SRC), "-o", str(tmp)], check=True)
-    tmp.replace(PEAK_OUT)
-    return PEAK_OUT
-
-
-def build_all(force: bool = False) -> None:
-    """Both libraries, compiled in parallel."""
-    from concurrent.futures import ThreadPoolExecutor
-
-    with ThreadPoolExecutor(2) as ex:
-        futs = [ex.submit(build_library, force), ex.submit(build_peak_library, force)]
-        for f in futs:
-            f.result()
-
-
 if __name__ == "__main__":
     build_library(force="--force" in sys.argv, verbose=True,
                   extra=["-Xptxas", "-v"] if "-v" in sys.argv else None)
-    build_peak_library(force="--force" in sys.argv)

@@ -5,7 +5,7 @@ reference's (3, n) float64 array on the host (scipy.stats, global numpy RNG,
 :40-41,69-76,112-119,155-162) so that unknown code paths keep working; the
 simulator does not call it for these classes.  It recognises them and draws
 on the device instead (Philox-4x32-10 + Box-Muller, see
-``csrc/rng.cuh``), from the parameters returned by :func:`device_spec`.
+``csrc/philox.cuh``), from the parameters returned by :func:`device_spec`.
 A Distribution subclass the device does not know is drawn here, on the host,
 and uploaded.
 """

@@ -13,9 +13,9 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("last", [0, 15, 4094, 6143, 16379])
 def test_table_interval_equals_the_conversions(last):
-    from ctraj.build import build_peak_library
+    from bench_kernels.build import build as build_probes
 
-    lib = ctypes.CDLL(str(build_peak_library()))
+    lib = ctypes.CDLL(str(build_probes()))
     lib.ctraj_peak_interval_check.restype = ctypes.c_int
     lib.ctraj_peak_interval_check.argtypes = [ctypes.c_longlong, ctypes.c_uint,
                                               ctypes.POINTER(ctypes.c_ulonglong)]
