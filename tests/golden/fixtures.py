@@ -21,15 +21,20 @@ def load(name):
     return {k: z[k] for k in z.files}
 
 
-def build_beamline(fx, V=None):
-    """Beamline of this package's element classes from a fixture's spec."""
+def build_beamline(fx, V=None, classes=None, drop=()):
+    """Beamline from a fixture's spec: of this package's element classes, or,
+    with ``classes`` (a function from class name to class, e.g. the
+    reference's), of those; fields named in ``drop`` are left to the class's
+    default.  Lens forces are this package's StarkForce (the reference's
+    public ``a_interp`` field takes any callable) or a scipy interp1d."""
     import ctraj
     from scipy.interpolate import interp1d
 
     spec = json.loads(str(fx["spec"]))
+    cls = classes or (lambda name: getattr(ctraj, name))
     elems = []
     for s in spec["elements"]:
-        kw = {k: v for k, v in s.items() if k not in ("cls", "force")}
+        kw = {k: v for k, v in s.items() if k not in ("cls", "force") and k not in drop}
         if s["cls"] == "ElectrostaticLens":
             f = s["force"]
             knots = fx[f"table_{f['table']}_knots"]
@@ -38,8 +43,8 @@ def build_beamline(fx, V=None):
                                                   R=f["R"], mass=f["mass"], field_order=f["order"])
             else:
                 kw["a_interp"] = interp1d(knots, fx[f"table_{f['table']}_values"])
-        elems.append(getattr(ctraj, s["cls"])(**kw))
-    return ctraj.Beamline(elems)
+        elems.append(cls(s["cls"])(**kw))
+    return cls("Beamline")(elems)
 
 
 def expected_labels(fx):

@@ -1,10 +1,10 @@
 """Generate golden fixtures by running the reference itself.
 
-Run in a container that has the reference checked out (default
-/root/reference); the GPU machines never run this, they only read the .npz
+Run where the reference is checked out (its src directory given by
+--reference-src or CTRAJ_REFERENCE_SRC); the GPU machines never run this, they only read the .npz
 files it writes next to itself.
 
-    python tests/golden/make_golden.py [--reference-src /root/reference/src]
+    python tests/golden/make_golden.py --reference-src <reference>/src
 
 For every case it builds the case's beamline from the reference's own classes,
 injects seeded initial conditions straight into ``Molecule.init_trajectory``
@@ -36,6 +36,9 @@ import time
 from pathlib import Path
 
 import numpy as np
+
+sys.path.insert(0, str(Path(__file__).resolve().parent))
+import refstubs  # noqa: E402
 
 HERE = Path(__file__).resolve().parent
 M_PER_IN = 0.0254
@@ -399,14 +402,11 @@ def run_reference(specs, tables, ics, n_trace):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference-src", default="/root/reference/src")
+    refstubs.add_argument(ap)
     ap.add_argument("--only", nargs="*")
     ap.add_argument("--quick", action="store_true", help="10x fewer molecules (smoke)")
     args = ap.parse_args()
-    sys.path.insert(0, str(HERE))
-    import refstubs
-
-    refstubs.install(args.reference_src)
+    refstubs.install(refstubs.require(args.reference_src))
     install_mesh_stand_ins()
     import numpy
     import scipy

@@ -1,13 +1,13 @@
 """Record the HDF5 layout the reference writes for a simulation result.
 
-Run in a container that has the reference checked out (default
-/root/reference).  h5py is replaced by the in-memory recorder fake_h5py.py
+Run where the reference is checked out (its src directory given by
+--reference-src or CTRAJ_REFERENCE_SRC).  h5py is replaced by the in-memory recorder fake_h5py.py
 (h5py is not installed here), the reference's own classes propagate a few
 molecules of the ``config1`` fixture (aperture + hexapole lens), and the
 reference's ``SimulationResult.save_to_hdf`` writes them; the recorded groups,
 attributes and datasets go to hdf_layout.npz.
 
-    python tests/golden/make_golden_hdf.py [--reference-src /root/reference/src]
+    python tests/golden/make_golden_hdf.py --reference-src <reference>/src
 """
 from __future__ import annotations
 
@@ -17,6 +17,9 @@ import sys
 from pathlib import Path
 
 import numpy as np
+
+sys.path.insert(0, str(Path(__file__).resolve().parent))
+import refstubs  # noqa: E402
 
 HERE = Path(__file__).resolve().parent
 N_MOLECULES = 40
@@ -32,16 +35,14 @@ def to_json(v):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference-src", default="/root/reference/src")
+    refstubs.add_argument(ap)
     args = ap.parse_args()
     sys.path.insert(0, str(HERE))
     import fake_h5py
 
     sys.modules["h5py"] = fake_h5py  # before the reference imports it
     import make_golden
-    import refstubs
-
-    refstubs.install(args.reference_src)
+    refstubs.install(refstubs.require(args.reference_src))
     from trajectories.distributions import CeNTREXVelocityDistribution, GaussianPositionDistribution
     from trajectories.molecule import Molecule
     from trajectories.trajectory_simulator import Counter, SimulationResult

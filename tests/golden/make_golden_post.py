@@ -1,9 +1,9 @@
 """Generate golden outputs of the reference's z-plane post-processing.
 
-Run in a container that has the reference checked out (default
-/root/reference); GPU machines only read the .npz files this writes.
+Run where the reference is checked out (its src directory given by
+--reference-src or CTRAJ_REFERENCE_SRC); GPU machines only read the .npz files this writes.
 
-    python tests/golden/make_golden_post.py [--reference-src /root/reference/src]
+    python tests/golden/make_golden_post.py --reference-src <reference>/src
 
 For the fixture cases ``config0``, ``config1`` and ``example_lens`` (initial
 conditions from their .npz files, made by make_golden.py) it re-propagates the
@@ -23,6 +23,9 @@ from pathlib import Path
 
 import numpy as np
 
+sys.path.insert(0, str(Path(__file__).resolve().parent))
+import refstubs  # noqa: E402
+
 HERE = Path(__file__).resolve().parent
 
 CASES = {
@@ -35,13 +38,11 @@ CASES = {
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference-src", default="/root/reference/src")
+    refstubs.add_argument(ap)
     args = ap.parse_args()
     sys.path.insert(0, str(HERE))
     import make_golden
-    import refstubs
-
-    refstubs.install(args.reference_src)
+    refstubs.install(refstubs.require(args.reference_src))
     from trajectories.molecule import Molecule
     from trajectories.post_processing import find_radial_pos_dist, find_vel_dist
     from trajectories.trajectory_simulator import Counter, SimulationResult

@@ -1,10 +1,10 @@
 """Golden outputs of the reference's Stark-table generation on a synthetic
 Hamiltonian.
 
-Run in a container that has the reference checked out (default
-/root/reference); the GPU machines only read the .npz this writes.
+Run where the reference is checked out (its src directory given by
+--reference-src or CTRAJ_REFERENCE_SRC); the GPU machines only read the .npz this writes.
 
-    python tests/golden/make_golden_stark.py [--reference-src /root/reference/src]
+    python tests/golden/make_golden_stark.py --reference-src <reference>/src
 
 The reference builds Stark curves from the TlF Hamiltonian of the third-party
 package centrex_TlF (stark_potential.py:5-7,22-27), which is not installed and
@@ -36,6 +36,9 @@ import types
 from pathlib import Path
 
 import numpy as np
+
+sys.path.insert(0, str(Path(__file__).resolve().parent))
+import refstubs  # noqa: E402
 
 HERE = Path(__file__).resolve().parent
 J_MAX = 4
@@ -126,13 +129,11 @@ class _Axes:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference-src", default="/root/reference/src")
+    refstubs.add_argument(ap)
     args = ap.parse_args()
     sys.path.insert(0, str(HERE))
     H0, HE, HB = install_tlf_stub()  # before refstubs, so the stub modules above are used
-    import refstubs
-
-    refstubs.install(args.reference_src)
+    refstubs.install(refstubs.require(args.reference_src))
     import trajectories.stark_potential as sp
     from trajectories.beamline_elements.electrostatic_lens import ElectrostaticLens
 

@@ -71,7 +71,34 @@ _STUBS = [
 ]
 
 
-def install(reference_src="/root/reference/src"):
+ENV = "CTRAJ_REFERENCE_SRC"
+
+
+def reference_src(explicit=None):
+    """The reference's ``src`` directory: ``explicit`` if given, else the
+    environment variable CTRAJ_REFERENCE_SRC; None when neither names an
+    existing directory."""
+    import os
+
+    path = explicit or os.environ.get(ENV)
+    return path if path and os.path.isdir(path) else None
+
+
+def add_argument(ap):
+    """--reference-src for the fixture generators (defaults to CTRAJ_REFERENCE_SRC)."""
+    import os
+
+    ap.add_argument("--reference-src", default=os.environ.get(ENV),
+                    help=f"the reference's src directory (default: ${ENV})")
+
+
+def require(path):
+    if not reference_src(path):
+        raise SystemExit(f"the reference's src directory is required: pass --reference-src or set {ENV}")
+    return reference_src(path)
+
+
+def install(reference_src):
     """Install the stubs and put the reference's ``src`` directory on sys.path."""
     for name in _STUBS:
         if name not in sys.modules:
