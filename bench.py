@@ -77,6 +77,15 @@ def shared_roof(lens_steps_per_s: float, sms: int, mhz: float) -> dict:
             "wavefronts_per_lookup": SHARED_WAVEFRONTS_PER_LOOKUP, "lookups_per_step": LOOKUPS_PER_RK4_STEP,
             "roof": roof, "achieved": lens_steps_per_s, "frac": lens_steps_per_s / roof,
             "note": "1 shared-memory wavefront per cycle per SM; wavefronts per lookup from ncu"}
+L2_NOTE = ("GPU arm: 256 MiB written before every run on the run's stream inside the timed region; "
+           "CPU arm: not applicable")
+
+
+def bench_config(n: int) -> dict:
+    """The workload both arms (this engine and --impl reference) time."""
+    return {"workload": WORKLOAD, "molecules_per_step": n, "l2": L2_NOTE}
+
+
 WORKLOAD = ("lens beamline: aperture r=6mm@0.30m, hexapole lens z0=0.80m L=0.60m R=17.5mm V=30kV "
             "(4096-knot Stark spline, a=h*6.7GHz, d=4.2D), RK4 dt=1us, detection@3.0m; "
             "x,y~N(0,1.5mm) vx,vy~N(0,20m/s) vz~N(184,16m/s)")
@@ -89,7 +98,9 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--molecules", type=float, default=1e7)
-    p.add_argument("--cpu-sample", type=float, default=2e6, help="molecules per CPU sample")
+    p.add_argument("--cpu-sample", type=float, default=0,
+                   help="molecules of the CPU-baseline sample (default: --molecules, the GPU arm's step)")
+    p.add_argument("--no-parity", action="store_true", help="skip the full-size parity checks")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-sweep", action="store_true", help="skip the batched-sweep measurement")
@@ -180,26 +191,65 @@ def cpu_sample(n: int, threads: int, seed: int):
     return r["steps"], dt
 
 
-def cpu_baseline(n: int, reps: int = 1):
+def reference_python_rate():
+    """The reference's own Python run_simulation(n_jobs=cores) on this workload,
+    measured where the reference is installed (oracle/measure_reference_python.py
+    wrote the file); labelled, never part of the GPU/CPU ratio."""
+    path = ROOT / "oracle" / "reference_python_rate.json"
+    try:
+        r = json.loads(path.read_text())
+    except (OSError, ValueError):
+        return None
+    return {"value": r["value"], "unit": UNIT, "cores": r["cores"], "machine": r["machine"],
+            "molecules": r["molecules"], "steps_per_molecule": r["steps_per_molecule"], "api": r["api"],
+            "recipe": r["recipe"], "when": r["when"],
+            "note": "measured in the container holding the reference (not the GPU machine, where the reference "
+                    "is not installed); reported for reference only, not used in any ratio"}
+
+
+def config0_oracle_check(gpu):
+    """Config 0 (ballistic beamline, 1e5 molecules, numpy default_rng(0) initial
+    conditions): the oracle on the same initial conditions as the GPU FP64 run
+    `gpu` (from config0_gpu), labels and final rows compared bit for bit."""
+    import numpy as np
+
+    from ctraj.compiler import compile_beamline
+    from ctraj.workloads import ballistic_beamline
+    from oracle import oracle
+
+    cb = compile_beamline(ballistic_beamline())
+    o = oracle.run(cb, gpu["ics"], threads=os.cpu_count() or 1)
+    fin = np.isfinite(o["final"]).all(0) & np.isfinite(gpu["final"]).all(0)
+    return {"labels_equal": bool(np.array_equal(o["label"], gpu["label"])),
+            "final_rows_equal": bool(np.array_equal(o["final"][:, fin], gpu["final"][:, fin])
+                                     and np.array_equal(fin, np.isfinite(o["final"]).all(0))),
+            "counts_equal": bool(np.array_equal(o["counts"], gpu["counts"])),
+            "molecule_steps_equal": bool(o["steps"] == gpu["molecule_steps"])}
+
+
+def cpu_baseline(n: int, config0=None):
+    """The oracle on all host cores on one sample of n molecules of the bench
+    workload, plus (config0) the oracle side of the config-0 parity check."""
     threads = os.cpu_count() or 1
-    steps = secs = 0
-    for k in range(reps):
-        s, dt = cpu_sample(n, threads, seed=100 + k)
-        steps += s
-        secs += dt
-    return {"value": steps / secs, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n} molecules of the same workload per repetition x {reps}, ICs drawn on the "
-                      f"host (numpy), FP64 oracle/ctraj_oracle.c on {threads} threads"}
+    cpu_sample(min(n, 100_000), threads, seed=99)  # warm-up: library load, page-in
+    steps, secs = cpu_sample(n, threads, seed=100)
+    out = {"value": steps / secs, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{n} molecules of the same workload (one run), ICs drawn on the host (numpy), "
+                     f"FP64 oracle/ctraj_oracle.c on {threads} threads, {secs:.2f} s",
+           "reference_python": reference_python_rate()}
+    if config0 is not None:
+        out["config0_check"] = config0_oracle_check(config0)
+    return out
 
 
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    n = int(args.cpu_sample)
+    n = int(args.molecules)
     threads = os.cpu_count() or 1
     for k in range(args.warmup):
-        cpu_sample(max(n // 10, 1000), threads, seed=k)
+        cpu_sample(min(n, 100_000), threads, seed=k)
     steps = secs = 0
     for k in range(args.steps):
         s, dt = cpu_sample(n, threads, seed=1000 + k)
@@ -209,11 +259,13 @@ def run_reference(args):
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy draws)",
-            "impl": "reference",
-            "config": {"workload": WORKLOAD, "molecules_per_step": n},
+            "impl": "reference", "config": bench_config(n),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{n} molecules per step; the reference is pure Python and cannot "
-                                       f"run on the GPU machine, so its FP64 C restatement (oracle/) is timed"},
+                             "sample": f"{n} molecules per step (the GPU arm's step), {args.warmup} warm-up "
+                                       f"steps of {min(n, 100_000)}; the reference is pure Python and "
+                                       f"cannot run on the GPU machine, so its FP64 C restatement "
+                                       f"(oracle/) is timed on {threads} threads",
+                             "reference_python": reference_python_rate()},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -265,9 +317,9 @@ class Clocks:
 
 
 def fp32_peak(device: int):
-    from ctraj.build import PEAK_OUT
+    from bench_kernels.build import build as build_probes
 
-    lib = ctypes.CDLL(str(PEAK_OUT))
+    lib = ctypes.CDLL(str(build_probes()))
     lib.ctraj_peak_fp32.restype = ctypes.c_int
     lib.ctraj_peak_fp32.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                     ctypes.POINTER(ctypes.c_double)]
@@ -286,7 +338,7 @@ def step_probe(device: int, bl):
     import numpy as np
     import torch
 
-    from ctraj.build import PEAK_OUT
+    from bench_kernels.build import build as build_probes
 
     lens = [e for e in bl.elements if type(e).__name__ == "ElectrostaticLens"][0]
     F = lens.a_interp
@@ -305,7 +357,7 @@ def step_probe(device: int, bl):
     qq = np.zeros((len(F.coef), 4), np.float32)
     qq[:, 0], qq[:, 1], qq[:, 2] = a, b, c
     qqd = torch.from_numpy(qq).to(f"cuda:{device}")
-    lib = ctypes.CDLL(str(PEAK_OUT))
+    lib = ctypes.CDLL(str(build_probes()))
     lib.ctraj_peak_step.restype = ctypes.c_int
     lib.ctraj_peak_step.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_int, ctypes.c_int,
                                     ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
@@ -469,6 +521,69 @@ def bench_adjoint(eng, stream, flush, steps: int, warmup: int):
             "fd_check": {"molecules": 100_000, "h": "1e-4 relative, central, FP64 forward",
                          "max_rel_error_fp32_adjoint": float(rel.max())},
             "timing": "CUDA events on the launching stream around the call (result on the host), L2 flushed before each"}
+
+
+EDGE_BAND = 1e-6   # m: molecules nearer than this to an edge (FP64 margin) may change label in FP32
+POS_TOL = 1e-6     # m: FP32 final positions against FP64
+
+
+def parity_config1(eng, cb, n: int, seed: int, xs, vs, timed_counts=None) -> dict:
+    """The bench workload at its full size: the FP32 run (the timed path, with
+    per-molecule outputs) against the FP64 run of the same Philox stream.  Every
+    molecule farther than 1 um from an edge (FP64 margin) must get the same
+    label, and the same-label molecules' final x, y must agree within 1 um."""
+    import torch
+
+    outs, runs = {}, {}
+    for prec in (32, 64):
+        o = {"label": torch.empty(n, dtype=torch.int32, device="cuda"),
+             "final": torch.empty((10, n), dtype=torch.float64, device="cuda"),
+             "margin": torch.empty(n, dtype=torch.float64, device="cuda")}
+        runs[prec] = eng.run(cb, n, precision=prec, xdist=xs, vdist=vs, seed=seed, device_outputs=o, timing=True)
+        outs[prec] = o
+    o32, o64 = outs[32], outs[64]
+    far = o64["margin"] >= EDGE_BAND
+    same = (o32["label"] == o64["label"]) & far
+    d = (o32["final"][:, same] - o64["final"][:, same]).abs()
+    m = lambda t: float(t.max()) if t.numel() else 0.0  # noqa: E731
+    r32, r64 = runs[32], runs[64]
+    out = {"workload": "the bench workload (lens beamline, FP32) against FP64 on the same Philox stream",
+           "molecules": n, "seed": seed,
+           "edge_band": int((~far).sum()),
+           "label_mismatch_off_band": int(((o32["label"] != o64["label"]) & far).sum()),
+           "label_mismatch_in_band": int(((o32["label"] != o64["label"]) & ~far).sum()),
+           "max_abs_dx_m": m(d[0]), "max_abs_dy_m": m(d[1]), "max_abs_dv_m_per_s": m(d[3:6]),
+           "max_abs_dt_s": m(d[9]), "position_tolerance_m": POS_TOL,
+           "counts_fp32": r32.counter_dict(), "counts_fp64": r64.counter_dict(),
+           "detected_fraction_fp32": float(r32.counts[-1]) / n, "detected_fraction_fp64": float(r64.counts[-1]) / n,
+           "fp64_ms": r64.extra.get("front_ms", 0.0) + r64.extra.get("lens_ms", 0.0)}
+    if timed_counts is not None:
+        out["fp32_counts_equal_timed_run"] = bool(list(timed_counts) == list(r32.counts))
+    out["pass"] = (out["label_mismatch_off_band"] == 0 and out["max_abs_dx_m"] <= POS_TOL
+                   and out["max_abs_dy_m"] <= POS_TOL)
+    del outs, o32, o64, d
+    torch.cuda.empty_cache()
+    return out
+
+
+def config0_gpu(eng, n: int = 100_000, seed: int = 0) -> dict:
+    """Config 0: the plain ballistic beamline (apertures r = 6 mm at 0.30 m,
+    10 x 8 mm at 1.00 m, r = 10 mm at 2.00 m, detection plane at 3.00 m) in FP64,
+    n molecules drawn on the host with numpy default_rng(seed) from the bench's
+    distributions; per-element counts and the detected fraction."""
+    from ctraj.compiler import compile_beamline
+    from ctraj.distributions import host_draw
+    from ctraj.workloads import ballistic_beamline, source
+
+    cb = compile_beamline(ballistic_beamline())
+    xd, vd = source()
+    ics = host_draw(xd, vd, n, seed=seed)
+    r = eng.run(cb, n, precision=64, ics=ics, outputs=True)
+    return {"ics": ics, "label": r.label, "final": r.final, "counts": r.counts, "molecule_steps": r.molecule_steps,
+            "report": {"workload": "ballistic beamline (config 0), FP64, initial conditions numpy "
+                                   f"default_rng({seed})", "molecules": n, "seed": seed,
+                       "counts": r.counter_dict(), "detected_fraction": float(r.counts[-1]) / n,
+                       "molecule_steps": int(r.molecule_steps)}}
 
 
 def bench_large(eng, stream, flush, n_total: int = 1_000_000_000, chunk: int = 134_000_000):
@@ -687,6 +802,15 @@ def main():
 
     if rank != 0:
         return
+    # parity at the quoted sizes (outside the timed region): config 1 on the
+    # last timed step's Philox stream, config 0 at 1e5 (its oracle check runs
+    # in the CPU-baseline leg below)
+    parity = None
+    cfg0 = None
+    if not args.no_parity:
+        parity = {"config1": parity_config1(eng, cb, n, seeds[-1], xs, vs, timed_counts=batch[-1].counts)}
+        cfg0 = config0_gpu(eng)
+        parity["config0"] = cfg0["report"]
     sweep = None if args.no_sweep else bench_sweep(eng, stream, flush, args.steps, args.warmup,
                                                    torch.cuda.get_device_name(local))
     adjoint = None if args.no_adjoint else bench_adjoint(eng, stream, flush, args.steps, args.warmup)
@@ -695,7 +819,7 @@ def main():
     roofline = {"bound": "fp32", "kernel": "k_lens_persist (RK4 through the hexapole lens; the lens pass = "
                                           "entrant ordering + k_lens_persist, timed together)",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                "peak_source": "measured in this run: FMA-chain kernel (csrc/peak/fp32_peak.cu), "
+                "peak_source": "measured in this run: FMA-chain kernel (bench_kernels/fp32_peak.cu), "
                                "MEASURED_PEAKS.json has no FP32 CUDA-core figure",
                 "flop_per_step": FLOP_PER_RK4_STEP, "lens_steps_per_launch": lens_steps / args.steps,
                 "lens_ms_per_launch": lens_ms / args.steps, "front_ms_per_launch": front_ms / args.steps,
@@ -718,13 +842,16 @@ def main():
     if mhz:
         roofline["shared_memory"] = shared_roof(lens_steps / (lens_ms / 1e3), torch.cuda.get_device_properties(
             local).multi_processor_count, mhz)
-    cpu = None if args.no_cpu or world > 1 else cpu_baseline(int(args.cpu_sample))
+    cpu = None if args.no_cpu or world > 1 else cpu_baseline(int(args.cpu_sample or n), config0=cfg0)
+    if parity is not None and cpu is not None and "config0_check" in cpu:
+        parity["config0"]["oracle"] = cpu["config0_check"]
     r0 = results[-1]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
             "data": "synthetic: Philox-4x32-10 initial conditions drawn on the device",
-            "config": {"workload": WORKLOAD, "molecules_per_gpu": n, "precision": "fp32",
+            "config": bench_config(n),
+            "engine": {"molecules_per_gpu": n, "precision": "fp32",
                        "pipelining": "ctraj_run_batch: the K runs alternate between two lanes (contexts with "
                                      "their own streams and buffers, one host thread each); a run's front "
                                      "overlaps the other lane's lens pass",
@@ -733,7 +860,7 @@ def main():
                        "parallelism": f"replicas x{world}",
                        "tuning": tuned["tuning"], "tuning_cached": tuned.get("cached", False)},
             "e2e": e2e, "sequential": sequential, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
-            "sweep": sweep, "adjoint": adjoint, "large": large,
+            "parity": parity, "sweep": sweep, "adjoint": adjoint, "large": large,
             "gpu_launches": int(sum(r.kernels for r in batch)),
             "molecule_steps_per_step": steps / args.steps, "counts_last_step": r0.counter_dict()}
     print(json.dumps(line), flush=True)
