@@ -1916,32 +1916,75 @@ namespace {
 // stand-in; noalloc_scratch() looks up the real address per device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[CTRAJ_NOALLOC_SCRATCH_BYTES];
 
-// Layout: control words (queue counters, tallies, stats) | per-chunk queue
-// counters | FP32 lens tables | three lens queues.
+// Layout: control words (queue counters, tallies, stats) | FP32 lens tables
+// (kNaTables) | lens-entrant order (kNaOrder) | two lens queues (kNaQueues).
 constexpr size_t kNaCtl = 0;
 constexpr size_t kNaTables = 4096;
 constexpr size_t kNaOrder = kNaTables + size_t(CTRAJ_NOALLOC_MAX_INTERVALS) * sizeof(float4);
 constexpr size_t kNaQueues =
     kNaOrder + ((size_t(kOrderBuckets) + CTRAJ_NOALLOC_MAX_MOLECULES) * sizeof(unsigned) + 255) / 256 * 256;
 
+// The array's device address differs between CUDA contexts (a non-primary
+// context made with cuCtxCreate loads its own copy of the module, and a
+// cudaDeviceReset replaces the primary context), so it is looked up once per
+// context, keyed by the context's process-unique id (cuCtxGetId), with that
+// context current.  The two driver functions are reached through the runtime
+// (cudaGetDriverEntryPointByVersion): the library does not link libcuda.
+struct NoallocSlot {
+  unsigned long long ctx_id;
+  void* ptr;
+};
+constexpr int kNoallocSlots = 64;
 std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[64] = {};
+NoallocSlot g_noalloc_slot[kNoallocSlots] = {};
+int g_noalloc_next = 0;
+using CtxGetCurrentFn = int (*)(void**);
+using CtxGetIdFn = int (*)(void*, unsigned long long*);
+CtxGetCurrentFn g_ctx_current = nullptr;
+CtxGetIdFn g_ctx_id = nullptr;
 
-// Device address of the scratch array on the current device, looked up once
-// per device with that device current (cudaGetSymbolAddress).
+int noalloc_driver_fns() {
+  if (g_ctx_current && g_ctx_id) return CTRAJ_OK;
+  void* f0 = nullptr;
+  void* f1 = nullptr;
+  cudaDriverEntryPointQueryResult q0 = cudaDriverEntryPointSymbolNotFound, q1 = cudaDriverEntryPointSymbolNotFound;
+  CT_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0));
+  CT_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1));
+  if (q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess || !f0 || !f1)
+    return fail(CTRAJ_ECUDA, "the CUDA driver does not provide cuCtxGetCurrent / cuCtxGetId");
+  g_ctx_current = reinterpret_cast<CtxGetCurrentFn>(f0);
+  g_ctx_id = reinterpret_cast<CtxGetIdFn>(f1);
+  return CTRAJ_OK;
+}
+
+// Device address of the scratch array in the calling thread's current
+// context: cudaGetSymbolAddress on the first call in that context (which
+// also loads the module there), the cached address afterwards.
 int noalloc_scratch(char** out) {
   int dev = 0;
   CT_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) return fail(CTRAJ_EINVAL, "device %d out of range", dev);
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      return fail(CTRAJ_ECUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
-    g_noalloc_ptr[dev] = p;
+  int st = noalloc_driver_fns();
+  if (st) return st;
+  void* ctx = nullptr;
+  if (g_ctx_current(&ctx) != 0) return fail(CTRAJ_ECUDA, "cuCtxGetCurrent failed");
+  if (!ctx) {  // no context current yet: make the device's primary context current
+    CT_CUDA(cudaSetDevice(dev));
+    if (g_ctx_current(&ctx) != 0 || !ctx) return fail(CTRAJ_ECUDA, "no CUDA context on device %d", dev);
   }
-  *out = static_cast<char*>(g_noalloc_ptr[dev]);
+  unsigned long long id = 0;
+  if (g_ctx_id(ctx, &id) != 0) return fail(CTRAJ_ECUDA, "cuCtxGetId failed");
+  for (const NoallocSlot& s : g_noalloc_slot)
+    if (s.ptr && s.ctx_id == id) {
+      *out = static_cast<char*>(s.ptr);
+      return CTRAJ_OK;
+    }
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) return fail(CTRAJ_ECUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+  g_noalloc_slot[g_noalloc_next] = NoallocSlot{id, p};  // the oldest context's entry is dropped
+  g_noalloc_next = (g_noalloc_next + 1) % kNoallocSlots;
+  *out = static_cast<char*>(p);
   return CTRAJ_OK;
 }
 
@@ -1966,8 +2009,37 @@ int noalloc_check_table(const ctraj_force_table& t, int k) {
   return CTRAJ_OK;
 }
 
+// Host-side checks of the elements' tables, before any CUDA call: table ids,
+// mesh shapes, lens field orders, and that the FP32 tables of all lenses and
+// meshes fit the scratch's CTRAJ_NOALLOC_MAX_INTERVALS float4 entries.
+int noalloc_check_tables(const ctraj_element* el, int n_el, const ctraj_force_table* tabs, int n_tab) {
+  size_t total = 0;
+  for (int i = 0; i < n_el; ++i) {
+    const ctraj_element& e = el[i];
+    if (e.type != CTRAJ_ELECTROSTATIC_LENS && e.type != CTRAJ_HONEYCOMB) continue;
+    if (e.table < 0 || e.table >= n_tab) return fail(CTRAJ_ESTATE, "element %d uses table %d, not given", i, e.table);
+    const ctraj_force_table& t = tabs[e.table];
+    if (e.type == CTRAJ_HONEYCOMB) {
+      int st = check_honeycomb(e, i, t.kind, t.n_knots);
+      if (st) return st;
+      total += size_t(t.n_knots);
+    } else {
+      if (t.kind == CTRAJ_TABLE_MESH) return fail(CTRAJ_EINVAL, "lens element %d: table %d is a mesh table", i, e.table);
+      if (t.kind == CTRAJ_TABLE_STARK_SPLINE && e.field_order != 1 && e.field_order != 2)
+        return fail(CTRAJ_EINVAL, "lens element %d: field_order must be 1 or 2", i);
+      const bool lin = stark_linear(t.kind, t.n_knots, t.knots, t.coef, e);
+      total += size_t(t.n_knots - 1) * (lin ? 2 : 1);
+    }
+  }
+  if (total > size_t(CTRAJ_NOALLOC_MAX_INTERVALS))
+    return fail(CTRAJ_EINVAL, "lens and mesh tables need %zu float4 entries: the scratch holds at most %d",
+                total, CTRAJ_NOALLOC_MAX_INTERVALS);
+  return CTRAJ_OK;
+}
+
 // Plan and FP32 lens tables (written into the scratch through a small stack
-// buffer: nothing is allocated on the host heap either).
+// buffer: nothing is allocated on the host heap either).  The tables were
+// checked by noalloc_check_tables.
 int noalloc_plan(const ctraj_element* el, int n_el, int n_labels, const ctraj_force_table* tabs,
                  int n_tab, const ctraj_run_args* a, float4* dev_tables, cudaStream_t s, Plan& P) {
   std::memset(&P, 0, sizeof P);
@@ -1997,13 +2069,8 @@ int noalloc_plan(const ctraj_element* el, int n_el, int n_labels, const ctraj_fo
       honeycomb_constants(e, f);
     }
     if (e.type != CTRAJ_ELECTROSTATIC_LENS && e.type != CTRAJ_HONEYCOMB) continue;
-    if (e.table < 0 || e.table >= n_tab) return fail(CTRAJ_ESTATE, "element %d uses table %d, not given", i, e.table);
     const ctraj_force_table& t = tabs[e.table];
     if (e.type == CTRAJ_HONEYCOMB) {  // cell centres (x, y, 0, 0)
-      int st = check_honeycomb(e, i, t.kind, t.n_knots);
-      if (st) return st;
-      if (offset + size_t(t.n_knots) > size_t(CTRAJ_NOALLOC_MAX_INTERVALS))
-        return fail(CTRAJ_EINVAL, "lens and mesh tables exceed %d entries", CTRAJ_NOALLOC_MAX_INTERVALS);
       for (int j0 = 0; j0 < t.n_knots; j0 += 256) {
         const int m = std::min(256, t.n_knots - j0);
         for (int j = 0; j < m; ++j)
@@ -2016,15 +2083,10 @@ int noalloc_plan(const ctraj_element* el, int n_el, int n_labels, const ctraj_fo
       offset += size_t(t.n_knots);
       continue;
     }
-    if (t.kind == CTRAJ_TABLE_MESH) return fail(CTRAJ_EINVAL, "lens element %d: table %d is a mesh table", i, e.table);
-    if (t.kind == CTRAJ_TABLE_STARK_SPLINE && e.field_order != 1 && e.field_order != 2)
-      return fail(CTRAJ_EINVAL, "lens element %d: field_order must be 1 or 2", i);
     if (P.first_lens == n_el) P.first_lens = i;
     const int n_int = t.n_knots - 1;
     const bool lin = stark_linear(t.kind, t.n_knots, t.knots, t.coef, e);
     const int entries = lin ? 2 * n_int : n_int;  // float4
-    if (offset + size_t(entries) > size_t(CTRAJ_NOALLOC_MAX_INTERVALS))
-      return fail(CTRAJ_EINVAL, "lens tables exceed %d entries", CTRAJ_NOALLOC_MAX_INTERVALS);
     const double x0 = t.knots[0], h = (t.knots[t.n_knots - 1] - t.knots[0]) / double(n_int);
     const double alpha = e.p[6], mass = e.p[5];
     const double kappa = e.field_order == 1 ? alpha / mass : 2.0 * alpha / mass;
@@ -2066,9 +2128,10 @@ int noalloc_plan(const ctraj_element* el, int n_el, int n_labels, const ctraj_fo
 }
 
 // The launch sequence of launch_all (FP32), on the scratch's queues.
+// *max_steps receives the largest lens step bound of any lens queue.
 template <bool kOut>
 int noalloc_launch(const Plan& P, const RunDev& R, Queue* q, unsigned* order_buf, cudaStream_t s,
-                   int* launches) {
+                   int* launches, unsigned* max_steps) {
   int dev = 0, sms = 0;
   CT_CUDA(cudaGetDevice(&dev));
   CT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -2084,9 +2147,11 @@ int noalloc_launch(const Plan& P, const RunDev& R, Queue* q, unsigned* order_buf
   int cur = 0, nxt = 1;
   for (int i = 0; i < P.n_el && n > 0; ++i) {
     if (P.el[i].type != CTRAJ_ELECTROSTATIC_LENS) continue;
-    unsigned count = 0;
-    CT_CUDA(cudaMemcpyAsync(&count, q[cur].count, sizeof count, cudaMemcpyDeviceToHost, s));
+    unsigned ctl[2] = {0, 0};  // the queue's count and largest step bound
+    CT_CUDA(cudaMemcpyAsync(ctl, q[cur].count, sizeof ctl, cudaMemcpyDeviceToHost, s));
     CT_CUDA(cudaStreamSynchronize(s));
+    const unsigned count = ctl[0];
+    *max_steps = std::max(*max_steps, ctl[1]);
     if (count == 0) break;
     CT_CUDA(cudaMemsetAsync(q[nxt].count, 0, kCtlWords * sizeof(unsigned), s));
     // the persistent pass finishes every molecule: nothing stays inside the lens
@@ -2137,9 +2202,10 @@ extern "C" int ctraj_run_noalloc(const ctraj_element* el, int32_t n_el, int32_t 
     int st = noalloc_check_table(tabs[k], k);
     if (st) return st;
   }
-  char* scratch = nullptr;
-  int st = noalloc_scratch(&scratch);
+  int st = noalloc_check_tables(el, n_el, tabs, n_tab);
   if (st) return st;
+  char* scratch = nullptr;
+  if ((st = noalloc_scratch(&scratch))) return st;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const size_t cap = CTRAJ_NOALLOC_MAX_MOLECULES;
   const size_t qb = queue_bytes(cap, 32);
@@ -2184,9 +2250,10 @@ extern "C" int ctraj_run_noalloc(const ctraj_element* el, int32_t n_el, int32_t 
     R.out_final = a->out_final;
   }
   int launches = 0;
+  unsigned max_steps = 0;
   unsigned* order_buf = reinterpret_cast<unsigned*>(scratch + kNaOrder);
-  st = out ? noalloc_launch<true>(P, R, q, order_buf, s, &launches)
-           : noalloc_launch<false>(P, R, q, order_buf, s, &launches);
+  st = out ? noalloc_launch<true>(P, R, q, order_buf, s, &launches, &max_steps)
+           : noalloc_launch<false>(P, R, q, order_buf, s, &launches, &max_steps);
   if (st) return st;
   unsigned long long hc[CTRAJ_MAX_LABELS + 1], hs[kStatCount];
   CT_CUDA(cudaMemcpyAsync(hc, counts, sizeof hc, cudaMemcpyDeviceToHost, s));
@@ -2202,6 +2269,9 @@ extern "C" int ctraj_run_noalloc(const ctraj_element* el, int32_t n_el, int32_t 
     stats->table_range = int64_t(hs[kStatTableRange]);
     stats->bad_steps = int64_t(hs[kStatBadSteps]);
     stats->kernels = launches;
+    stats->max_lens_steps = int32_t(max_steps);
+    for (int i = 0; i < P.n_el; ++i)
+      stats->linear_tables += P.el[i].type == CTRAJ_ELECTROSTATIC_LENS && P.lf[i].force == kForceStark2Lin;
   }
   if (hs[kStatRangeError])
     return fail(CTRAJ_ERANGE, "%llu molecules looked up the lens table above its last knot", hs[kStatRangeError]);

@@ -254,6 +254,7 @@ SIGNATURES = {
 
 # ctraj_run_noalloc limits (include/ctraj.h)
 NOALLOC_MAX_MOLECULES = 131072
+NOALLOC_MAX_INTERVALS = 16384
 NOALLOC_SCRATCH_BYTES = 32 << 20
 
 

@@ -17,8 +17,8 @@
  *
  * The reference has no foreign-function interface of its own (it is ~2 kLoC of
  * Python); every entry point below replaces the Python function cited beside
- * it, and the Python package shipped with this library binds them through
- * ctypes (INTEGRATION.md shows the binding).
+ * it, and the Python package shipped with this library (ctraj._abi) binds them
+ * through ctypes.
  *
  * Conventions: every function returns an int status (CTRAJ_OK == 0, negative
  * on error) and never throws.  ctraj_last_error() returns a message for the
@@ -212,13 +212,15 @@ typedef struct ctraj_run_stats {
   int32_t timed;            /* 1 when the *_ms fields below were measured     */
   float front_ms;           /* CUDA-event time of the ballistic front kernel  */
   float lens_ms;            /* CUDA-event time of all lens kernels            */
-  int32_t max_lens_steps;   /* ctraj_run: upper bound on the RK4 steps of the
-                               molecule with the most steps in a lens
-                               (rint(L/dz) + 2), the length of the lens pass's
-                               critical path; 0 from the other entry points   */
-  int32_t linear_tables;    /* ctraj_run: lens elements whose FP32 run used the
-                               8-byte linear form of their Stark table (the
-                               host's accuracy and coverage test passed)     */
+  int32_t max_lens_steps;   /* ctraj_run, ctraj_run_batch, ctraj_run_noalloc:
+                               upper bound on the RK4 steps of the molecule
+                               with the most steps in a lens (rint(L/dz) + 2),
+                               the length of the lens pass's critical path; 0
+                               from the other entry points                    */
+  int32_t linear_tables;    /* ctraj_run, ctraj_run_batch, ctraj_run_noalloc:
+                               lens elements whose FP32 run used the 8-byte
+                               linear form of their Stark table (the host's
+                               accuracy and coverage test passed)             */
 } ctraj_run_stats;
 
 /* ---- context -------------------------------------------------------------- */
@@ -480,30 +482,38 @@ int ctraj_soft_transmission(ctraj_context* ctx, const ctraj_soft_args* args,
 /*
  * Allocation-free run.  This entry point has no counterpart in the reference.
  *
- * ctraj_run_noalloc propagates molecules exactly as ctraj_run does (same
- * kernels -- the persistent lens pass with the default compaction interval --
- * same results molecule by molecule) but needs no context and allocates no
- * device memory: its scratch (lens queues, queue counters, tallies, the FP32
- * lens tables, the lens-entrant order) lives in one file-scope __device__ array of
- * CTRAJ_NOALLOC_SCRATCH_BYTES that every GPU which loads libctraj.so holds
- * until the process exits.  It is for callers that cannot allocate device
- * memory while they run: an application that hands this library a fixed
- * device-memory budget at start-up and owns every allocation itself, or a
- * service that must not call cudaMalloc/cudaFree on its request path because
- * those calls synchronize the whole device and stall the other work on it.
+ * ctraj_run_noalloc propagates molecules exactly as ctraj_run does with its
+ * default tuning (same kernels: the ballistic front, the lens-entrant
+ * ordering and the persistent lens pass with compaction interval 256; same
+ * counts, stats and per-molecule outputs, bit for bit) but needs no context
+ * and allocates no device memory: its scratch (lens queues, queue counters,
+ * tallies, the FP32 lens tables, the lens-entrant order) lives in one
+ * file-scope __device__ array of CTRAJ_NOALLOC_SCRATCH_BYTES that every GPU
+ * which loads libctraj.so holds until the process exits.  It is for callers
+ * that cannot allocate device memory while they run: an application that
+ * hands this library a fixed device-memory budget at start-up and owns every
+ * allocation itself, or a service that must not call cudaMalloc/cudaFree on
+ * its request path because those calls synchronize the whole device and
+ * stall the other work on it.
  *
  * Limits: precision 32 only; at most CTRAJ_NOALLOC_MAX_MOLECULES molecules per
- * call (larger n is rejected with CTRAJ_EINVAL); initial conditions drawn on
- * the device or given in device memory (CTRAJ_IC_DEVICE); per-molecule outputs,
- * if any, in device memory (CTRAJ_OUT_DEVICE); counts are written to the host
- * array args->counts.  Runs on the calling thread's current device and on
+ * call and at most CTRAJ_NOALLOC_MAX_INTERVALS FP32 table entries over all
+ * lenses and meshes (larger inputs are rejected with CTRAJ_EINVAL before any
+ * CUDA call); initial conditions drawn on the device or given in device
+ * memory (CTRAJ_IC_DEVICE); per-molecule outputs, if any, in device memory
+ * (CTRAJ_OUT_DEVICE); counts are written to the host array args->counts.
+ * Runs on the calling thread's current device and context and on
  * `cuda_stream` (NULL = the legacy default stream), and returns after the
  * counts are on the host.
  *
- * The first call on a device looks up the array's device address with that
- * device current; make that first call before capturing any stream.  All
- * calls share the one array and each overwrites it, so calls that overlap on
- * the GPU (from two host threads, or on two streams) race: serialize them.
+ * The array's device address is looked up (cudaGetSymbolAddress) by the first
+ * call in each CUDA context, with that context current: the first call on a
+ * device, the first call in a context created with cuCtxCreate, and the first
+ * call after cudaDeviceReset (which replaces the primary context).  Make that
+ * first call before any stream capture.  All calls share the one array and
+ * each overwrites it (it starts every call by clearing its counters), so calls
+ * that overlap on the GPU (from two host threads, or on two streams) race:
+ * serialize them.
  */
 #define CTRAJ_NOALLOC_MAX_MOLECULES 131072
 #define CTRAJ_NOALLOC_MAX_INTERVALS 16384 /* FP32 table entries over all lenses (one per knot interval, two in the linear Stark form) + honeycomb cells */

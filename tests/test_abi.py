@@ -84,3 +84,47 @@ def test_struct_layout_matches_header():
 def test_missing_library_fails_loudly(tmp_path):
     with pytest.raises(RuntimeError, match="not built"):
         _abi.load_library(tmp_path / "nope.so")
+
+
+def _noalloc_call(lib, cb, n, precision=32):
+    """ctraj_run_noalloc with device draws; returns (status, message)."""
+    from ctraj.distributions import device_spec
+    from ctraj.workloads import source
+
+    a = _abi.RunArgs()
+    a.n, a.precision, a.g, a.ic_mode = n, precision, 9.80665, _abi.IC_DEVICE_DRAW
+    a.xdist, a.vdist = (device_spec(d, r) for d, r in zip(source(), ("position", "velocity")))
+    counts = (ctypes.c_int64 * (len(cb.labels) + 1))()
+    a.counts = ctypes.addressof(counts)
+    st = _abi.RunStats()
+    tabs = cb.table_structs()
+    status = lib.ctraj_run_noalloc(cb.elements, cb.n_elements, len(cb.labels), tabs, len(cb.tables),
+                                   ctypes.byref(a), None, ctypes.byref(st))
+    return status, lib.ctraj_last_error().decode()
+
+
+def test_noalloc_rejects_what_its_scratch_cannot_hold_before_any_cuda_call():
+    """Sizes beyond the allocation-free entry point's fixed scratch are refused
+    with CTRAJ_EINVAL and a clear message, without touching the GPU (this runs
+    on machines without one)."""
+    import numpy as np
+    from scipy.interpolate import interp1d
+
+    import ctraj
+    from ctraj.compiler import compile_beamline
+    from ctraj.workloads import lens_beamline
+
+    lib = _abi.load_library()
+    lib.ctraj_last_error.restype = ctypes.c_char_p
+    cb = compile_beamline(lens_beamline())
+    st, msg = _noalloc_call(lib, cb, _abi.NOALLOC_MAX_MOLECULES + 1)
+    assert st == _abi.EINVAL and "at most" in msg
+    st, msg = _noalloc_call(lib, cb, 1000, precision=64)
+    assert st == _abi.EINVAL and "precision 32" in msg
+    # a radial table of more knot intervals than the scratch's table entries
+    r = np.linspace(0.0, 0.02, _abi.NOALLOC_MAX_INTERVALS + 2)
+    lens = ctraj.ElectrostaticLens(name="ES lens", z0=0.8, L=0.6, d=0.035, dz=1e-3,
+                                   a_interp=interp1d(r, -1e3 * r))
+    big = compile_beamline(ctraj.Beamline([lens]))
+    st, msg = _noalloc_call(lib, big, 1000)
+    assert st == _abi.EINVAL and "scratch holds at most" in msg, msg
