@@ -654,7 +654,7 @@ def main():
     from ctraj.distributions import device_spec
     from ctraj.engine import default_engine
     from ctraj.trajectory_simulator import TrajectorySimulator
-    from ctraj.tuning import autotune
+    from ctraj.tuning import autotune, batch_measure
     from ctraj.workloads import lens_beamline, source
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -684,8 +684,9 @@ def main():
     for k in range(args.warmup):
         step(seed=k)
     # launch knobs picked on this workload (outside the timed region), then re-warm
-    tuned = autotune(eng, cb, n, dict(precision=32, xdist=xs, vdist=vs, seed=7, offset=rank * n),
-                     device_name=torch.cuda.get_device_name(local))
+    run_kw = dict(precision=32, xdist=xs, vdist=vs, seed=7, offset=rank * n)
+    tuned = autotune(eng, cb, n, run_kw, device_name=torch.cuda.get_device_name(local),
+                     batch=batch_measure(eng, cb, n, run_kw, runs=8, l2_flush_bytes=flush.numel()))
     for k in range(args.warmup):
         step(seed=k)
     eng.run_batch(cb, n, list(range(max(2, args.warmup))), precision=32, xdist=xs, vdist=vs, offset=rank * n,

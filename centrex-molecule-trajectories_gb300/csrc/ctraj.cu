@@ -119,6 +119,8 @@ struct ctraj_context {
   int front_waves = 4;          // k_front grid in units of resident CTAs
   int lens_mode = CTRAJ_LENS_PERSISTENT;  // FP32 lens pass
   int lens_interval = 256;      // persistent mode: steps between CTA compactions
+  int front_threads = 256;      // k_front block size
+  int batch_group = 4;          // ctraj_run_batch: runs sharing one lens pass
   unsigned run_max_steps = 0;   // largest lens queue step bound of the last run
   bool timing = false;
   // before front, after front, before the first lens chunk, after the last one
@@ -145,6 +147,12 @@ struct ctraj_context {
   uint64_t peer_generation = ~uint64_t(0);
   DevBuf l2_flush;              // scratch written before each run of a batch
   cudaEvent_t batch_ev = nullptr;
+  // grouped batches: per-run counts and stats (device and pinned host), the
+  // host initial conditions of a group's runs
+  DevBuf group_ctl;
+  unsigned long long* group_host = nullptr;
+  size_t group_host_words = 0;
+  DevBuf group_ics;
 };
 
 namespace ctraj {
@@ -447,13 +455,11 @@ LensKernel lens_kernel(int force, bool staged) {
   return staged ? lens_kernel32<kOut, true, kRing>(force) : lens_kernel32<kOut, false, kRing>(force);
 }
 
-// The persistent FP32 lens pass of lens element i over queue Qin (count
-// entries, at most max_steps steps each): order the entrants longest first,
-// then one k_lens_persist launch, one CTA per SM.
 // The persistent FP32 lens pass of lens element i over queue Qin: order the
 // entrants longest first into `order_buf` (kOrderBuckets + the queue's
-// entries), then one k_lens_persist launch, one CTA per SM.
-template <bool kOut, bool kRing = false>
+// entries), then one k_lens_persist launch, one CTA per SM.  kMode: plain,
+// ring recording or grouped batch.
+template <bool kOut, int kMode = kModePlain>
 int enqueue_persistent(const Plan& P, const RunDev& R, int i, const Queue& Qin, const Queue& Qnext,
                        unsigned* order_buf, int sms, int interval, cudaStream_t s, int* launches) {
   using M = Mol32<kOut, false>;
@@ -463,20 +469,20 @@ int enqueue_persistent(const Plan& P, const RunDev& R, int i, const Queue& Qin, 
   PK k;
   switch (P.lf[i].force) {
     case kForceStark2:
-      k = staged ? k_lens_persist<M, kOut, kForceStark2, true, kRing>
-                 : k_lens_persist<M, kOut, kForceStark2, false, kRing>;
+      k = staged ? k_lens_persist<M, kOut, kForceStark2, true, kMode>
+                 : k_lens_persist<M, kOut, kForceStark2, false, kMode>;
       break;
     case kForceStark2Lin:
-      k = staged ? k_lens_persist<M, kOut, kForceStark2Lin, true, kRing>
-                 : k_lens_persist<M, kOut, kForceStark2Lin, false, kRing>;
+      k = staged ? k_lens_persist<M, kOut, kForceStark2Lin, true, kMode>
+                 : k_lens_persist<M, kOut, kForceStark2Lin, false, kMode>;
       break;
     case kForceStark1:
-      k = staged ? k_lens_persist<M, kOut, kForceStark1, true, kRing>
-                 : k_lens_persist<M, kOut, kForceStark1, false, kRing>;
+      k = staged ? k_lens_persist<M, kOut, kForceStark1, true, kMode>
+                 : k_lens_persist<M, kOut, kForceStark1, false, kMode>;
       break;
     default:
-      k = staged ? k_lens_persist<M, kOut, kForceRadial, true, kRing>
-                 : k_lens_persist<M, kOut, kForceRadial, false, kRing>;
+      k = staged ? k_lens_persist<M, kOut, kForceRadial, true, kMode>
+                 : k_lens_persist<M, kOut, kForceRadial, false, kMode>;
       break;
   }
   const size_t smem = (staged ? size_t(P.lf[i].n_int) * sizeof(float4) : 0) + kPersistThreads * sizeof(SwapSlot);
@@ -493,12 +499,12 @@ int enqueue_persistent(const Plan& P, const RunDev& R, int i, const Queue& Qin, 
   return CTRAJ_OK;
 }
 
-template <bool kOut, bool kRing = false>
+template <bool kOut, int kMode = kModePlain>
 int launch_persistent(ctraj_context* c, const Plan& P, const RunDev& R, int i, const Queue& Qin, const Queue& Qnext,
                       unsigned count, int* launches) {
   int st = c->lens_order.ensure((size_t(kOrderBuckets) + count) * sizeof(unsigned), 25);
   if (st) return st;
-  return enqueue_persistent<kOut, kRing>(P, R, i, Qin, Qnext, c->lens_order.as<unsigned>(), c->sm_count,
+  return enqueue_persistent<kOut, kMode>(P, R, i, Qin, Qnext, c->lens_order.as<unsigned>(), c->sm_count,
                                          c->lens_interval, c->stream, launches);
 }
 
@@ -517,11 +523,12 @@ int launch_all(ctraj_context* c, const Plan& P, const RunDev& R0, Queue* q, int*
   cudaStream_t s = c->stream;
   if (c->timing) CT_CUDA(cudaEventRecord(c->ev[0], s));
   if (n > 0) {
-    auto kf = k_front<MolT, kOut, kRing>;
-    int bps = blocks_per_sm(kf, kThreads, 0);
-    int64_t want = (n + kThreads - 1) / kThreads;
+    auto kf = k_front<MolT, kOut, kRing ? kModeRing : kModePlain>;
+    const int ft = c->front_threads;
+    int bps = blocks_per_sm(kf, ft, 0);
+    int64_t want = (n + ft - 1) / ft;
     int grid = int(std::min<int64_t>(want, int64_t(bps) * c->sm_count * c->front_waves));
-    kf<<<grid, kThreads, 0, s>>>(P, R, q[0]);
+    kf<<<grid, ft, 0, s>>>(P, R, q[0]);
     CT_CUDA(cudaGetLastError());
     ++*launches;
   }
@@ -562,7 +569,7 @@ int launch_all(ctraj_context* c, const Plan& P, const RunDev& R0, Queue* q, int*
     }
     if constexpr (!k64) {
       if (c->lens_mode == CTRAJ_LENS_PERSISTENT) {
-        int st = launch_persistent<kOut, kRing>(c, P, R, i, q[cur], q[nxt], count, launches);
+        int st = launch_persistent<kOut, kRing ? kModeRing : kModePlain>(c, P, R, i, q[cur], q[nxt], count, launches);
         if (st) return st;
         c->host_max[2 + i] = 0;  // no continuation queue
         std::swap(cur, nxt);
@@ -764,6 +771,9 @@ int ctraj_destroy(ctraj_context* c) {
   if (c->peer) ctraj_destroy(c->peer);
   cudaSetDevice(c->device);
   c->l2_flush.release();
+  c->group_ctl.release();
+  c->group_ics.release();
+  if (c->group_host) cudaFreeHost(c->group_host);
   if (c->batch_ev) cudaEventDestroy(c->batch_ev);
   if (c->host_max) cudaFreeHost(c->host_max);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -776,17 +786,21 @@ int ctraj_set_tuning(ctraj_context* c, const ctraj_tuning* t) {
   if (t->chunk_first < 1 || t->chunk_max < t->chunk_first || t->chunk_max > 1000000 ||
       t->chunk_growth < 100 || t->chunk_growth > 1000 || t->front_waves < 1 || t->front_waves > 64 ||
       (t->lens_mode != CTRAJ_LENS_PERSISTENT && t->lens_mode != CTRAJ_LENS_CHUNKED) || t->lens_interval < 1 ||
-      t->lens_interval > 100000)
+      t->lens_interval > 100000 || (t->front_threads != 128 && t->front_threads != 256 && t->front_threads != 512) ||
+      t->batch_group < 1 || t->batch_group > CTRAJ_MAX_BATCH_GROUP)
     return fail(CTRAJ_EINVAL,
                 "tuning out of range (chunk_first %d, chunk_growth %d, chunk_max %d, front_waves %d, lens_mode %d, "
-                "lens_interval %d)",
-                t->chunk_first, t->chunk_growth, t->chunk_max, t->front_waves, t->lens_mode, t->lens_interval);
+                "lens_interval %d, front_threads %d, batch_group %d)",
+                t->chunk_first, t->chunk_growth, t->chunk_max, t->front_waves, t->lens_mode, t->lens_interval,
+                t->front_threads, t->batch_group);
   c->chunk = t->chunk_first;
   c->chunk_growth = t->chunk_growth;
   c->chunk_max = t->chunk_max;
   c->front_waves = t->front_waves;
   c->lens_mode = t->lens_mode;
   c->lens_interval = t->lens_interval;
+  c->front_threads = t->front_threads;
+  c->batch_group = t->batch_group;
   ++c->generation;
   return CTRAJ_OK;
 }
@@ -799,6 +813,8 @@ int ctraj_get_tuning(ctraj_context* c, ctraj_tuning* t) {
   t->front_waves = c->front_waves;
   t->lens_mode = c->lens_mode;
   t->lens_interval = c->lens_interval;
+  t->front_threads = c->front_threads;
+  t->batch_group = c->batch_group;
   return CTRAJ_OK;
 }
 
@@ -995,30 +1011,210 @@ int ctraj_run(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* stats)
   return run_impl(c, a, stats, nullptr);
 }
 
-// One lane of a pipelined batch: runs lane, lane + 2, ... on context x.
+// ---------------------------------------------------------------------------
+// Grouped batches: consecutive runs of ctraj_run_batch whose molecules share
+// one persistent lens pass per lens.  A lens pass ends with a long tail in
+// which only the slowest molecules (the most RK4 steps) are left; sharing the
+// pass lets that tail overlap the bulk of the other runs, so the group costs
+// one tail instead of one per run.  Each molecule carries its run's index in
+// the group; every count and stat goes to its run's own slots, so each run's
+// results are those of ctraj_run.
+// ---------------------------------------------------------------------------
+
+// Whether run a can share the lens pass of a group whose first run is first.
+static bool group_member(const ctraj_context* c, const ctraj_run_args* a, const ctraj_run_args* first) {
+  return a->precision == 32 && a->out_mode == CTRAJ_OUT_NONE && c->lens_mode == CTRAJ_LENS_PERSISTENT &&
+         a->g == first->g;
+}
+
+// Runs a[0..g) as one group on context c; per-run counts go to a[j].counts
+// and stats to stats[j] (may be NULL).  flush > 0: that many bytes of the
+// context's scratch are written before each run's front.  Returns the status
+// of the first failing run (by index) and its index in *failed (-1 if none).
+static int run_group(ctraj_context* c, const ctraj_run_args* a, int g, ctraj_run_stats* stats, uint64_t flush,
+                     int* failed) {
+  *failed = 0;
+  int st;
+  for (int j = 0; j < g; ++j) {
+    *failed = j;
+    if ((st = validate_run(c, &a[j]))) return st;
+  }
+  *failed = 0;
+  CT_CUDA(cudaSetDevice(c->device));
+  cudaStream_t s = c->stream;
+  int64_t total = 0;
+  size_t ic_bytes = 0;
+  for (int j = 0; j < g; ++j) {
+    total += a[j].n;
+    if (a[j].ic_mode == CTRAJ_IC_HOST && a[j].n > 0) ic_bytes += align256(size_t(a[j].n) * 6 * 8);
+  }
+  if (total > int64_t(0x7fffffff)) return fail(CTRAJ_EINVAL, "a batch group holds more than 2^31 molecules");
+  // per-run counts (n_labels + 1 words each, the stride tally_cfg uses) then
+  // per-run stats (kStatCount each)
+  const size_t cw = size_t(c->n_labels + 1), words = size_t(g) * (cw + kStatCount);
+  if ((st = c->group_ctl.ensure(words * 8))) return st;
+  if (words > c->group_host_words) {
+    if (c->group_host) cudaFreeHost(c->group_host);
+    c->group_host = nullptr;
+    c->group_host_words = 0;
+    CT_CUDA(cudaMallocHost(&c->group_host, words * 8));
+    c->group_host_words = words;
+  }
+  if (ic_bytes && (st = c->group_ics.ensure(ic_bytes, 25))) return st;
+  unsigned long long* run_counts = c->group_ctl.as<unsigned long long>();
+  unsigned long long* run_stats = run_counts + size_t(g) * cw;
+  // per run: plan and RunDev (host initial conditions go to their own slice)
+  Plan P;
+  std::vector<RunDev> R(g);
+  size_t ic_off = 0;
+  for (int j = 0; j < g; ++j) {
+    ctraj_run_args aj = a[j];
+    if (aj.ic_mode == CTRAJ_IC_HOST && aj.n > 0) {
+      double* dst = c->group_ics.as<double>(ic_off);
+      CT_CUDA(cudaMemcpyAsync(dst, aj.ics, size_t(aj.n) * 6 * 8, cudaMemcpyHostToDevice, s));
+      ic_off += align256(size_t(aj.n) * 6 * 8);
+      aj.ic_mode = CTRAJ_IC_DEVICE;
+      aj.ics = dst;
+    }
+    if ((st = prepare(c, &aj, P, R[j]))) return st;
+    R[j].counts = run_counts + size_t(j) * cw;
+    R[j].stats = run_stats + size_t(j) * kStatCount;
+    R[j].run_tag = j;
+  }
+  // one set of lens queues for the group, entries tagged with their run
+  const size_t cap = size_t(std::max<int64_t>(total, 1));
+  int n_lens = 0;
+  for (int i = 0; i < P.n_el; ++i) n_lens += P.el[i].type == CTRAJ_ELECTROSTATIC_LENS;
+  const int n_queues = n_lens == 0 ? 1 : (n_lens == 1 ? 2 : 3);
+  for (int k = 0; k < n_queues; ++k)
+    if ((st = c->queue[k].ensure(queue_bytes(cap, 32, true)))) return st;
+  unsigned* ctl = c->qctl.as<unsigned>();
+  Queue q[3];
+  for (int k = 0; k < 3; ++k)
+    layout_queue(&c->queue[std::min(k, n_queues - 1)], cap, 32, ctl + kCtlWords * k, &q[k], true);
+  CT_CUDA(cudaMemsetAsync(c->qctl.p, 0, 4096, s));
+  CT_CUDA(cudaMemsetAsync(run_counts, 0, words * 8, s));
+  bool timing = false;
+  for (int j = 0; j < g; ++j) timing = timing || a[j].timing;
+  int launches = 0;
+  c->timing = timing;
+  if (timing) CT_CUDA(cudaEventRecord(c->ev[0], s));
+  auto kf = k_front<Mol32<false, false>, false, kModeBatch>;
+  const int ft = c->front_threads;
+  const int bps = blocks_per_sm(kf, ft, 0);
+  for (int j = 0; j < g; ++j) {
+    if (flush) CT_CUDA(cudaMemsetAsync(c->l2_flush.p, j & 0xff, size_t(flush), s));
+    if (a[j].n == 0) continue;
+    const int64_t want = (a[j].n + ft - 1) / ft;
+    const int grid = int(std::min<int64_t>(want, int64_t(bps) * c->sm_count * c->front_waves));
+    kf<<<grid, ft, 0, s>>>(P, R[j], q[0]);
+    CT_CUDA(cudaGetLastError());
+    ++launches;
+  }
+  const int fronts = launches;
+  if (timing) CT_CUDA(cudaEventRecord(c->ev[1], s));
+  RunDev Rg = R[0];  // the lens passes: tallies and stats per run
+  Rg.cfg_counts = run_counts;
+  Rg.cfg_stats = run_stats;
+  Rg.counts = nullptr;
+  Rg.stats = nullptr;
+  bool started = false;
+  int cur = 0, nxt = 2;
+  for (int i = 0; i < P.n_el && total > 0; ++i) {
+    if (P.el[i].type != CTRAJ_ELECTROSTATIC_LENS) continue;
+    CT_CUDA(cudaMemcpyAsync(c->host_max, q[cur].count, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    CT_CUDA(cudaStreamSynchronize(s));
+    const unsigned count = c->host_max[0];
+    if (count == 0) break;
+    if (timing && !started) CT_CUDA(cudaEventRecord(c->ev[2], s));
+    started = true;
+    CT_CUDA(cudaMemsetAsync(q[nxt].count, 0, kCtlWords * sizeof(unsigned), s));
+    if ((st = launch_persistent<false, kModeBatch>(c, P, Rg, i, q[cur], q[nxt], count, &launches))) return st;
+    std::swap(cur, nxt);
+  }
+  if (timing) {
+    if (!started) CT_CUDA(cudaEventRecord(c->ev[2], s));
+    CT_CUDA(cudaEventRecord(c->ev[3], s));
+  }
+  CT_CUDA(cudaMemcpyAsync(c->group_host, run_counts, words * 8, cudaMemcpyDeviceToHost, s));
+  CT_CUDA(cudaStreamSynchronize(s));
+  float front_ms = 0.f, lens_ms = 0.f;
+  if (timing) {
+    CT_CUDA(cudaEventElapsedTime(&front_ms, c->ev[0], c->ev[1]));
+    CT_CUDA(cudaEventElapsedTime(&lens_ms, c->ev[2], c->ev[3]));
+  }
+  int linear = 0;
+  for (int i = 0; i < P.n_el; ++i) linear += P.el[i].type == CTRAJ_ELECTROSTATIC_LENS && P.lf[i].force == kForceStark2Lin;
+  int status = CTRAJ_OK;
+  *failed = -1;
+  for (int j = 0; j < g; ++j) {
+    const unsigned long long* hc = c->group_host + size_t(j) * cw;
+    const unsigned long long* hs = c->group_host + size_t(g) * cw + size_t(j) * kStatCount;
+    for (int k = 0; k <= c->n_labels; ++k) a[j].counts[k] = int64_t(hc[k]);
+    if (stats) {
+      ctraj_run_stats& o = stats[j];
+      std::memset(&o, 0, sizeof o);
+      o.molecules = a[j].n;
+      o.molecule_steps = int64_t(hs[kStatSteps]);
+      o.lens_steps = int64_t(hs[kStatLensSteps]);
+      o.max_lens_steps = int32_t(hs[kStatMaxSteps]);
+      o.linear_tables = linear;
+      o.edge_band = -1;
+      o.table_range = int64_t(hs[kStatTableRange]);
+      o.bad_steps = int64_t(hs[kStatBadSteps]);
+      // each run its front launch; the group's shared launches are credited to its first run
+      o.kernels = (a[j].n > 0 ? 1 : 0) + (j == 0 ? launches - fronts : 0);
+      if (timing) {  // the group's kernel times, shared out evenly
+        o.timed = 1;
+        o.front_ms = front_ms / float(g);
+        o.lens_ms = lens_ms / float(g);
+      }
+    }
+    if (status == CTRAJ_OK && hs[kStatRangeError]) {
+      status = fail(CTRAJ_ERANGE, "%llu molecules looked up the lens table above its last knot "
+                    "(interp1d would raise ValueError)", hs[kStatRangeError]);
+      *failed = j;
+    } else if (status == CTRAJ_OK && hs[kStatBadSteps]) {
+      status = fail(CTRAJ_ESTEPS, "%llu molecules have a non-finite or oversize lens step count rint(L/dz)",
+                    hs[kStatBadSteps]);
+      *failed = j;
+    }
+  }
+  return status;
+}
+
+// One lane of a pipelined batch: groups lane, lane + 2, ... of `groups`
+// (first run, run count) on context x.
 struct BatchLane {
   int status = CTRAJ_OK;
   int run = -1;
   std::string error;
 };
 
-static void batch_lane(ctraj_context* x, const ctraj_run_args* a, int32_t n_runs, int lane,
-                       ctraj_run_stats* stats, uint64_t flush, BatchLane* out) {
+static void batch_lane(ctraj_context* x, const ctraj_run_args* a, const std::vector<std::pair<int, int>>* groups,
+                       int lane, ctraj_run_stats* stats, uint64_t flush, BatchLane* out) {
   int st = CTRAJ_OK;
-  int k = lane;
+  int run = -1;
   if (cudaSetDevice(x->device) != cudaSuccess) st = fail(CTRAJ_ECUDA, "cudaSetDevice(%d) failed", x->device);
   if (!st && flush) st = x->l2_flush.ensure(size_t(flush));
-  for (; !st && k < n_runs; k += 2) {
+  for (size_t gi = size_t(lane); !st && gi < groups->size(); gi += 2) {
+    const int k = (*groups)[gi].first, g = (*groups)[gi].second;
+    run = k;
+    if (g > 1) {
+      int bad = -1;
+      st = run_group(x, a + k, g, stats ? stats + k : nullptr, flush, &bad);
+      if (st) run = k + std::max(bad, 0);
+      continue;
+    }
     if (flush) {
       const cudaError_t e = cudaMemsetAsync(x->l2_flush.p, k & 0xff, size_t(flush), x->stream);
       if (e != cudaSuccess) st = fail(CTRAJ_ECUDA, "L2 flush: %s", cudaGetErrorString(e));
     }
     if (!st) st = run_impl(x, a + k, stats ? stats + k : nullptr, nullptr);
-    if (st) break;
   }
   if (st) {
     out->status = st;
-    out->run = k;
+    out->run = run;
     out->error = g_error;
   }
 }
@@ -1051,6 +1247,8 @@ static int batch_peer(ctraj_context* c) {
     p->front_waves = c->front_waves;
     p->lens_mode = c->lens_mode;
     p->lens_interval = c->lens_interval;
+    p->front_threads = c->front_threads;
+    p->batch_group = c->batch_group;
     ++p->generation;
     c->peer_generation = c->generation;
   }
@@ -1064,9 +1262,24 @@ int ctraj_run_batch(ctraj_context* c, const ctraj_run_args* a, int32_t n_runs, c
   if (l2_flush_bytes > (uint64_t(1) << 34)) return fail(CTRAJ_EINVAL, "l2_flush_bytes above 16 GiB");
   if (n_runs == 0) return CTRAJ_OK;
   CT_CUDA(cudaSetDevice(c->device));
+  // consecutive runs form groups of up to batch_group that share lens passes
+  std::vector<std::pair<int, int>> groups;
+  for (int k = 0; k < n_runs;) {
+    int g = 1;
+    if (c->batch_group > 1 && a[k].n >= 0 && group_member(c, &a[k], &a[k])) {
+      int64_t total = a[k].n;
+      while (g < c->batch_group && k + g < n_runs && a[k + g].n >= 0 && group_member(c, &a[k + g], &a[k]) &&
+             total + a[k + g].n <= int64_t(0x7fffffff)) {
+        total += a[k + g].n;
+        ++g;
+      }
+    }
+    groups.emplace_back(k, g);
+    k += g;
+  }
   BatchLane lanes[2];
-  if (n_runs == 1) {
-    batch_lane(c, a, 1, 0, stats, l2_flush_bytes, &lanes[0]);
+  if (groups.size() == 1) {
+    batch_lane(c, a, &groups, 0, stats, l2_flush_bytes, &lanes[0]);
   } else {
     int st = batch_peer(c);
     if (st) return st;
@@ -1078,13 +1291,13 @@ int ctraj_run_batch(ctraj_context* c, const ctraj_run_args* a, int32_t n_runs, c
     bool threaded = true;
     std::thread second;
     try {
-      second = std::thread(batch_lane, c->peer, a, n_runs, 1, stats, l2_flush_bytes, &lanes[1]);
+      second = std::thread(batch_lane, c->peer, a, &groups, 1, stats, l2_flush_bytes, &lanes[1]);
     } catch (const std::system_error&) {
       threaded = false;  // no thread to be had: the lanes run one after the other
     }
-    batch_lane(c, a, n_runs, 0, stats, l2_flush_bytes, &lanes[0]);
+    batch_lane(c, a, &groups, 0, stats, l2_flush_bytes, &lanes[0]);
     if (threaded) second.join();
-    else batch_lane(c->peer, a, n_runs, 1, stats, l2_flush_bytes, &lanes[1]);
+    else batch_lane(c->peer, a, &groups, 1, stats, l2_flush_bytes, &lanes[1]);
     // and later work on ctx's stream after all of it
     CT_CUDA(cudaEventRecord(c->peer->batch_ev, c->peer->stream));
     CT_CUDA(cudaStreamWaitEvent(c->stream, c->peer->batch_ev, 0));
@@ -1302,12 +1515,13 @@ int sweep_enqueue(ctraj_context* c, const Plan& P, const RunDev& R, const SweepL
   if (c->timing) CT_CUDA(record(c->ev[0]));
   if (R.n > 0) {
     auto kf = k_sweep_front<Mol32<false, false>>;
-    const int bps = blocks_per_sm(kf, kThreads, 0);
-    const int64_t want = (R.n + kThreads - 1) / kThreads;
+    const int ft = c->front_threads;
+    const int bps = blocks_per_sm(kf, ft, 0);
+    const int64_t want = (R.n + ft - 1) / ft;
     const int grid = int(std::min<int64_t>(want, int64_t(bps) * c->sm_count * c->front_waves));
     SweepQueues Qs{};
     for (int t = 0; t < W.n_tab; ++t) Qs.q[t] = W.qa[t];
-    kf<<<grid, kThreads, 0, s>>>(P, R, Qs, W.n_tab);
+    kf<<<grid, ft, 0, s>>>(P, R, Qs, W.n_tab);
     CT_CUDA(cudaGetLastError());
     ++launches;
   }
@@ -1557,6 +1771,7 @@ extern "C" int ctraj_run_sweep(ctraj_context* c, const ctraj_sweep* sw, const ct
   put(W.chunks.data(), W.chunks.size() * sizeof(int));
   put(&c->lens_mode, sizeof c->lens_mode);
   put(&c->lens_interval, sizeof c->lens_interval);
+  put(&c->front_threads, sizeof c->front_threads);
   put(&W.force, sizeof W.force);
   const bool same = key == c->sweep_key;
   cudaStream_t s = c->stream;

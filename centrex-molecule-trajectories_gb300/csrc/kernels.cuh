@@ -35,6 +35,7 @@ namespace ctraj {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kThreads = 256;
+constexpr int kFrontMaxThreads = 512;  // k_front is launched with 128-512 threads (tuning)
 // Lens chunks: 512 threads, 2 CTAs per SM (<= 64 registers): 32 warps share
 // two copies of the staged table (2 x 64 KiB for 4096 knots).
 constexpr int kLensThreads = 512;
@@ -90,6 +91,19 @@ __device__ __forceinline__ int find_cfg(const RunDev& R, int64_t i) {
     else hi = mid - 1;
   }
   return lo;
+}
+
+// Per-run stats of a grouped batch (all 32 lanes call; run < 0: nothing to
+// add): lanes of the same run are combined, one global atomic per run and
+// nonzero stat.  Sums fit in 32 bits per warp (steps of one molecule < 2^26).
+__device__ __forceinline__ void stats_run(const RunDev& R, int run, const unsigned (&v)[kStatMaxSteps]) {
+  const unsigned peers = __match_any_sync(kFull, run);
+  const bool leader = run >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1;
+#pragma unroll
+  for (int k = 0; k < kStatMaxSteps; ++k) {
+    const unsigned t = __reduce_add_sync(peers, v[k]);
+    if (leader && t) atomicAdd(&R.cfg_stats[size_t(run) * kStatCount + k], (unsigned long long)t);
+  }
 }
 
 __device__ __forceinline__ void tally_flush(BlockTally& S, const RunDev& R, int n_labels) {
@@ -157,9 +171,14 @@ enum : int { kTagNone = 0, kTagCarry = 1, kTagSlot = 2 };
 
 // Append the lanes with push == true to Q and raise Q's largest remaining
 // step count (all lanes call).  Returns the lane's slot.
+//
+// run_max (grouped batch): where the largest step bound of this lane's run is
+// kept (per lane, so lanes of different runs may push together); warp_max:
+// the same for a warp whose lanes all belong to one run (one atomic).
 template <int kTag = kTagNone, class M>
 __device__ __forceinline__ unsigned push_lens(const Queue& Q, bool push, const M& m, const LensStep& st,
-                                              int tag = 0) {
+                                              int tag = 0, unsigned long long* run_max = nullptr,
+                                              unsigned long long* warp_max = nullptr) {
   const unsigned slot = queue_slot(push, Q.count);
   if (push) {
     m.store(Q, slot, st);
@@ -168,7 +187,11 @@ __device__ __forceinline__ unsigned push_lens(const Queue& Q, bool push, const M
   }
   const unsigned rem = push ? unsigned(st.n_total < 0 ? st.bound : st.n_total - st.n_done) : 0u;
   const unsigned wmax = __reduce_max_sync(kFull, rem);
-  if ((threadIdx.x & 31) == 0 && wmax) atomicMax(Q.max_steps, wmax);
+  if ((threadIdx.x & 31) == 0 && wmax) {
+    atomicMax(Q.max_steps, wmax);
+    if (warp_max) atomicMax(warp_max, (unsigned long long)wmax);
+  }
+  if (run_max && rem) atomicMax(run_max, (unsigned long long)rem);
   return slot;
 }
 
@@ -191,11 +214,15 @@ __device__ __forceinline__ void ring_entry(const ctraj_ring& G, unsigned long lo
 }
 
 // ---------------------------------------------------------------------------
-// kRing (FP32 ring recording): the molecules queued at the recorded lens
+// kModeRing (FP32 ring recording): the molecules queued at the recorded lens
 // (the first lens) get their queue slot as record slot, and those stopped by
-// its entrance test are appended to the ring at once.
-template <class M, bool kOut, bool kRing = false>
-__global__ void __launch_bounds__(kThreads) k_front(const __grid_constant__ Plan P, const RunDev R,
+// its entrance test are appended to the ring at once.  kModeBatch (grouped
+// batch): the lens entrants carry the run's tag R.run_tag, and the largest
+// step bound queued is kept in the run's stats (counts and stats go to the
+// run's own slots through R.counts / R.stats).  The block size is a launch
+// parameter (at most kFrontMaxThreads).
+template <class M, bool kOut, int kMode = kModePlain>
+__global__ void __launch_bounds__(kFrontMaxThreads) k_front(const __grid_constant__ Plan P, const RunDev R,
                                                     const Queue Q) {
   __shared__ BlockTally S;
   tally_init(S);
@@ -221,11 +248,12 @@ __global__ void __launch_bounds__(kThreads) k_front(const __grid_constant__ Plan
         band += (m.margin < double(kEdgeBand)) ? 1 : 0;
         write_outputs<M, kOut>(R, m, label);
       }
-      if constexpr (kRing) {  // listed; k_ring_reserve / k_ring_write append them
+      if constexpr (kMode == kModeRing) {  // listed; k_ring_reserve / k_ring_write append them
         if (label == R.rec_entrance_label && lens_at == R.rec_lens) R.ent_id[atomicAdd(R.ent_count, 1u)] = int32_t(i);
       }
     }
-    push_lens<kRing ? kTagSlot : kTagNone>(Q, label == kQueued, m, st);
+    push_lens<kMode == kModeRing ? kTagSlot : (kMode == kModeBatch ? kTagCarry : kTagNone)>(
+        Q, label == kQueued, m, st, R.run_tag, nullptr, kMode == kModeBatch ? R.stats + kStatMaxSteps : nullptr);
     tally_warp(S, label, P.n_labels);
   }
   stat_add(S, kStatSteps, steps);
@@ -239,7 +267,7 @@ __global__ void __launch_bounds__(kThreads) k_front(const __grid_constant__ Plan
 // (cfg_table[c]), and every tally is also kept per configuration.  The sweep
 // beamline has one lens, so a molecule queued here is at that lens.
 template <class M>
-__global__ void __launch_bounds__(kThreads) k_sweep_front(const __grid_constant__ Plan P, const RunDev R,
+__global__ void __launch_bounds__(kFrontMaxThreads) k_sweep_front(const __grid_constant__ Plan P, const RunDev R,
                                                           const __grid_constant__ SweepQueues Qs,
                                                           const int n_tables) {
   __shared__ BlockTally S;
@@ -568,16 +596,20 @@ struct PersistAcc {
 // One CTA's share of a persistent pass over Qin.  The first static_entries
 // queue positions are dealt out interleaved across CTAs (entry (w * grid +
 // b) * 32 + lane to lane `lane` of warp w of CTA b); the rest are taken in
-// order by the lanes that become idle.  kSweep: molecules carry their
+// order by the lanes that become idle.  kModeSweep: molecules carry their
 // configuration (Queue::cfg), whose beta and kappa scale the unscaled table,
-// and tallies are also kept per configuration.  Every thread of the CTA
-// calls it; it returns with all of the CTA's molecules finalised.
-template <class M, bool kOut, int F, bool kStaged, bool kSweep, bool kRing = false>
+// and tallies are also kept per configuration.  kModeBatch: molecules carry
+// their run (Queue::cfg) and every tally and stat goes to that run's slots
+// (RunDev::cfg_counts, cfg_stats).  Every thread of the CTA calls it; it
+// returns with all of the CTA's molecules finalised.
+template <class M, bool kOut, int F, bool kStaged, int kMode>
 __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, const int li, const Queue& Qin,
                                              const Queue& Qnext, const LensArgs& L, const unsigned* order,
                                              const int interval, const unsigned static_entries,
                                              const float4* s_tab, SwapSlot* s_swap, unsigned* s_wcount,
                                              BlockTally& S, PersistAcc& acc) {
+  constexpr bool kSweep = kMode == kModeSweep, kRing = kMode == kModeRing, kBatch = kMode == kModeBatch;
+  constexpr int kNextTag = kMode == kModePlain ? kTagNone : kTagCarry;
   const unsigned n_in = *(volatile unsigned*)Qin.count;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned lanes_lt = (1u << lane) - 1u;
@@ -590,7 +622,7 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
   int phase = kIdle;
   unsigned flags = 0;
   float dt = 0.f, hdt = 0.f, c2 = 0.f, dt6 = 0.f, dt26 = 0.f;
-  int n0 = 0, cfg = 0;  // cfg: the configuration (kSweep) or the record slot (kRing)
+  int n0 = 0, cfg = 0;  // cfg: the configuration (sweep), the record slot (ring) or the run (batch)
   float beta = 0.f, kappa = 1.f;
   bool fresh = false;
   unsigned idx = 0;
@@ -612,7 +644,7 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
     idx = order ? __ldg(order + j) : j;
     flags = 0;
     m.load_state(Qin, idx, P, st);
-    if (kSweep || kRing) cfg = Qin.cfg[idx];
+    if (kMode != kModePlain) cfg = Qin.cfg[idx];
     if constexpr (kRing) {
       if (rec_on) {  // the entrance state opens the record
         to_rec = R.rec_stride - st.n_done % R.rec_stride;
@@ -653,6 +685,8 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
     if (!__any_sync(kFull, phase == kLost || phase == kExit || phase == kBad)) return;
     int label = kNone;
     bool enter = false;
+    // this lane's additions to the stats (kStat* order up to kStatRangeError)
+    unsigned d[kStatMaxSteps] = {0u, 0u, 0u, 0u, 0u, 0u};
     if (phase == kLost || phase == kExit || phase == kBad) {
       m.load_rest(Qin, idx, st, !fresh);
       if constexpr (kRing) {
@@ -672,15 +706,15 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
           }
         }
       }
-      acc.lsteps += unsigned(st.n_done - n0);
+      d[kStatLensSteps] = unsigned(st.n_done - n0);
       if (phase == kBad) {  // rint(L/dz) not usable: the reference raises here
         label = e.label_inside;
-        ++acc.bad;
-        acc.steps += unsigned(m.rows);
+        d[kStatBadSteps] = 1;
+        d[kStatSteps] = unsigned(m.rows);
         write_outputs<M, kOut>(R, m, label);
       } else {
-        acc.range += (flags & 1u) ? 1 : 0;
-        acc.rerr += (flags & 2u) ? 1 : 0;
+        d[kStatTableRange] = (flags & 1u) ? 1 : 0;
+        d[kStatRangeError] = (flags & 2u) ? 1 : 0;
         m.lens_end(P, li, st, phase == kLost);
         if (phase == kLost) {
           label = e.label_inside;
@@ -691,21 +725,35 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
             enter = enter_lens(m, P, lens_at, nst);
             if (!enter) {
               label = P.el[lens_at].label_inside;
-              ++acc.bad;
+              d[kStatBadSteps] += 1;
             }
           }
         }
         if (label != kQueued) {
-          acc.steps += unsigned(m.rows);
-          acc.band += (m.margin < double(kEdgeBand)) ? 1 : 0;
+          d[kStatSteps] = unsigned(m.rows);
+          d[kStatEdgeBand] = (m.margin < double(kEdgeBand)) ? 1 : 0;
           write_outputs<M, kOut>(R, m, label);
         }
       }
       phase = kIdle;
     }
-    push_lens<(kSweep || kRing) ? kTagCarry : kTagNone>(Qnext, enter, m, nst, cfg);
-    tally_warp(S, label, P.n_labels);
-    if (kSweep) tally_cfg(R, cfg, label, P.n_labels);
+    if constexpr (kBatch) {
+      push_lens<kNextTag>(Qnext, enter, m, nst, cfg, enter ? R.cfg_stats + size_t(cfg) * kStatCount + kStatMaxSteps
+                                                              : nullptr);
+      const bool done = label != kNone;
+      stats_run(R, done ? cfg : -1, d);
+      tally_cfg(R, cfg, label, P.n_labels);
+    } else {
+      acc.steps += d[kStatSteps];
+      acc.lsteps += d[kStatLensSteps];
+      acc.band += d[kStatEdgeBand];
+      acc.bad += d[kStatBadSteps];
+      acc.range += d[kStatTableRange];
+      acc.rerr += d[kStatRangeError];
+      push_lens<kNextTag>(Qnext, enter, m, nst, cfg);
+      tally_warp(S, label, P.n_labels);
+      if (kSweep) tally_cfg(R, cfg, label, P.n_labels);
+    }
   };
 
   {
@@ -798,7 +846,7 @@ __device__ __forceinline__ void persist_flush(BlockTally& S, const RunDev& R, in
   tally_flush(S, R, n_labels);
 }
 
-template <class M, bool kOut, int F, bool kStaged, bool kRing = false>
+template <class M, bool kOut, int F, bool kStaged, int kMode = kModePlain>
 __global__ void __launch_bounds__(kPersistThreads, 1) k_lens_persist(const __grid_constant__ Plan P, const RunDev R,
                                                                      const int li, const Queue Qin, const Queue Qnext,
                                                                      const LensArgs L, const unsigned* order,
@@ -814,9 +862,9 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_lens_persist(const __gri
   __syncthreads();
   PersistAcc acc;
   // a short queue spreads over all SMs through the interleaved first entries
-  persist_pass<M, kOut, F, kStaged, false, kRing>(P, R, li, Qin, Qnext, L, order, interval,
-                                                  gridDim.x * kPersistThreads, s_dyn, s_swap, s_wcount, S, acc);
-  persist_flush(S, R, P.n_labels, acc);
+  persist_pass<M, kOut, F, kStaged, kMode>(P, R, li, Qin, Qnext, L, order, interval,
+                                            gridDim.x * kPersistThreads, s_dyn, s_swap, s_wcount, S, acc);
+  if (kMode != kModeBatch) persist_flush(S, R, P.n_labels, acc);  // a batch's tallies went to its runs
 }
 
 // Batched sweep: the Stark tables' lens queues in one launch.  Each CTA
@@ -875,8 +923,8 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_sweep_persist(const __gr
     L.n_int = T.n_int[t];
     L.n_smem = kStaged ? T.n_int[t] : 0;
     // no interleaved first entries: each CTA takes from its table's queue in order
-    persist_pass<M, false, F, kStaged, true>(P, R, li, Q, Q, L, T.order[t], interval, 0u, s_dyn, s_swap, s_wcount,
-                                            S, acc);
+    persist_pass<M, false, F, kStaged, kModeSweep>(P, R, li, Q, Q, L, T.order[t], interval, 0u, s_dyn, s_swap,
+                                                  s_wcount, S, acc);
   }
   persist_flush(S, R, P.n_labels, acc);
 }

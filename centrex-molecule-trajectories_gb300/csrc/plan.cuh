@@ -130,6 +130,13 @@ struct RunDev {
   const float* cfg_kappa;     // n_cfg
   const int32_t* cfg_table;   // n_cfg: which lens queue / table
   unsigned long long* cfg_counts;  // n_cfg x (n_labels + 1)
+  // grouped batch (ctraj_run_batch): the runs of a group share one lens
+  // queue; a molecule carries its run's index in the group (Queue::cfg, set
+  // by the run's front launch from run_tag), its counts go to cfg_counts and
+  // its stats to cfg_stats (runs x kStatCount), both indexed by that run.
+  int run_tag;
+  int pad5;
+  unsigned long long* cfg_stats;
   // ring recording (ctraj_run_ring): the molecules reaching lens rec_lens get
   // a record slot (their queue position at the front, carried in Queue::cfg);
   // (x, y, vx, vy) is staged every rec_stride RK4 steps, and the molecules
@@ -160,8 +167,14 @@ enum : int {
   kStatTableRange = 3,
   kStatBadSteps = 4,
   kStatRangeError = 5,
+  kStatMaxSteps = 6,  // grouped batch: largest step bound queued at a lens (atomicMax, not a sum)
   kStatCount = 8,
 };
+
+// Kernel modes: a plain run, a batched sweep (molecules carry their lens
+// configuration), ring recording (molecules carry their record slot), a
+// grouped batch (molecules carry their run).
+enum : int { kModePlain = 0, kModeSweep = 1, kModeRing = 2, kModeBatch = 3 };
 
 // Molecules inside a lens between two chunks of RK4 steps (SoA, capacity n):
 // the state, the carried rounding errors of the FP32 integration, and the

@@ -15,7 +15,7 @@ PKG_DIR = Path(__file__).resolve().parent
 LIB_DIR = PKG_DIR / "_lib"
 LIB_PATH = LIB_DIR / "libctraj.so"
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 # status codes
 OK = 0
@@ -146,6 +146,8 @@ class Tuning(ctypes.Structure):
         ("front_waves", ctypes.c_int32),
         ("lens_mode", ctypes.c_int32),
         ("lens_interval", ctypes.c_int32),
+        ("front_threads", ctypes.c_int32),
+        ("batch_group", ctypes.c_int32),
     ]
 
 
@@ -255,6 +257,7 @@ SIGNATURES = {
 # ctraj_run_noalloc limits (include/ctraj.h)
 NOALLOC_MAX_MOLECULES = 131072
 NOALLOC_MAX_INTERVALS = 16384
+MAX_BATCH_GROUP = 64
 NOALLOC_SCRATCH_BYTES = 32 << 20
 
 

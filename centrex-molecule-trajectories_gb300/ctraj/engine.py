@@ -78,11 +78,13 @@ class Engine:
         _abi.check(self.lib.ctraj_synchronize(self.ctx), self.lib)
 
     def set_tuning(self, chunk_first: int = 64, chunk_growth: int = 200, chunk_max: int = 1024,
-                   front_waves: int = 4, lens_mode: int = _abi.LENS_PERSISTENT, lens_interval: int = 256):
-        """ctraj_set_tuning: chunked-lens knobs, front grid, and the FP32 lens
-        pass (persistent or chunked) with its compaction interval."""
+                   front_waves: int = 4, lens_mode: int = _abi.LENS_PERSISTENT, lens_interval: int = 256,
+                   front_threads: int = 256, batch_group: int = 4):
+        """ctraj_set_tuning: chunked-lens knobs, front grid and block size, the
+        FP32 lens pass (persistent or chunked) with its compaction interval, and
+        the runs of a batch that share one lens pass."""
         t = _abi.Tuning(int(chunk_first), int(chunk_growth), int(chunk_max), int(front_waves), int(lens_mode),
-                        int(lens_interval))
+                        int(lens_interval), int(front_threads), int(batch_group))
         _abi.check(self.lib.ctraj_set_tuning(self.ctx, ctypes.byref(t)), self.lib)
 
     def get_tuning(self) -> dict:
@@ -232,7 +234,9 @@ class Engine:
                   l2_flush_bytes: int = 0) -> list:
         """ctraj_run_batch: one run per entry of ``seeds`` (with device draws) or
         of ``ics`` (a list of (6, n) arrays or tensors), pipelined over two
-        lanes; result k equals ``run(cb, n, seed=seeds[k], ...)``."""
+        lanes, groups of ``batch_group`` runs sharing each lens pass; result k
+        equals ``run(cb, n, seed=seeds[k], ...)``.  ``n`` is one molecule count
+        for every run or a list of them."""
         self.load(cb)
         if ics is not None:
             ics_list = list(ics)
@@ -243,13 +247,16 @@ class Engine:
             seeds = list(seeds)
             ics_list = [None] * len(seeds)
         n_runs = len(seeds)
+        ns = [int(x) for x in n] if np.ndim(n) else [int(n)] * n_runs
+        if len(ns) != n_runs:
+            raise ValueError("one molecule count per run")
         nl = len(cb.labels)
         args = (_abi.RunArgs * max(n_runs, 1))()
         stats = (_abi.RunStats * max(n_runs, 1))()
         counts = [np.zeros(nl + 1, np.int64) for _ in range(n_runs)]
         keep = []
         for k in range(n_runs):
-            a, kk = self._args(n, precision, ics_list[k], xdist, vdist, seeds[k], offset, g)
+            a, kk = self._args(ns[k], precision, ics_list[k], xdist, vdist, seeds[k], offset, g)
             a.timing = 1 if timing else 0
             a.counts = counts[k].ctypes.data
             args[k] = a

@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define CTRAJ_ABI_VERSION 1
+#define CTRAJ_ABI_VERSION 2
 
 /* ---- status codes -------------------------------------------------------- */
 enum {
@@ -242,7 +242,9 @@ int ctraj_set_beamline(ctraj_context* ctx, const ctraj_element* elements,
                        int32_t n_elements, int32_t n_labels);
 
 /* Launch tuning of a context.  No reference counterpart: these are the knobs
- * of this engine's kernels, set by the Python autotuner (ctraj.tuning).
+ * of this engine's kernels, set by the Python autotuner (ctraj.tuning); the
+ * closest reference analogue is its chunking of N_traj into 100 * n_jobs
+ * tasks (trajectory_simulator.py:47-49).  Results never depend on them.
  *   chunk_first   RK4 steps of the first lens chunk (molecules still inside the
  *                 lens are compacted between chunks)            default 64
  *   chunk_growth  each chunk is this many percent of the previous  default 200
@@ -255,8 +257,18 @@ int ctraj_set_beamline(ctraj_context* ctx, const ctraj_element* elements,
  *                 between).  FP64 runs are always chunked.  Results (and ring
  *                 records) do not depend on it.             default persistent
  *   lens_interval persistent mode: RK4 steps between the CTA's compactions
- *                 once the lens queue is empty                   default 256 */
+ *                 once the lens queue is empty                   default 256
+ *   front_threads threads per block of the ballistic front kernel: 128, 256
+ *                 or 512                                          default 256
+ *   batch_group   ctraj_run_batch: consecutive runs (1-64) whose molecules
+ *                 share one persistent lens pass per lens, so the slowest
+ *                 molecules of one run (the pass's critical path) overlap the
+ *                 bulk of the others.  Applies to FP32 runs without
+ *                 per-molecule outputs in persistent lens mode; other runs,
+ *                 and batch_group 1, run one at a time.           default 4 */
 enum { CTRAJ_LENS_PERSISTENT = 0, CTRAJ_LENS_CHUNKED = 1 };
+
+#define CTRAJ_MAX_BATCH_GROUP 64
 
 typedef struct ctraj_tuning {
   int32_t chunk_first;
@@ -265,6 +277,8 @@ typedef struct ctraj_tuning {
   int32_t front_waves;
   int32_t lens_mode;
   int32_t lens_interval;
+  int32_t front_threads;
+  int32_t batch_group;
 } ctraj_tuning;
 
 int ctraj_set_tuning(ctraj_context* ctx, const ctraj_tuning* tuning);

@@ -39,6 +39,50 @@ def _same(batch, alone):
         assert b.extra["max_lens_steps"] == a.extra["max_lens_steps"]
 
 
+@pytest.mark.parametrize("group", [1, 2, 3, 16])
+def test_grouped_batch_equals_single_runs(engine, group):
+    """Runs sharing lens passes (batch_group > 1) give each run's own results;
+    groups of 2 and 3 over 7 runs leave a partial last group, 16 takes them all."""
+    cb = compile_beamline(lens_beamline())
+    xs, vs = _specs()
+    n = 150_000
+    seeds = [101 + 13 * k for k in range(7)]
+    alone = [engine.run(cb, n + 1000 * k, xdist=xs, vdist=vs, seed=s, offset=3) for k, s in enumerate(seeds)]
+    try:
+        engine.set_tuning(batch_group=group, front_threads=128 if group == 3 else 256)
+        batch = engine.run_batch(cb, [n + 1000 * k for k in range(7)], seeds, xdist=xs, vdist=vs, offset=3)
+    finally:
+        engine.set_tuning()
+    _same(batch, alone)
+
+
+def test_grouped_batch_two_lenses_and_host_ics(engine):
+    """A group over a two-lens beamline (the second lens's entrants carry their
+    run through the first lens pass) with initial conditions from the host."""
+    import ctraj
+    from ctraj.distributions import host_draw
+    from ctraj.stark import hexapole_force
+
+    f = hexapole_force(V=30e3, R=17.5e-3, splitting_hz=6.7e9)
+    bl = ctraj.Beamline([ctraj.CircularAperture(name="A1", z0=0.30, L=1e-3, d=12e-3),
+                         ctraj.ElectrostaticLens(name="ES lens", z0=0.8, L=0.3, d=35e-3, V=30e3, dt=1e-6, a_interp=f),
+                         ctraj.ElectrostaticLens(name="ES lens 2", z0=1.3, L=0.3, d=35e-3, V=30e3, dt=1e-6,
+                                                 a_interp=f),
+                         ctraj.CircularAperture(name="Detection plane", z0=3.0, L=0.0, d=float("inf"))])
+    cb = compile_beamline(bl)
+    xd, vd = source()
+    n = 120_000
+    ics = [host_draw(xd, vd, n, seed=40 + k) for k in range(5)]
+    alone = [engine.run(cb, n, ics=a) for a in ics]
+    try:
+        engine.set_tuning(batch_group=4)
+        batch = engine.run_batch(cb, n, None, ics=ics)
+    finally:
+        engine.set_tuning()
+    _same(batch, alone)
+    assert alone[0].counts[cb.labels.index("Inside lens")] > 0
+
+
 @pytest.mark.parametrize("n_runs", [0, 1, 2, 5])
 def test_batch_equals_single_runs(engine, n_runs):
     cb = compile_beamline(lens_beamline())
