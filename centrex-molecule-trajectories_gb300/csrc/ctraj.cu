@@ -121,6 +121,7 @@ struct ctraj_context {
   int lens_interval = 256;      // persistent mode: steps between CTA compactions
   int front_threads = 256;      // k_front block size
   int batch_group = 4;          // ctraj_run_batch: runs sharing one lens pass
+  int lens_threads = 512;       // persistent FP32 lens pass: threads per CTA
   unsigned run_max_steps = 0;   // largest lens queue step bound of the last run
   bool timing = false;
   // before front, after front, before the first lens chunk, after the last one
@@ -433,6 +434,23 @@ int blocks_per_sm(KernelT k, int threads, size_t smem) {
   return b;
 }
 
+// k_front over n molecules into queue Q: threads per block, a grid of
+// `waves` x resident CTAs (or fewer), the staging area for lens entrants in
+// dynamic shared memory.
+template <class M, bool kOut, int kMode>
+int launch_front(const Plan& P, const RunDev& R, const Queue& Q, int64_t n, int threads, int sms, int waves,
+                 cudaStream_t s) {
+  auto kf = k_front<M, kOut, kMode>;
+  const size_t smem = front_smem<M>(threads);
+  CT_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  const int bps = blocks_per_sm(kf, threads, smem);
+  const int64_t want = (n + threads - 1) / threads;
+  const int grid = int(std::min<int64_t>(want, int64_t(bps) * sms * waves));
+  kf<<<grid, threads, smem, s>>>(P, R, Q);
+  CT_CUDA(cudaGetLastError());
+  return CTRAJ_OK;
+}
+
 // The lens kernel for lens element i: FP32 is specialised on the force law,
 // FP64 evaluates the reference's force code for every table kind.
 using LensKernel = void (*)(const Plan, const RunDev, const int, const Queue, const Queue,
@@ -458,34 +476,49 @@ LensKernel lens_kernel(int force, bool staged) {
 // The persistent FP32 lens pass of lens element i over queue Qin: order the
 // entrants longest first into `order_buf` (kOrderBuckets + the queue's
 // entries), then one k_lens_persist launch, one CTA per SM.  kMode: plain,
-// ring recording or grouped batch.
+// ring recording or grouped batch.  threads: CTA size (tuning lens_threads);
+// 768 and 1024 are compiled for the staged-table plain and batch passes
+// without per-molecule outputs (the throughput path), 512 for every pass.
+using PersistKernel = void (*)(const Plan, const RunDev, const int, const Queue, const Queue, const LensArgs,
+                               const unsigned*, const int);
+
+template <bool kOut, int F, bool kStaged, int kMode>
+PersistKernel persist_kernel(int threads, int* used) {
+  using M = Mol32<kOut, false>;
+  if constexpr (!kOut && kStaged && (kMode == kModePlain || kMode == kModeBatch)) {
+    if (threads == 1024) {
+      *used = 1024;
+      return k_lens_persist<M, kOut, F, kStaged, kMode, 1024>;
+    }
+    if (threads == 768) {
+      *used = 768;
+      return k_lens_persist<M, kOut, F, kStaged, kMode, 768>;
+    }
+  }
+  *used = kPersistThreads;
+  return k_lens_persist<M, kOut, F, kStaged, kMode, kPersistThreads>;
+}
+
+template <bool kOut, int F, int kMode>
+PersistKernel persist_kernel(bool staged, int threads, int* used) {
+  return staged ? persist_kernel<kOut, F, true, kMode>(threads, used)
+                : persist_kernel<kOut, F, false, kMode>(threads, used);
+}
+
 template <bool kOut, int kMode = kModePlain>
 int enqueue_persistent(const Plan& P, const RunDev& R, int i, const Queue& Qin, const Queue& Qnext,
-                       unsigned* order_buf, int sms, int interval, cudaStream_t s, int* launches) {
-  using M = Mol32<kOut, false>;
-  using PK = void (*)(const Plan, const RunDev, const int, const Queue, const Queue, const LensArgs,
-                      const unsigned*, const int);
+                       unsigned* order_buf, int sms, int interval, cudaStream_t s, int* launches,
+                       int threads = kPersistThreads) {
   const bool staged = P.lf[i].n_smem > 0;
-  PK k;
+  int kt = kPersistThreads;
+  PersistKernel k;
   switch (P.lf[i].force) {
-    case kForceStark2:
-      k = staged ? k_lens_persist<M, kOut, kForceStark2, true, kMode>
-                 : k_lens_persist<M, kOut, kForceStark2, false, kMode>;
-      break;
-    case kForceStark2Lin:
-      k = staged ? k_lens_persist<M, kOut, kForceStark2Lin, true, kMode>
-                 : k_lens_persist<M, kOut, kForceStark2Lin, false, kMode>;
-      break;
-    case kForceStark1:
-      k = staged ? k_lens_persist<M, kOut, kForceStark1, true, kMode>
-                 : k_lens_persist<M, kOut, kForceStark1, false, kMode>;
-      break;
-    default:
-      k = staged ? k_lens_persist<M, kOut, kForceRadial, true, kMode>
-                 : k_lens_persist<M, kOut, kForceRadial, false, kMode>;
-      break;
+    case kForceStark2: k = persist_kernel<kOut, kForceStark2, kMode>(staged, threads, &kt); break;
+    case kForceStark2Lin: k = persist_kernel<kOut, kForceStark2Lin, kMode>(staged, threads, &kt); break;
+    case kForceStark1: k = persist_kernel<kOut, kForceStark1, kMode>(staged, threads, &kt); break;
+    default: k = persist_kernel<kOut, kForceRadial, kMode>(staged, threads, &kt); break;
   }
-  const size_t smem = (staged ? size_t(P.lf[i].n_int) * sizeof(float4) : 0) + kPersistThreads * sizeof(SwapSlot);
+  const size_t smem = (staged ? size_t(P.lf[i].n_int) * sizeof(float4) : 0) + size_t(kt) * sizeof(SwapSlot);
   CT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   unsigned* hist = order_buf;
   unsigned* order = hist + kOrderBuckets;
@@ -493,7 +526,7 @@ int enqueue_persistent(const Plan& P, const RunDev& R, int i, const Queue& Qin, 
   k_order_count<<<sms, kOrderThreads, 0, s>>>(P, i, Qin, hist);
   k_order_scan<<<1, kOrderBuckets, 0, s>>>(hist);
   k_order_place<<<sms, kOrderThreads, 0, s>>>(P, i, Qin, hist, order);
-  k<<<sms, kPersistThreads, smem, s>>>(P, R, i, Qin, Qnext, lens_args(P, i, true), order, interval);
+  k<<<sms, kt, smem, s>>>(P, R, i, Qin, Qnext, lens_args(P, i, true), order, interval);
   CT_CUDA(cudaGetLastError());
   *launches += 4;
   return CTRAJ_OK;
@@ -505,7 +538,7 @@ int launch_persistent(ctraj_context* c, const Plan& P, const RunDev& R, int i, c
   int st = c->lens_order.ensure((size_t(kOrderBuckets) + count) * sizeof(unsigned), 25);
   if (st) return st;
   return enqueue_persistent<kOut, kMode>(P, R, i, Qin, Qnext, c->lens_order.as<unsigned>(), c->sm_count,
-                                         c->lens_interval, c->stream, launches);
+                                         c->lens_interval, c->stream, launches, c->lens_threads);
 }
 
 // k_front, then for each lens: read the lens queue's size and largest
@@ -523,13 +556,9 @@ int launch_all(ctraj_context* c, const Plan& P, const RunDev& R0, Queue* q, int*
   cudaStream_t s = c->stream;
   if (c->timing) CT_CUDA(cudaEventRecord(c->ev[0], s));
   if (n > 0) {
-    auto kf = k_front<MolT, kOut, kRing ? kModeRing : kModePlain>;
-    const int ft = c->front_threads;
-    int bps = blocks_per_sm(kf, ft, 0);
-    int64_t want = (n + ft - 1) / ft;
-    int grid = int(std::min<int64_t>(want, int64_t(bps) * c->sm_count * c->front_waves));
-    kf<<<grid, ft, 0, s>>>(P, R, q[0]);
-    CT_CUDA(cudaGetLastError());
+    int st = launch_front<MolT, kOut, kRing ? kModeRing : kModePlain>(P, R, q[0], n, c->front_threads, c->sm_count,
+                                                                       c->front_waves, s);
+    if (st) return st;
     ++*launches;
   }
   if (c->timing) CT_CUDA(cudaEventRecord(c->ev[1], s));
@@ -787,12 +816,13 @@ int ctraj_set_tuning(ctraj_context* c, const ctraj_tuning* t) {
       t->chunk_growth < 100 || t->chunk_growth > 1000 || t->front_waves < 1 || t->front_waves > 64 ||
       (t->lens_mode != CTRAJ_LENS_PERSISTENT && t->lens_mode != CTRAJ_LENS_CHUNKED) || t->lens_interval < 1 ||
       t->lens_interval > 100000 || (t->front_threads != 128 && t->front_threads != 256 && t->front_threads != 512) ||
-      t->batch_group < 1 || t->batch_group > CTRAJ_MAX_BATCH_GROUP)
+      t->batch_group < 1 || t->batch_group > CTRAJ_MAX_BATCH_GROUP ||
+      (t->lens_threads != 512 && t->lens_threads != 768 && t->lens_threads != 1024))
     return fail(CTRAJ_EINVAL,
                 "tuning out of range (chunk_first %d, chunk_growth %d, chunk_max %d, front_waves %d, lens_mode %d, "
-                "lens_interval %d, front_threads %d, batch_group %d)",
+                "lens_interval %d, front_threads %d, batch_group %d, lens_threads %d)",
                 t->chunk_first, t->chunk_growth, t->chunk_max, t->front_waves, t->lens_mode, t->lens_interval,
-                t->front_threads, t->batch_group);
+                t->front_threads, t->batch_group, t->lens_threads);
   c->chunk = t->chunk_first;
   c->chunk_growth = t->chunk_growth;
   c->chunk_max = t->chunk_max;
@@ -801,6 +831,7 @@ int ctraj_set_tuning(ctraj_context* c, const ctraj_tuning* t) {
   c->lens_interval = t->lens_interval;
   c->front_threads = t->front_threads;
   c->batch_group = t->batch_group;
+  c->lens_threads = t->lens_threads;
   ++c->generation;
   return CTRAJ_OK;
 }
@@ -815,6 +846,7 @@ int ctraj_get_tuning(ctraj_context* c, ctraj_tuning* t) {
   t->lens_interval = c->lens_interval;
   t->front_threads = c->front_threads;
   t->batch_group = c->batch_group;
+  t->lens_threads = c->lens_threads;
   return CTRAJ_OK;
 }
 
@@ -1099,16 +1131,12 @@ static int run_group(ctraj_context* c, const ctraj_run_args* a, int g, ctraj_run
   int launches = 0;
   c->timing = timing;
   if (timing) CT_CUDA(cudaEventRecord(c->ev[0], s));
-  auto kf = k_front<Mol32<false, false>, false, kModeBatch>;
-  const int ft = c->front_threads;
-  const int bps = blocks_per_sm(kf, ft, 0);
   for (int j = 0; j < g; ++j) {
     if (flush) CT_CUDA(cudaMemsetAsync(c->l2_flush.p, j & 0xff, size_t(flush), s));
     if (a[j].n == 0) continue;
-    const int64_t want = (a[j].n + ft - 1) / ft;
-    const int grid = int(std::min<int64_t>(want, int64_t(bps) * c->sm_count * c->front_waves));
-    kf<<<grid, ft, 0, s>>>(P, R[j], q[0]);
-    CT_CUDA(cudaGetLastError());
+    if ((st = launch_front<Mol32<false, false>, false, kModeBatch>(P, R[j], q[0], a[j].n, c->front_threads,
+                                                                  c->sm_count, c->front_waves, s)))
+      return st;
     ++launches;
   }
   const int fronts = launches;
@@ -1249,6 +1277,7 @@ static int batch_peer(ctraj_context* c) {
     p->lens_interval = c->lens_interval;
     p->front_threads = c->front_threads;
     p->batch_group = c->batch_group;
+    p->lens_threads = c->lens_threads;
     ++p->generation;
     c->peer_generation = c->generation;
   }
@@ -2352,11 +2381,8 @@ int noalloc_launch(const Plan& P, const RunDev& R, Queue* q, unsigned* order_buf
   CT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const int64_t n = R.n;
   if (n > 0) {
-    auto kf = k_front<Mol32<kOut, false>, kOut>;
-    const int bps = blocks_per_sm(kf, kThreads, 0);
-    const int grid = int(std::min<int64_t>((n + kThreads - 1) / kThreads, int64_t(bps) * sms * 4));
-    kf<<<grid, kThreads, 0, s>>>(P, R, q[0]);
-    CT_CUDA(cudaGetLastError());
+    int st = launch_front<Mol32<kOut, false>, kOut, kModePlain>(P, R, q[0], n, kThreads, sms, 4, s);
+    if (st) return st;
     ++*launches;
   }
   int cur = 0, nxt = 1;

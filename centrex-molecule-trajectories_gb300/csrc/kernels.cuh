@@ -7,9 +7,10 @@
 //   conditions, walks the ballistic elements in closed form and stops at the
 //   first lens entrance.  Molecules lost on the way (98 % on the lens-beamline
 //   workload) are tallied at once; molecules inside the lens bore get their
-//   step count, step size and exit-snap time (in double) and are appended to
-//   a queue with one atomic per warp (ballot + prefix popcount): the stream
-//   compaction between element segments.
+//   step count, step size and exit-snap time (in double) and are staged in
+//   shared memory (ballot + prefix popcount per warp), then appended to a
+//   queue by the CTA with one atomic per flush: the stream compaction between
+//   element segments.
 // k_lens_chunk (one thread per queued molecule, the lens's table staged in
 //   shared memory per CTA): at most `chunk` RK4 steps per molecule, then the
 //   molecules still inside the lens are compacted into the next chunk's
@@ -36,6 +37,7 @@ namespace ctraj {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kThreads = 256;
 constexpr int kFrontMaxThreads = 512;  // k_front is launched with 128-512 threads (tuning)
+constexpr int kFrontSlack = 64;        // k_front: staged lens entrants flushed beyond this many
 // Lens chunks: 512 threads, 2 CTAs per SM (<= 64 registers): 32 warps share
 // two copies of the staged table (2 x 64 KiB for 4096 knots).
 constexpr int kLensThreads = 512;
@@ -221,17 +223,58 @@ __device__ __forceinline__ void ring_entry(const ctraj_ring& G, unsigned long lo
 // step bound queued is kept in the run's stats (counts and stats go to the
 // run's own slots through R.counts / R.stats).  The block size is a launch
 // parameter (at most kFrontMaxThreads).
+//
+// Lens entrants are staged in shared memory (kFrontSlack beyond one entry per
+// thread) and appended to the queue by the CTA with one global atomic per
+// flush -- normally one flush per CTA, since few molecules reach a lens --
+// instead of one returning atomic per warp on the queue's single counter.
+template <class M>
+struct FrontEntry {
+  M m;
+  LensStep st;
+};
+
+template <class M>
+__host__ __device__ constexpr size_t front_smem(int threads) {
+  return size_t(threads + kFrontSlack) * sizeof(FrontEntry<M>);
+}
+
 template <class M, bool kOut, int kMode = kModePlain>
 __global__ void __launch_bounds__(kFrontMaxThreads) k_front(const __grid_constant__ Plan P, const RunDev R,
                                                     const Queue Q) {
+  extern __shared__ unsigned char s_front[];
+  FrontEntry<M>* stage = reinterpret_cast<FrontEntry<M>*>(s_front);
   __shared__ BlockTally S;
+  __shared__ unsigned s_n, s_base, s_max;
   tally_init(S);
+  if (threadIdx.x == 0) s_n = s_max = 0;
   __syncthreads();
   const int lane = threadIdx.x & 31;
+  const unsigned lanes_lt = (1u << lane) - 1u;
+  // the staged entrants to the queue (every thread calls; block-uniform)
+  auto flush = [&]() {
+    if (threadIdx.x == 0) {
+      s_base = s_n ? atomicAdd(Q.count, s_n) : 0u;
+      if (s_max) {
+        atomicMax(Q.max_steps, s_max);
+        if (kMode == kModeBatch) atomicMax(R.stats + kStatMaxSteps, (unsigned long long)s_max);
+      }
+    }
+    __syncthreads();
+    for (unsigned j = threadIdx.x; j < s_n; j += blockDim.x) {
+      const unsigned slot = s_base + j;
+      stage[j].m.store(Q, slot, stage[j].st);
+      if (kMode == kModeRing) Q.cfg[slot] = int(slot);  // the record slot
+      if (kMode == kModeBatch) Q.cfg[slot] = R.run_tag;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_n = s_max = 0;
+    __syncthreads();
+  };
   unsigned long long steps = 0, band = 0, bad = 0;
   const int64_t stride = int64_t(gridDim.x) * blockDim.x;
-  for (int64_t base = int64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31); base < R.n; base += stride) {
-    const int64_t i = base + lane;
+  for (int64_t base = int64_t(blockIdx.x) * blockDim.x; base < R.n; base += stride) {  // block-uniform
+    const int64_t i = base + threadIdx.x;
     int label = kNone;
     M m;
     LensStep st;
@@ -245,17 +288,34 @@ __global__ void __launch_bounds__(kFrontMaxThreads) k_front(const __grid_constan
       }
       if (label != kQueued) {
         steps += unsigned(m.rows);
-        band += (m.margin < double(kEdgeBand)) ? 1 : 0;
+        band += (m.margin < kEdgeBand) ? 1 : 0;
         write_outputs<M, kOut>(R, m, label);
       }
       if constexpr (kMode == kModeRing) {  // listed; k_ring_reserve / k_ring_write append them
         if (label == R.rec_entrance_label && lens_at == R.rec_lens) R.ent_id[atomicAdd(R.ent_count, 1u)] = int32_t(i);
       }
     }
-    push_lens<kMode == kModeRing ? kTagSlot : (kMode == kModeBatch ? kTagCarry : kTagNone)>(
-        Q, label == kQueued, m, st, R.run_tag, nullptr, kMode == kModeBatch ? R.stats + kStatMaxSteps : nullptr);
+    // stage this warp's lens entrants (one shared atomic per warp)
+    const bool push = label == kQueued;
+    const unsigned pm = __ballot_sync(kFull, push);
+    if (pm) {
+      unsigned wb = 0;
+      if (lane == 0) wb = atomicAdd(&s_n, unsigned(__popc(pm)));
+      wb = __shfl_sync(kFull, wb, 0);
+      const unsigned rem = push ? unsigned(st.n_total < 0 ? st.bound : st.n_total - st.n_done) : 0u;
+      const unsigned wmax = __reduce_max_sync(kFull, rem);
+      if (push) {
+        FrontEntry<M>& e = stage[wb + __popc(pm & lanes_lt)];
+        e.m = m;
+        e.st = st;
+      }
+      if (lane == 0 && wmax) atomicMax(&s_max, wmax);
+    }
     tally_warp(S, label, P.n_labels);
+    __syncthreads();
+    if (s_n > unsigned(kFrontSlack)) flush();  // room for a full iteration stays
   }
+  flush();
   stat_add(S, kStatSteps, steps);
   stat_add(S, kStatEdgeBand, band);
   stat_add(S, kStatBadSteps, bad);
@@ -602,7 +662,7 @@ struct PersistAcc {
 // their run (Queue::cfg) and every tally and stat goes to that run's slots
 // (RunDev::cfg_counts, cfg_stats).  Every thread of the CTA calls it; it
 // returns with all of the CTA's molecules finalised.
-template <class M, bool kOut, int F, bool kStaged, int kMode>
+template <class M, bool kOut, int F, bool kStaged, int kMode, int kT = kPersistThreads>
 __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, const int li, const Queue& Qin,
                                              const Queue& Qnext, const LensArgs& L, const unsigned* order,
                                              const int interval, const unsigned static_entries,
@@ -731,7 +791,7 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
         }
         if (label != kQueued) {
           d[kStatSteps] = unsigned(m.rows);
-          d[kStatEdgeBand] = (m.margin < double(kEdgeBand)) ? 1 : 0;
+          d[kStatEdgeBand] = (m.margin < kEdgeBand) ? 1 : 0;
           write_outputs<M, kOut>(R, m, label);
         }
       }
@@ -784,7 +844,7 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
     __syncthreads();
     unsigned total = 0, base = 0, used = 0;
 #pragma unroll
-    for (int w = 0; w < kPersistThreads / 32; ++w) {
+    for (int w = 0; w < kT / 32; ++w) {
       const unsigned c = s_wcount[w];
       base += w < warp ? c : 0u;
       total += c;
@@ -846,14 +906,17 @@ __device__ __forceinline__ void persist_flush(BlockTally& S, const RunDev& R, in
   tally_flush(S, R, n_labels);
 }
 
-template <class M, bool kOut, int F, bool kStaged, int kMode = kModePlain>
-__global__ void __launch_bounds__(kPersistThreads, 1) k_lens_persist(const __grid_constant__ Plan P, const RunDev R,
-                                                                     const int li, const Queue Qin, const Queue Qnext,
-                                                                     const LensArgs L, const unsigned* order,
-                                                                     const int interval) {
+// kT: threads per CTA (512, 768 or 1024; one CTA per SM, so kT / 32 warps
+// per SM), a compile-time constant so that __launch_bounds__ gives the
+// register budget of that occupancy (128, 80 or 64 per thread).
+template <class M, bool kOut, int F, bool kStaged, int kMode = kModePlain, int kT = kPersistThreads>
+__global__ void __launch_bounds__(kT, 1) k_lens_persist(const __grid_constant__ Plan P, const RunDev R,
+                                                        const int li, const Queue Qin, const Queue Qnext,
+                                                        const LensArgs L, const unsigned* order,
+                                                        const int interval) {
   extern __shared__ float4 s_dyn[];
   __shared__ BlockTally S;
-  __shared__ unsigned s_wcount[kPersistThreads / 32];
+  __shared__ unsigned s_wcount[kT / 32];
   SwapSlot* s_swap = reinterpret_cast<SwapSlot*>(s_dyn + (kStaged ? L.n_int : 0));
   if (*(volatile unsigned*)Qin.count == 0) return;
   tally_init(S);
@@ -862,8 +925,8 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_lens_persist(const __gri
   __syncthreads();
   PersistAcc acc;
   // a short queue spreads over all SMs through the interleaved first entries
-  persist_pass<M, kOut, F, kStaged, kMode>(P, R, li, Qin, Qnext, L, order, interval,
-                                            gridDim.x * kPersistThreads, s_dyn, s_swap, s_wcount, S, acc);
+  persist_pass<M, kOut, F, kStaged, kMode, kT>(P, R, li, Qin, Qnext, L, order, interval, gridDim.x * kT, s_dyn,
+                                                s_swap, s_wcount, S, acc);
   if (kMode != kModeBatch) persist_flush(S, R, P.n_labels, acc);  // a batch's tallies went to its runs
 }
 

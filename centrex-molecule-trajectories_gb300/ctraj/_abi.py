@@ -148,6 +148,7 @@ class Tuning(ctypes.Structure):
         ("lens_interval", ctypes.c_int32),
         ("front_threads", ctypes.c_int32),
         ("batch_group", ctypes.c_int32),
+        ("lens_threads", ctypes.c_int32),
     ]
 
 

@@ -5,7 +5,8 @@ launch that refills lanes and compacts the last molecules every
 ``lens_interval`` steps, or chunked launches), the length of the first lens
 chunk, the growth of later chunks and their maximum (how often molecules still
 inside a lens are compacted into full warps in chunked mode, which FP64 runs
-always use), the front kernel's grid (``front_waves``) and block size
+always use), the persistent pass's CTA size (``lens_threads``, i.e. warps per
+SM), the front kernel's grid (``front_waves``) and block size
 (``front_threads``), and how many consecutive runs of a batch share one lens
 pass (``batch_group``).  None of them changes a result.
 The best setting depends on the beamline: how fast molecules are lost inside
@@ -25,19 +26,20 @@ import os
 from pathlib import Path
 
 DEFAULT = dict(chunk_first=64, chunk_growth=200, chunk_max=1024, front_waves=4, lens_mode=0, lens_interval=256,
-               front_threads=256, batch_group=4)
+               front_threads=256, batch_group=4, lens_threads=512)
 
 
 def axes():
     """The search axes, in order: each is a list of partial settings tried on
     top of the best setting found so far.  First the lens pass (persistent, or
-    chunked with each chunk schedule), then the persistent pass's compaction
-    interval, then the front kernel's grid and block size."""
+    chunked with each chunk schedule), then the persistent pass's CTA size and
+    compaction interval, then the front kernel's grid and block size."""
     lens = [dict(lens_mode=0)]
     for cf, g, cm in itertools.product((32, 64, 128), (150, 200, 300), (256, 512, 1024, 2048)):
         if cm >= cf:
             lens.append(dict(lens_mode=1, chunk_first=cf, chunk_growth=g, chunk_max=cm))
     return [lens,
+            [dict(lens_threads=lt) for lt in (512, 768, 1024)],
             [dict(lens_interval=iv) for iv in (64, 128, 256, 512, 1024)],
             [dict(front_waves=fw) for fw in (1, 2, 4, 8)],
             [dict(front_threads=ft) for ft in (128, 256, 512)]]

@@ -265,7 +265,12 @@ int ctraj_set_beamline(ctraj_context* ctx, const ctraj_element* elements,
  *                 molecules of one run (the pass's critical path) overlap the
  *                 bulk of the others.  Applies to FP32 runs without
  *                 per-molecule outputs in persistent lens mode; other runs,
- *                 and batch_group 1, run one at a time.           default 4 */
+ *                 and batch_group 1, run one at a time.           default 4
+ *   lens_threads  threads per CTA of the persistent FP32 lens pass (one CTA
+ *                 per SM): 512, 768 or 1024, i.e. 16, 24 or 32 warps per SM
+ *                 within a register budget of 128, 80 or 64 per thread.  768
+ *                 and 1024 apply to runs without per-molecule outputs whose
+ *                 table is staged in shared memory; others use 512.  default 512 */
 enum { CTRAJ_LENS_PERSISTENT = 0, CTRAJ_LENS_CHUNKED = 1 };
 
 #define CTRAJ_MAX_BATCH_GROUP 64
@@ -279,6 +284,7 @@ typedef struct ctraj_tuning {
   int32_t lens_interval;
   int32_t front_threads;
   int32_t batch_group;
+  int32_t lens_threads;
 } ctraj_tuning;
 
 int ctraj_set_tuning(ctraj_context* ctx, const ctraj_tuning* tuning);

@@ -252,7 +252,8 @@ def test_results_do_not_depend_on_tuning(engine):
         for t in (dict(chunk_first=16, chunk_growth=100, chunk_max=16, front_waves=1, lens_mode=1),
                   dict(chunk_first=2048, chunk_growth=150, chunk_max=8192, front_waves=8, lens_mode=1),
                   dict(lens_interval=1), dict(lens_interval=5000, front_waves=2),
-                  dict(front_threads=128, front_waves=8), dict(front_threads=512, front_waves=1)):
+                  dict(front_threads=128, front_waves=8), dict(front_threads=512, front_waves=1),
+                  dict(lens_threads=768), dict(lens_threads=1024, lens_interval=64)):
             engine.set_tuning(**t)
             r = engine.run(cb, 200_000, xdist=xd, vdist=vd, seed=9, outputs=True)
             np.testing.assert_array_equal(r.counts, ref.counts)
