@@ -121,7 +121,8 @@ struct ctraj_context {
   int lens_interval = 256;      // persistent mode: steps between CTA compactions
   int front_threads = 256;      // k_front block size
   int batch_group = 4;          // ctraj_run_batch: runs sharing one lens pass
-  int lens_threads = 512;       // persistent FP32 lens pass: threads per CTA
+  int lens_threads = 512;       // persistent FP32 lens pass: molecule lanes per CTA
+  int lens_molecules = 1;       // persistent FP32 lens pass: molecules per thread
   unsigned run_max_steps = 0;   // largest lens queue step bound of the last run
   bool timing = false;
   // before front, after front, before the first lens chunk, after the last one
@@ -476,49 +477,64 @@ LensKernel lens_kernel(int force, bool staged) {
 // The persistent FP32 lens pass of lens element i over queue Qin: order the
 // entrants longest first into `order_buf` (kOrderBuckets + the queue's
 // entries), then one k_lens_persist launch, one CTA per SM.  kMode: plain,
-// ring recording or grouped batch.  threads: CTA size (tuning lens_threads);
-// 768 and 1024 are compiled for the staged-table plain and batch passes
-// without per-molecule outputs (the throughput path), 512 for every pass.
+// ring recording or grouped batch.  lanes: molecules per CTA (tuning
+// lens_threads), mpt: molecules per thread (tuning lens_molecules), so the CTA
+// has lanes / mpt threads.  Compiled for the staged-table plain and batch
+// passes without per-molecule outputs (the throughput path): 512, 768 or
+// 1024 lanes at one molecule per thread, and for the hexapole Stark forms
+// also at two; every other pass (and setting) runs 512 threads x 1.
 using PersistKernel = void (*)(const Plan, const RunDev, const int, const Queue, const Queue, const LensArgs,
                                const unsigned*, const int);
 
 template <bool kOut, int F, bool kStaged, int kMode>
-PersistKernel persist_kernel(int threads, int* used) {
+PersistKernel persist_kernel(int lanes, int mpt, int* threads, int* used_mpt) {
   using M = Mol32<kOut, false>;
+  *used_mpt = 1;
   if constexpr (!kOut && kStaged && (kMode == kModePlain || kMode == kModeBatch)) {
-    if (threads == 1024) {
-      *used = 1024;
+    if constexpr (F == kForceStark2 || F == kForceStark2Lin) {
+      if (mpt == 2) {
+        *used_mpt = 2;
+        *threads = lanes / 2;
+        if (lanes == 1024) return k_lens_persist<M, kOut, F, kStaged, kMode, 512, 2>;
+        if (lanes == 768) return k_lens_persist<M, kOut, F, kStaged, kMode, 384, 2>;
+        *threads = 256;
+        return k_lens_persist<M, kOut, F, kStaged, kMode, 256, 2>;
+      }
+    }
+    if (lanes == 1024) {
+      *threads = 1024;
       return k_lens_persist<M, kOut, F, kStaged, kMode, 1024>;
     }
-    if (threads == 768) {
-      *used = 768;
+    if (lanes == 768) {
+      *threads = 768;
       return k_lens_persist<M, kOut, F, kStaged, kMode, 768>;
     }
   }
-  *used = kPersistThreads;
+  *threads = kPersistThreads;
   return k_lens_persist<M, kOut, F, kStaged, kMode, kPersistThreads>;
 }
 
 template <bool kOut, int F, int kMode>
-PersistKernel persist_kernel(bool staged, int threads, int* used) {
-  return staged ? persist_kernel<kOut, F, true, kMode>(threads, used)
-                : persist_kernel<kOut, F, false, kMode>(threads, used);
+PersistKernel persist_kernel(bool staged, int lanes, int mpt, int* threads, int* used_mpt) {
+  return staged ? persist_kernel<kOut, F, true, kMode>(lanes, mpt, threads, used_mpt)
+                : persist_kernel<kOut, F, false, kMode>(lanes, mpt, threads, used_mpt);
 }
 
 template <bool kOut, int kMode = kModePlain>
 int enqueue_persistent(const Plan& P, const RunDev& R, int i, const Queue& Qin, const Queue& Qnext,
                        unsigned* order_buf, int sms, int interval, cudaStream_t s, int* launches,
-                       int threads = kPersistThreads) {
+                       int lanes = kPersistThreads, int mpt = 1) {
   const bool staged = P.lf[i].n_smem > 0;
-  int kt = kPersistThreads;
+  int kt = kPersistThreads, km = 1;
   PersistKernel k;
   switch (P.lf[i].force) {
-    case kForceStark2: k = persist_kernel<kOut, kForceStark2, kMode>(staged, threads, &kt); break;
-    case kForceStark2Lin: k = persist_kernel<kOut, kForceStark2Lin, kMode>(staged, threads, &kt); break;
-    case kForceStark1: k = persist_kernel<kOut, kForceStark1, kMode>(staged, threads, &kt); break;
-    default: k = persist_kernel<kOut, kForceRadial, kMode>(staged, threads, &kt); break;
+    case kForceStark2: k = persist_kernel<kOut, kForceStark2, kMode>(staged, lanes, mpt, &kt, &km); break;
+    case kForceStark2Lin: k = persist_kernel<kOut, kForceStark2Lin, kMode>(staged, lanes, mpt, &kt, &km); break;
+    case kForceStark1: k = persist_kernel<kOut, kForceStark1, kMode>(staged, lanes, mpt, &kt, &km); break;
+    default: k = persist_kernel<kOut, kForceRadial, kMode>(staged, lanes, mpt, &kt, &km); break;
   }
-  const size_t smem = (staged ? size_t(P.lf[i].n_int) * sizeof(float4) : 0) + size_t(kt) * sizeof(SwapSlot);
+  const size_t smem =
+      (staged ? size_t(P.lf[i].n_int) * sizeof(float4) : 0) + size_t(kt) * size_t(km) * sizeof(SwapSlot);
   CT_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   unsigned* hist = order_buf;
   unsigned* order = hist + kOrderBuckets;
@@ -538,7 +554,8 @@ int launch_persistent(ctraj_context* c, const Plan& P, const RunDev& R, int i, c
   int st = c->lens_order.ensure((size_t(kOrderBuckets) + count) * sizeof(unsigned), 25);
   if (st) return st;
   return enqueue_persistent<kOut, kMode>(P, R, i, Qin, Qnext, c->lens_order.as<unsigned>(), c->sm_count,
-                                         c->lens_interval, c->stream, launches, c->lens_threads);
+                                         c->lens_interval, c->stream, launches, c->lens_threads,
+                                         c->lens_molecules);
 }
 
 // k_front, then for each lens: read the lens queue's size and largest
@@ -817,12 +834,13 @@ int ctraj_set_tuning(ctraj_context* c, const ctraj_tuning* t) {
       (t->lens_mode != CTRAJ_LENS_PERSISTENT && t->lens_mode != CTRAJ_LENS_CHUNKED) || t->lens_interval < 1 ||
       t->lens_interval > 100000 || (t->front_threads != 128 && t->front_threads != 256 && t->front_threads != 512) ||
       t->batch_group < 1 || t->batch_group > CTRAJ_MAX_BATCH_GROUP ||
-      (t->lens_threads != 512 && t->lens_threads != 768 && t->lens_threads != 1024))
+      (t->lens_threads != 512 && t->lens_threads != 768 && t->lens_threads != 1024) ||
+      (t->lens_molecules != 1 && t->lens_molecules != 2))
     return fail(CTRAJ_EINVAL,
                 "tuning out of range (chunk_first %d, chunk_growth %d, chunk_max %d, front_waves %d, lens_mode %d, "
-                "lens_interval %d, front_threads %d, batch_group %d, lens_threads %d)",
+                "lens_interval %d, front_threads %d, batch_group %d, lens_threads %d, lens_molecules %d)",
                 t->chunk_first, t->chunk_growth, t->chunk_max, t->front_waves, t->lens_mode, t->lens_interval,
-                t->front_threads, t->batch_group, t->lens_threads);
+                t->front_threads, t->batch_group, t->lens_threads, t->lens_molecules);
   c->chunk = t->chunk_first;
   c->chunk_growth = t->chunk_growth;
   c->chunk_max = t->chunk_max;
@@ -832,6 +850,7 @@ int ctraj_set_tuning(ctraj_context* c, const ctraj_tuning* t) {
   c->front_threads = t->front_threads;
   c->batch_group = t->batch_group;
   c->lens_threads = t->lens_threads;
+  c->lens_molecules = t->lens_molecules;
   ++c->generation;
   return CTRAJ_OK;
 }
@@ -847,6 +866,7 @@ int ctraj_get_tuning(ctraj_context* c, ctraj_tuning* t) {
   t->front_threads = c->front_threads;
   t->batch_group = c->batch_group;
   t->lens_threads = c->lens_threads;
+  t->lens_molecules = c->lens_molecules;
   return CTRAJ_OK;
 }
 
@@ -1278,6 +1298,7 @@ static int batch_peer(ctraj_context* c) {
     p->front_threads = c->front_threads;
     p->batch_group = c->batch_group;
     p->lens_threads = c->lens_threads;
+    p->lens_molecules = c->lens_molecules;
     ++p->generation;
     c->peer_generation = c->generation;
   }

@@ -662,7 +662,27 @@ struct PersistAcc {
 // their run (Queue::cfg) and every tally and stat goes to that run's slots
 // (RunDev::cfg_counts, cfg_stats).  Every thread of the CTA calls it; it
 // returns with all of the CTA's molecules finalised.
-template <class M, bool kOut, int F, bool kStaged, int kMode, int kT = kPersistThreads>
+// The state of one molecule slot of a thread in the persistent pass.
+template <class M>
+struct PersistSlot {
+  M m;
+  LensStep st;
+  int phase;
+  unsigned flags;
+  float dt, hdt, c2, dt6, dt26;
+  int n0, cfg;  // cfg: the configuration (sweep), the record slot (ring) or the run (batch)
+  float beta, kappa;
+  bool fresh;
+  unsigned idx;
+  int to_rec;   // ring recording: steps to the next staged record
+};
+
+// kMPT: molecules per thread (1 or 2).  Each thread steps its kMPT molecules
+// in turn, so a step of one has the other's independent chain to issue
+// against; each slot s of a warp is finalised and refilled like a warp of
+// its own, and the compaction of phase B packs molecules into the lowest
+// threads' slots.  kMPT = 1 is the one-molecule pass.
+template <class M, bool kOut, int F, bool kStaged, int kMode, int kT = kPersistThreads, int kMPT = 1>
 __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, const int li, const Queue& Qin,
                                              const Queue& Qnext, const LensArgs& L, const unsigned* order,
                                              const int interval, const unsigned static_entries,
@@ -675,108 +695,120 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
   const unsigned lanes_lt = (1u << lane) - 1u;
   const ctraj_element& e = P.el[li];
   const bool classic = e.scheme == CTRAJ_RK4_CLASSIC;
-
-  M m;
-  LensStep st, nst;
-  st.n_done = 0;
-  int phase = kIdle;
-  unsigned flags = 0;
-  float dt = 0.f, hdt = 0.f, c2 = 0.f, dt6 = 0.f, dt26 = 0.f;
-  int n0 = 0, cfg = 0;  // cfg: the configuration (sweep), the record slot (ring) or the run (batch)
-  float beta = 0.f, kappa = 1.f;
-  bool fresh = false;
-  unsigned idx = 0;
   const bool rec_on = kRing && li == R.rec_lens;
-  int to_rec = 0;  // ring recording: steps to the next staged record
 
-  auto derive = [&]() {
-    dt = float(st.dt);
-    hdt = 0.5f * dt;
-    c2 = classic ? hdt : dt;
-    dt6 = dt * (1.0f / 6.0f);
-    dt26 = float(st.dt * st.dt / 6.0);
+  PersistSlot<M> X[kMPT];
+#pragma unroll
+  for (int s = 0; s < kMPT; ++s) {
+    X[s].st.n_done = 0;
+    X[s].phase = kIdle;
+    X[s].flags = 0;
+    X[s].dt = X[s].hdt = X[s].c2 = X[s].dt6 = X[s].dt26 = 0.f;
+    X[s].n0 = X[s].cfg = 0;
+    X[s].beta = 0.f;
+    X[s].kappa = 1.f;
+    X[s].fresh = false;
+    X[s].idx = 0;
+    X[s].to_rec = 0;
+  }
+
+  auto derive = [&](PersistSlot<M>& x) {
+    x.dt = float(x.st.dt);
+    x.hdt = 0.5f * x.dt;
+    x.c2 = classic ? x.hdt : x.dt;
+    x.dt6 = x.dt * (1.0f / 6.0f);
+    x.dt26 = float(x.st.dt * x.st.dt / 6.0);
     if (kSweep) {
-      beta = __ldg(R.cfg_beta + cfg);
-      kappa = __ldg(R.cfg_kappa + cfg);
+      x.beta = __ldg(R.cfg_beta + x.cfg);
+      x.kappa = __ldg(R.cfg_kappa + x.cfg);
     }
   };
-  auto take = [&](unsigned j) {  // queue position j
-    idx = order ? __ldg(order + j) : j;
-    flags = 0;
-    m.load_state(Qin, idx, P, st);
-    if (kMode != kModePlain) cfg = Qin.cfg[idx];
+  auto take = [&](PersistSlot<M>& x, unsigned j) {  // queue position j
+    x.idx = order ? __ldg(order + j) : j;
+    x.flags = 0;
+    x.m.load_state(Qin, x.idx, P, x.st);
+    if (kMode != kModePlain) x.cfg = Qin.cfg[x.idx];
     if constexpr (kRing) {
       if (rec_on) {  // the entrance state opens the record
-        to_rec = R.rec_stride - st.n_done % R.rec_stride;
-        if (st.n_done == 0) R.rec[size_t(cfg) * R.rec_max] = make_float4(m.x, m.y, m.vx, m.vy);
+        x.to_rec = R.rec_stride - x.st.n_done % R.rec_stride;
+        if (x.st.n_done == 0) R.rec[size_t(x.cfg) * R.rec_max] = make_float4(x.m.x, x.m.y, x.m.vx, x.m.vy);
       }
     }
     bool ok = true;
-    fresh = st.n_total < 0;
-    if (fresh) {  // step setup deferred by the front kernel
-      m.load_vz(Qin, idx);
-      ok = enter_lens(m, P, li, st);
+    x.fresh = x.st.n_total < 0;
+    if (x.fresh) {  // step setup deferred by the front kernel
+      x.m.load_vz(Qin, x.idx);
+      ok = enter_lens(x.m, P, li, x.st);
     }
-    n0 = st.n_done;
-    derive();
-    phase = !ok ? kBad : (st.n_done < st.n_total ? kRun : kExit);
+    x.n0 = x.st.n_done;
+    derive(x);
+    x.phase = !ok ? kBad : (x.st.n_done < x.st.n_total ? kRun : kExit);
   };
-  auto run = [&](int n_steps) {
-    if (!__any_sync(kFull, phase == kRun)) return;
-    for (int k = 0; k < n_steps; ++k) {
-      if (phase == kRun) {
-        bool lost = m.template lens_step<F, kStaged, kSweep>(L, dt, hdt, c2, dt6, dt26, s_tab, flags, beta, kappa);
-        if (F == kForceRadial && (flags & 2u)) lost = true;
-        ++st.n_done;
-        if constexpr (kRing) {
-          if (rec_on && --to_rec == 0) {
-            to_rec = R.rec_stride;
-            R.rec[size_t(cfg) * R.rec_max + st.n_done / R.rec_stride] = make_float4(m.x, m.y, m.vx, m.vy);
-          }
-        }
-        if (lost) phase = kLost;
-        else if (st.n_done == st.n_total) phase = kExit;
+  auto step = [&](PersistSlot<M>& x) {
+    bool lost = x.m.template lens_step<F, kStaged, kSweep>(L, x.dt, x.hdt, x.c2, x.dt6, x.dt26, s_tab, x.flags,
+                                                          x.beta, x.kappa);
+    if (F == kForceRadial && (x.flags & 2u)) lost = true;
+    ++x.st.n_done;
+    if constexpr (kRing) {
+      if (rec_on && --x.to_rec == 0) {
+        x.to_rec = R.rec_stride;
+        R.rec[size_t(x.cfg) * R.rec_max + x.st.n_done / R.rec_stride] = make_float4(x.m.x, x.m.y, x.m.vx, x.m.vy);
       }
     }
+    if (lost) x.phase = kLost;
+    else if (x.st.n_done == x.st.n_total) x.phase = kExit;
   };
-  // all lanes: the lanes whose molecule is lost or left the lens are tallied
-  // (or queued at the next lens) and become idle
-  auto finalize = [&]() {
-    if (!__any_sync(kFull, phase == kLost || phase == kExit || phase == kBad)) return;
+  auto run = [&](int n_steps) {
+    bool any = false;
+#pragma unroll
+    for (int s = 0; s < kMPT; ++s) any = any || X[s].phase == kRun;
+    if (!__any_sync(kFull, any)) return;
+    for (int k = 0; k < n_steps; ++k) {
+#pragma unroll
+      for (int s = 0; s < kMPT; ++s)
+        if (X[s].phase == kRun) step(X[s]);
+    }
+  };
+  // all lanes: the slot-x molecules that were lost or left the lens are
+  // tallied (or queued at the next lens) and the slot becomes idle
+  auto finalize = [&](PersistSlot<M>& x) {
+    if (!__any_sync(kFull, x.phase == kLost || x.phase == kExit || x.phase == kBad)) return;
+    M& m = x.m;
+    LensStep nst;
     int label = kNone;
     bool enter = false;
     // this lane's additions to the stats (kStat* order up to kStatRangeError)
     unsigned d[kStatMaxSteps] = {0u, 0u, 0u, 0u, 0u, 0u};
-    if (phase == kLost || phase == kExit || phase == kBad) {
-      m.load_rest(Qin, idx, st, !fresh);
+    if (x.phase == kLost || x.phase == kExit || x.phase == kBad) {
+      m.load_rest(Qin, x.idx, x.st, !x.fresh);
       if constexpr (kRing) {
         if (rec_on) {  // close the record (the state after the losing step) before the exit snap
           int n_rec = 0;
-          if (phase == kLost) {
-            const int s = R.rec_stride, k = st.n_done;
-            if (k % s != 0) R.rec[size_t(cfg) * R.rec_max + k / s + 1] = make_float4(m.x, m.y, m.vx, m.vy);
-            n_rec = k / s + 1 + (k % s != 0 ? 1 : 0);
-            R.rec_last[cfg] = k;
+          if (x.phase == kLost) {
+            const int rs = R.rec_stride, k = x.st.n_done;
+            if (k % rs != 0) R.rec[size_t(x.cfg) * R.rec_max + k / rs + 1] = make_float4(m.x, m.y, m.vx, m.vy);
+            n_rec = k / rs + 1 + (k % rs != 0 ? 1 : 0);
+            R.rec_last[x.cfg] = k;
           }
-          R.rec_n[cfg] = n_rec;  // 0: left the lens (or unusable step count), not recorded
-          if (fresh) {
-            R.rec_id[cfg] = m.id;
-            R.rec_t0[cfg] = m.t;
-            R.rec_vz[cfg] = m.vz;
+          R.rec_n[x.cfg] = n_rec;  // 0: left the lens (or unusable step count), not recorded
+          if (x.fresh) {
+            R.rec_id[x.cfg] = m.id;
+            R.rec_t0[x.cfg] = m.t;
+            R.rec_vz[x.cfg] = m.vz;
           }
         }
       }
-      d[kStatLensSteps] = unsigned(st.n_done - n0);
-      if (phase == kBad) {  // rint(L/dz) not usable: the reference raises here
+      d[kStatLensSteps] = unsigned(x.st.n_done - x.n0);
+      if (x.phase == kBad) {  // rint(L/dz) not usable: the reference raises here
         label = e.label_inside;
         d[kStatBadSteps] = 1;
         d[kStatSteps] = unsigned(m.rows);
         write_outputs<M, kOut>(R, m, label);
       } else {
-        d[kStatTableRange] = (flags & 1u) ? 1 : 0;
-        d[kStatRangeError] = (flags & 2u) ? 1 : 0;
-        m.lens_end(P, li, st, phase == kLost);
-        if (phase == kLost) {
+        d[kStatTableRange] = (x.flags & 1u) ? 1 : 0;
+        d[kStatRangeError] = (x.flags & 2u) ? 1 : 0;
+        m.lens_end(P, li, x.st, x.phase == kLost);
+        if (x.phase == kLost) {
           label = e.label_inside;
         } else {
           int lens_at = -1;
@@ -795,14 +827,14 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
           write_outputs<M, kOut>(R, m, label);
         }
       }
-      phase = kIdle;
+      x.phase = kIdle;
     }
     if constexpr (kBatch) {
-      push_lens<kNextTag>(Qnext, enter, m, nst, cfg, enter ? R.cfg_stats + size_t(cfg) * kStatCount + kStatMaxSteps
-                                                              : nullptr);
+      push_lens<kNextTag>(Qnext, enter, m, nst, x.cfg,
+                          enter ? R.cfg_stats + size_t(x.cfg) * kStatCount + kStatMaxSteps : nullptr);
       const bool done = label != kNone;
-      stats_run(R, done ? cfg : -1, d);
-      tally_cfg(R, cfg, label, P.n_labels);
+      stats_run(R, done ? x.cfg : -1, d);
+      tally_cfg(R, x.cfg, label, P.n_labels);
     } else {
       acc.steps += d[kStatSteps];
       acc.lsteps += d[kStatLensSteps];
@@ -810,27 +842,39 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
       acc.bad += d[kStatBadSteps];
       acc.range += d[kStatTableRange];
       acc.rerr += d[kStatRangeError];
-      push_lens<kNextTag>(Qnext, enter, m, nst, cfg);
+      push_lens<kNextTag>(Qnext, enter, m, nst, x.cfg);
       tally_warp(S, label, P.n_labels);
-      if (kSweep) tally_cfg(R, cfg, label, P.n_labels);
+      if (kSweep) tally_cfg(R, x.cfg, label, P.n_labels);
     }
   };
 
-  {
-    const unsigned j = (unsigned(warp) * gridDim.x + blockIdx.x) * 32u + unsigned(lane);
-    if (j < min(n_in, static_entries)) take(j);
+  // the first static_entries queue positions, interleaved across CTAs
+#pragma unroll
+  for (int s = 0; s < kMPT; ++s) {
+    const unsigned j = ((unsigned(s) * (kT / 32) + unsigned(warp)) * gridDim.x + blockIdx.x) * 32u + unsigned(lane);
+    if (j < min(n_in, static_entries)) take(X[s], j);
   }
   // phase A
   for (bool exhausted = static_entries >= n_in && static_entries > 0; !exhausted;) {
     run(kPersistService);
-    finalize();
-    const unsigned idle = __ballot_sync(kFull, phase == kIdle);
-    if (idle) {
+    unsigned idle[kMPT], n_idle = 0;
+#pragma unroll
+    for (int s = 0; s < kMPT; ++s) {
+      finalize(X[s]);
+      idle[s] = __ballot_sync(kFull, X[s].phase == kIdle);
+      n_idle += unsigned(__popc(idle[s]));
+    }
+    if (n_idle) {
       unsigned b = 0;
-      if (lane == 0) b = atomicAdd(Qin.head, unsigned(__popc(idle)));
+      if (lane == 0) b = atomicAdd(Qin.head, n_idle);
       b = static_entries + __shfl_sync(kFull, b, 0);
-      exhausted = b + unsigned(__popc(idle)) >= n_in;
-      if (phase == kIdle && b + __popc(idle & lanes_lt) < n_in) take(b + __popc(idle & lanes_lt));
+      exhausted = b + n_idle >= n_in;
+#pragma unroll
+      for (int s = 0; s < kMPT; ++s) {
+        const unsigned j = b + unsigned(__popc(idle[s] & lanes_lt));
+        if (X[s].phase == kIdle && j < n_in) take(X[s], j);
+        b += unsigned(__popc(idle[s]));
+      }
     } else {
       exhausted = static_entries + *(volatile unsigned*)Qin.head >= n_in;
     }
@@ -838,9 +882,21 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
   // phase B (every warp of the CTA enters it, then the barriers below match)
   for (;;) {
     run(interval);
-    finalize();
-    const unsigned held = __ballot_sync(kFull, phase != kIdle);
-    if (lane == 0) s_wcount[warp] = __popc(held);
+    unsigned held = 0;  // molecules this thread holds
+#pragma unroll
+    for (int s = 0; s < kMPT; ++s) {
+      finalize(X[s]);
+      held += X[s].phase != kIdle ? 1u : 0u;
+    }
+    unsigned excl = held;  // exclusive prefix of held over the warp's lanes
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned v = __shfl_up_sync(kFull, excl, o);
+      if (lane >= o) excl += v;
+    }
+    excl -= held;
+    const unsigned wsum = __shfl_sync(kFull, excl + held, 31);
+    if (lane == 0) s_wcount[warp] = wsum;
     __syncthreads();
     unsigned total = 0, base = 0, used = 0;
 #pragma unroll
@@ -852,44 +908,55 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
     }
     __syncthreads();
     if (total == 0) break;
-    if ((total + 31) / 32 < used) {
-      if (phase != kIdle) {
-        SwapSlot& w = s_swap[base + __popc(held & lanes_lt)];
-        w.a = make_float4(m.x, m.y, m.vx, m.vy);
-        w.b = make_float4(m.cx, m.cy, m.cvx, m.cvy);
-        w.dt = st.dt;
-        w.snap = st.snap;
-        w.c = make_int4(st.n_done, st.n_total, n0, int(idx));
-        w.flags = flags | (fresh ? 0x80000000u : 0u);
-        w.phase = unsigned(phase);
-        w.margin = m.margin;
-        w.cfg = cfg;
+    if ((total + 32 * kMPT - 1) / (32 * kMPT) < used) {
+      unsigned r = base + excl;
+#pragma unroll
+      for (int s = 0; s < kMPT; ++s) {
+        const PersistSlot<M>& x = X[s];
+        if (x.phase != kIdle) {
+          SwapSlot& w = s_swap[r++];
+          w.a = make_float4(x.m.x, x.m.y, x.m.vx, x.m.vy);
+          w.b = make_float4(x.m.cx, x.m.cy, x.m.cvx, x.m.cvy);
+          w.dt = x.st.dt;
+          w.snap = x.st.snap;
+          w.c = make_int4(x.st.n_done, x.st.n_total, x.n0, int(x.idx));
+          w.flags = x.flags | (x.fresh ? 0x80000000u : 0u);
+          w.phase = unsigned(x.phase);
+          w.margin = x.m.margin;
+          w.cfg = x.cfg;
+        }
       }
       __syncthreads();
-      phase = kIdle;
-      if (threadIdx.x < total) {
-        const SwapSlot& w = s_swap[threadIdx.x];
-        m.x = w.a.x;
-        m.y = w.a.y;
-        m.vx = w.a.z;
-        m.vy = w.a.w;
-        m.cx = w.b.x;
-        m.cy = w.b.y;
-        m.cvx = w.b.z;
-        m.cvy = w.b.w;
-        st.dt = w.dt;
-        st.snap = w.snap;
-        st.n_done = w.c.x;
-        st.n_total = w.c.y;
-        n0 = w.c.z;
-        idx = unsigned(w.c.w);
-        flags = w.flags & 0x7fffffffu;
-        fresh = (w.flags >> 31) != 0;
-        phase = int(w.phase);
-        m.margin = w.margin;
-        cfg = w.cfg;
-        if (kRing && rec_on) to_rec = R.rec_stride - st.n_done % R.rec_stride;
-        derive();
+      // molecule q goes to slot q % kMPT of thread q / kMPT: the lowest warps fill up
+#pragma unroll
+      for (int s = 0; s < kMPT; ++s) {
+        PersistSlot<M>& x = X[s];
+        x.phase = kIdle;
+        const unsigned q = threadIdx.x * kMPT + unsigned(s);
+        if (q < total) {
+          const SwapSlot& w = s_swap[q];
+          x.m.x = w.a.x;
+          x.m.y = w.a.y;
+          x.m.vx = w.a.z;
+          x.m.vy = w.a.w;
+          x.m.cx = w.b.x;
+          x.m.cy = w.b.y;
+          x.m.cvx = w.b.z;
+          x.m.cvy = w.b.w;
+          x.st.dt = w.dt;
+          x.st.snap = w.snap;
+          x.st.n_done = w.c.x;
+          x.st.n_total = w.c.y;
+          x.n0 = w.c.z;
+          x.idx = unsigned(w.c.w);
+          x.flags = w.flags & 0x7fffffffu;
+          x.fresh = (w.flags >> 31) != 0;
+          x.phase = int(w.phase);
+          x.m.margin = w.margin;
+          x.cfg = w.cfg;
+          if (kRing && rec_on) x.to_rec = R.rec_stride - x.st.n_done % R.rec_stride;
+          derive(x);
+        }
       }
       __syncthreads();
     }
@@ -906,10 +973,11 @@ __device__ __forceinline__ void persist_flush(BlockTally& S, const RunDev& R, in
   tally_flush(S, R, n_labels);
 }
 
-// kT: threads per CTA (512, 768 or 1024; one CTA per SM, so kT / 32 warps
-// per SM), a compile-time constant so that __launch_bounds__ gives the
-// register budget of that occupancy (128, 80 or 64 per thread).
-template <class M, bool kOut, int F, bool kStaged, int kMode = kModePlain, int kT = kPersistThreads>
+// kT: threads per CTA (one CTA per SM, so kT / 32 warps per SM), a
+// compile-time constant so that __launch_bounds__ gives the register budget
+// of that occupancy; kMPT molecules per thread (the swap area holds kT x kMPT
+// slots).
+template <class M, bool kOut, int F, bool kStaged, int kMode = kModePlain, int kT = kPersistThreads, int kMPT = 1>
 __global__ void __launch_bounds__(kT, 1) k_lens_persist(const __grid_constant__ Plan P, const RunDev R,
                                                         const int li, const Queue Qin, const Queue Qnext,
                                                         const LensArgs L, const unsigned* order,
@@ -925,8 +993,8 @@ __global__ void __launch_bounds__(kT, 1) k_lens_persist(const __grid_constant__ 
   __syncthreads();
   PersistAcc acc;
   // a short queue spreads over all SMs through the interleaved first entries
-  persist_pass<M, kOut, F, kStaged, kMode, kT>(P, R, li, Qin, Qnext, L, order, interval, gridDim.x * kT, s_dyn,
-                                                s_swap, s_wcount, S, acc);
+  persist_pass<M, kOut, F, kStaged, kMode, kT, kMPT>(P, R, li, Qin, Qnext, L, order, interval,
+                                                      gridDim.x * kT * kMPT, s_dyn, s_swap, s_wcount, S, acc);
   if (kMode != kModeBatch) persist_flush(S, R, P.n_labels, acc);  // a batch's tallies went to its runs
 }
 

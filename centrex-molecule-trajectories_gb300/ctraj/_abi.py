@@ -149,6 +149,7 @@ class Tuning(ctypes.Structure):
         ("front_threads", ctypes.c_int32),
         ("batch_group", ctypes.c_int32),
         ("lens_threads", ctypes.c_int32),
+        ("lens_molecules", ctypes.c_int32),
     ]
 
 

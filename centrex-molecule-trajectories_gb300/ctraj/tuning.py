@@ -5,8 +5,9 @@ launch that refills lanes and compacts the last molecules every
 ``lens_interval`` steps, or chunked launches), the length of the first lens
 chunk, the growth of later chunks and their maximum (how often molecules still
 inside a lens are compacted into full warps in chunked mode, which FP64 runs
-always use), the persistent pass's CTA size (``lens_threads``, i.e. warps per
-SM), the front kernel's grid (``front_waves``) and block size
+always use), the persistent pass's molecules per CTA (``lens_threads``) and
+per thread (``lens_molecules``), the front kernel's grid (``front_waves``)
+and block size
 (``front_threads``), and how many consecutive runs of a batch share one lens
 pass (``batch_group``).  None of them changes a result.
 The best setting depends on the beamline: how fast molecules are lost inside
@@ -26,7 +27,7 @@ import os
 from pathlib import Path
 
 DEFAULT = dict(chunk_first=64, chunk_growth=200, chunk_max=1024, front_waves=4, lens_mode=0, lens_interval=256,
-               front_threads=256, batch_group=4, lens_threads=512)
+               front_threads=256, batch_group=4, lens_threads=512, lens_molecules=1)
 
 
 def axes():
@@ -39,7 +40,7 @@ def axes():
         if cm >= cf:
             lens.append(dict(lens_mode=1, chunk_first=cf, chunk_growth=g, chunk_max=cm))
     return [lens,
-            [dict(lens_threads=lt) for lt in (512, 768, 1024)],
+            [dict(lens_threads=lt, lens_molecules=m) for lt in (512, 768, 1024) for m in (1, 2)],
             [dict(lens_interval=iv) for iv in (64, 128, 256, 512, 1024)],
             [dict(front_waves=fw) for fw in (1, 2, 4, 8)],
             [dict(front_threads=ft) for ft in (128, 256, 512)]]

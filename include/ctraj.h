@@ -266,11 +266,18 @@ int ctraj_set_beamline(ctraj_context* ctx, const ctraj_element* elements,
  *                 bulk of the others.  Applies to FP32 runs without
  *                 per-molecule outputs in persistent lens mode; other runs,
  *                 and batch_group 1, run one at a time.           default 4
- *   lens_threads  threads per CTA of the persistent FP32 lens pass (one CTA
- *                 per SM): 512, 768 or 1024, i.e. 16, 24 or 32 warps per SM
- *                 within a register budget of 128, 80 or 64 per thread.  768
- *                 and 1024 apply to runs without per-molecule outputs whose
- *                 table is staged in shared memory; others use 512.  default 512 */
+ *   lens_threads  molecules per CTA of the persistent FP32 lens pass (one CTA
+ *                 per SM): 512, 768 or 1024; at one molecule per thread that
+ *                 is 16, 24 or 32 warps per SM within a register budget of
+ *                 128, 80 or 64 per thread.                     default 512
+ *   lens_molecules molecules each thread of the persistent FP32 lens pass
+ *                 steps in turn (1 or 2; with 2 the CTA has lens_threads / 2
+ *                 threads, and each RK4 step has a second molecule's
+ *                 independent chain to issue against).  default 1
+ *                 lens_threads above 512 and lens_molecules 2 apply to runs
+ *                 without per-molecule outputs whose table is staged in
+ *                 shared memory (lens_molecules 2: hexapole Stark tables);
+ *                 others run 512 x 1. */
 enum { CTRAJ_LENS_PERSISTENT = 0, CTRAJ_LENS_CHUNKED = 1 };
 
 #define CTRAJ_MAX_BATCH_GROUP 64
@@ -285,6 +292,7 @@ typedef struct ctraj_tuning {
   int32_t front_threads;
   int32_t batch_group;
   int32_t lens_threads;
+  int32_t lens_molecules;
 } ctraj_tuning;
 
 int ctraj_set_tuning(ctraj_context* ctx, const ctraj_tuning* tuning);

@@ -39,17 +39,19 @@ def _same(batch, alone):
         assert b.extra["max_lens_steps"] == a.extra["max_lens_steps"]
 
 
-@pytest.mark.parametrize("group", [1, 2, 3, 16])
-def test_grouped_batch_equals_single_runs(engine, group):
-    """Runs sharing lens passes (batch_group > 1) give each run's own results;
-    groups of 2 and 3 over 7 runs leave a partial last group, 16 takes them all."""
+@pytest.mark.parametrize("group,lanes,mpt", [(1, 512, 1), (2, 768, 1), (3, 512, 2), (16, 768, 2), (4, 1024, 1)])
+def test_grouped_batch_equals_single_runs(engine, group, lanes, mpt):
+    """Runs sharing lens passes (batch_group > 1) give each run's own results,
+    whatever the lens pass's CTA shape; groups of 2 and 3 over 7 runs leave a
+    partial last group, 16 takes them all."""
     cb = compile_beamline(lens_beamline())
     xs, vs = _specs()
     n = 150_000
     seeds = [101 + 13 * k for k in range(7)]
     alone = [engine.run(cb, n + 1000 * k, xdist=xs, vdist=vs, seed=s, offset=3) for k, s in enumerate(seeds)]
     try:
-        engine.set_tuning(batch_group=group, front_threads=128 if group == 3 else 256)
+        engine.set_tuning(batch_group=group, front_threads=128 if group == 3 else 256, lens_threads=lanes,
+                          lens_molecules=mpt)
         batch = engine.run_batch(cb, [n + 1000 * k for k in range(7)], seeds, xdist=xs, vdist=vs, offset=3)
     finally:
         engine.set_tuning()

@@ -266,6 +266,19 @@ def test_results_do_not_depend_on_tuning(engine):
             engine.set_tuning(lens_mode=2)
         with pytest.raises(ValueError):
             engine.set_tuning(lens_interval=0)
+        # the lens-pass CTA shapes of the throughput path (runs without
+        # per-molecule outputs): counts and step totals equal
+        plain = engine.run(cb, 200_000, xdist=xd, vdist=vd, seed=9)
+        np.testing.assert_array_equal(plain.counts, ref.counts)
+        for t in (dict(lens_threads=768), dict(lens_threads=1024, lens_interval=64),
+                  dict(lens_threads=768, lens_molecules=2), dict(lens_threads=512, lens_molecules=2, lens_interval=32),
+                  dict(lens_threads=1024, lens_molecules=2, lens_interval=1000)):
+            engine.set_tuning(**t)
+            r = engine.run(cb, 200_000, xdist=xd, vdist=vd, seed=9)
+            np.testing.assert_array_equal(r.counts, ref.counts)
+            assert (r.molecule_steps, r.lens_steps) == (plain.molecule_steps, plain.lens_steps), t
+        with pytest.raises(ValueError):
+            engine.set_tuning(lens_molecules=3)
         with pytest.raises(ValueError):
             engine.set_tuning(front_threads=300)
         with pytest.raises(ValueError):
