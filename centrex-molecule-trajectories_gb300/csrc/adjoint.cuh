@@ -1,9 +1,10 @@
 // Soft transmission of the lens beamline and its discrete adjoint.
 //
 // The soft model replaces every hard aperture test of the propagation
-// (CircularAperture at its two planes, apertures.py:101-115; the lens
-// entrance and the bore test after each RK4 step, electrostatic_lens.py:60-66,
-// 112-118) by a sigmoid of the edge distance: a molecule at radius r in front
+// (CircularAperture at its two planes, apertures.py:101-115, in front of the
+// lens and behind it; the lens entrance and the bore test after each RK4
+// step, electrostatic_lens.py:60-66, 112-118) by a sigmoid of the edge
+// distance: a molecule at radius r in front
 // of an edge of radius R keeps the weight sigma((R - r) / w), w the sigmoid
 // width, and no molecule is removed.  The soft transmission is the mean over
 // molecules of the product of all weights, i.e. exp(sum of log-sigmoids); as
@@ -12,8 +13,9 @@
 // exp(log_floor), and its gradient are counted as zero.
 //
 // Parameters (in this order): lens voltage V, lens z0, the radius of one
-// circular aperture in front of the lens, the clip radius of the lens bore
-// (the field radius stays fixed), and the standard deviations of vx and vy.
+// circular aperture (in front of the lens or behind it), the clip radius of
+// the lens bore (the field radius stays fixed), and the standard deviations
+// of vx and vy.
 // Initial conditions are reparameterised: vx = mu_vx + sigma_vx n0 with n0 a
 // unit normal from the same Philox draw as ctraj_run (or given by the caller).
 //
@@ -24,7 +26,11 @@
 // hexapole force a_perp = w(r^2) (x, y) - g y^, w = kappa P(s), P the
 // derivative W'(E) of the cubic Stark spline on interval i at local
 // coordinate u = s - i, s = beta r^2 - s0, beta = alpha / h, kappa =
-// -2 alpha / m, alpha = 3 V / R^3.
+// -2 alpha / m, alpha = 3 V / R^3.  Behind the lens a molecule flies with
+// a = (0, -g) from its state after the last RK4 step, at z0 + N dz, to each
+// aperture plane (the reference's exit snap to z1 with the last step's lens
+// force, electrostatic_lens.py:74-77, a sub-step of at most dz / 2, is taken
+// as part of that ballistic flight: positions differ by nanometres).
 //
 // Gradients are the exact derivatives of this discrete computation (a
 // discrete adjoint): the forward pass stores the lens state every
@@ -33,9 +39,11 @@
 // four RK4 stage points) and runs the transposed step Jacobians over it in
 // reverse, accumulating dlog(T)/dV; the ballistic part is recomputed and
 // reversed the same way, giving d/d(lens z0) from the last flight time and
-// d/d(sigma_v) from the initial velocities.  The radius derivatives need no
-// adjoint (they do not change the dynamics) and are summed in the forward
-// pass.
+// d/d(sigma_v) from the initial velocities; the part behind the lens is
+// closed form and its adjoint (d/d(state after the lens), d/d(lens z0)) is
+// computed in the forward pass and starts the backward composition.  The
+// radius derivatives need no adjoint (they do not change the dynamics) and are
+// summed in the forward pass.
 #pragma once
 #include <type_traits>
 
@@ -143,7 +151,11 @@ struct SoftPlan {
   double z[kSoftMaxPlanes];         // plane positions; the last is the lens entrance (lens z0)
   double radius[kSoftMaxPlanes];    // edge radius at the plane; INFINITY: no test
   int param[kSoftMaxPlanes];        // 1: the radius is the aperture parameter
-  ctraj_element lens;               // step mode, dz / dt, L (p[7]), scheme
+  int n_post;                       // aperture planes behind the lens
+  double post_z[kSoftMaxPlanes];
+  double post_radius[kSoftMaxPlanes];
+  int post_param[kSoftMaxPlanes];
+  ctraj_element lens;               // step mode, dz / dt, L (p[7]), scheme; z0 = the parameter
   double V;
   double s0, beta, kappa, kappa1;   // table coordinate and force scales (kappa1 = kappa / V)
   double bore;                      // clip radius (parameter)
@@ -164,6 +176,7 @@ struct SoftQueue {
   int32_t* bid;
   int32_t* bslot;
   unsigned int* bcount;
+  double* bpost;  // gradient runs with planes behind the lens: (5, cap) d lw / d(x, y, vx, vy), d lw / d z0
 };
 
 // Per (survivor, segment): the segment's backward map
@@ -183,7 +196,7 @@ constexpr size_t kSoftCtlBytes = 256 + 8 * kSoftStatCount + 8 * kSoftAcc * kSoft
 
 // Column sums in a fixed order: block (b, k) adds rows [b chunk, (b + 1) chunk)
 // of column k, thread-strided, then a shared-memory tree.
-__global__ void __launch_bounds__(256) k_soft_reduce(const double* __restrict__ contrib, int64_t count,
+static __global__ void __launch_bounds__(256) k_soft_reduce(const double* __restrict__ contrib, int64_t count,
                                                      double* __restrict__ partial) {
   __shared__ double s[256];
   const int b = blockIdx.x, k = blockIdx.y;
@@ -500,6 +513,41 @@ __device__ __forceinline__ void check_adjoint(T R, T inv_w, T x, T y, T& lx, T& 
   }
 }
 
+// The aperture planes behind the lens: from the state (x, y, vx, vy) after the
+// last RK4 step, at zrel = N dz behind the lens entrance, a closed-form flight
+// with a = (0, -g) of t_p = (z_p - z0 - zrel) / vz to each plane p, whose soft
+// edge test adds to the log weight (and to d_ap for the aperture parameter).
+// With lam, d(these log weights) / d(x, y, vx, vy) is added to lam and
+// d / d(lens z0) (t_p falls by 1 / vz per unit of z0) to *gz0.
+template <class T>
+__device__ __forceinline__ void soft_behind(const SoftPlan& S, T x, T y, T vx, T vy, T vz, double zrel, T& lw,
+                                            T& d_ap, T* lam, T* gz0) {
+  const T inv_w = T(S.inv_w), g = T(S.g);
+  for (int p = 0; p < S.n_post; ++p) {
+    const double Rd = S.post_radius[p];
+    if (!(Rd < INFINITY)) continue;
+    const T R = T(Rd);
+    const T t = div_(T(S.post_z[p] - S.lens.z0 - zrel), vz);
+    const T xp = fma_(vx, t, x);
+    const T yp = fma_(mul_(mul_(T(-0.5), g), t), t, fma_(vy, t, y));
+    const T r = soft_radius(xp, yp);
+    T ls, dls;
+    log_sigmoid(mul_(add_(R, -r), inv_w), ls, dls);
+    lw = add_(lw, ls);
+    if (S.post_param[p]) d_ap = add_(d_ap, mul_(dls, inv_w));
+    if (lam && r > T(0)) {
+      const T f = div_(mul_(dls, inv_w), r);
+      const T gx = mul_(-f, xp), gy = mul_(-f, yp);
+      lam[0] = add_(lam[0], gx);
+      lam[1] = add_(lam[1], gy);
+      lam[2] = fma_(gx, t, lam[2]);
+      lam[3] = fma_(gy, t, lam[3]);
+      const T vyp = fma_(-g, t, vy);
+      *gz0 = add_(*gz0, -div_(fma_(gy, vyp, mul_(gx, vx)), vz));
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // k_soft_front: molecules whose weight at the lens entrance is still above
 // the floor are queued (by index) with their RK4 step count bound.
@@ -548,10 +596,12 @@ template <class T>
 struct SoftLensSteps {
   int N;
   T dt, hdt, c2, dt6, dt26;
+  double zrel;  // N dz: where the last RK4 step ends, from the lens entrance
   __device__ SoftLensSteps(const SoftPlan& S, T vz) {
     LensStep st;
     lens_setup(S.lens, double(vz), st);  // succeeded in k_soft_front
     N = st.n_total;
+    zrel = double(N) * st.dz;
     dt = T(st.dt);
     hdt = mul_(T(0.5), dt);
     c2 = S.lens.scheme == CTRAJ_RK4_CLASSIC ? hdt : dt;
@@ -639,6 +689,10 @@ __global__ void __launch_bounds__(kSoftThreads) k_soft_lens(const __grid_constan
       m.lw = add_(m.lw, ls);
       m.d_bore = add_(m.d_bore, d);
     }
+    T lam[4] = {T(0), T(0), T(0), T(0)}, gz = T(0);
+    if (alive && S.n_post > 0)  // the apertures behind the lens
+      soft_behind(S, add_(x, cx), add_(y, cy), add_(vx, cvx), add_(vy, cvy), m.vz, L.zrel, m.lw, m.d_ap,
+                  kGrad ? lam : nullptr, &gz);
     if (!(m.lw >= floor_)) alive = false;
     steps += unsigned(n);
     if (!alive) {
@@ -656,6 +710,11 @@ __global__ void __launch_bounds__(kSoftThreads) k_soft_lens(const __grid_constan
       const unsigned b = atomicAdd(Q.bcount, 1u);
       Q.bid[b] = int32_t(i);
       Q.bslot[b] = int32_t(slot);
+      if (S.n_post > 0) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) Q.bpost[size_t(q) * cap + b] = double(lam[q]);
+        Q.bpost[4 * cap + b] = double(gz);
+      }
     }
   }
   steps = warp_sum(steps);
@@ -737,7 +796,8 @@ __global__ void __launch_bounds__(kSoftThreads) k_soft_seg(const __grid_constant
 template <class T>
 __global__ void __launch_bounds__(kSoftThreads) k_soft_compose(const __grid_constant__ SoftPlan S, const SoftQueue Q,
                                                                const T* __restrict__ seg_out, int max_seg,
-                                                               size_t bcap, double* __restrict__ contrib) {
+                                                               size_t bcap, double* __restrict__ contrib,
+                                                               size_t cap) {
   const unsigned nb = *Q.bcount;
   const size_t plane = bcap * size_t(max_seg);
   const T inv_w = T(S.inv_w), bore = T(S.bore);
@@ -747,7 +807,15 @@ __global__ void __launch_bounds__(kSoftThreads) k_soft_compose(const __grid_cons
     m.init(S, i);
     const SoftLensSteps<T> L(S, m.vz);
     const int n_seg = (L.N + S.checkpoint - 1) / S.checkpoint;
-    T lx = T(0), ly = T(0), lvx = T(0), lvy = T(0), gV = T(0);
+    // the adjoint after the lens: the apertures behind it (zero without any)
+    T lx = T(0), ly = T(0), lvx = T(0), lvy = T(0), gV = T(0), gz_post = T(0);
+    if (S.n_post > 0) {
+      lx = T(Q.bpost[b]);
+      ly = T(Q.bpost[cap + b]);
+      lvx = T(Q.bpost[2 * cap + b]);
+      lvy = T(Q.bpost[3 * cap + b]);
+      gz_post = T(Q.bpost[4 * cap + b]);
+    }
     // unrolled so that the next segments' loads are issued while this one's
     // products wait (a thread walks its segments in order; the maps are read
     // once each)
@@ -787,7 +855,7 @@ __global__ void __launch_bounds__(kSoftThreads) k_soft_compose(const __grid_cons
       if (p == S.n_planes - 1) {
         // d t / d z0 = 1 / vz; d x / d t = v at the plane, d vy / d t = -g
         const T gt = fma_(lvy, T(-S.g), fma_(ly, pvy[p], mul_(lx, m.vx)));
-        gz0 = div_(gt, m.vz);
+        gz0 = add_(div_(gt, m.vz), gz_post);
       }
       lvx = fma_(t, lx, lvx);
       lvy = fma_(t, ly, lvy);

@@ -1,0 +1,7 @@
+// libctraj.so: the persistent FP32 lens kernel's configurations for the
+// force law kForceRadial (see k_persist.cuh).
+#include "k_persist.cuh"
+
+namespace ctraj {
+template PersistKernel persist_kernel_for<kForceRadial>(bool, int, bool, int, int, int*, int*);
+}  // namespace ctraj

@@ -567,7 +567,7 @@ __device__ __forceinline__ void order_range(unsigned n, unsigned& lo, unsigned& 
   hi = min(n, lo + per);
 }
 
-__global__ void __launch_bounds__(kOrderThreads) k_order_count(const __grid_constant__ Plan P, const int li,
+static __global__ void __launch_bounds__(kOrderThreads) k_order_count(const __grid_constant__ Plan P, const int li,
                                                                const Queue Q, unsigned* hist) {
   __shared__ unsigned h[kOrderBuckets];
   for (int b = threadIdx.x; b < kOrderBuckets; b += blockDim.x) h[b] = 0;
@@ -582,7 +582,7 @@ __global__ void __launch_bounds__(kOrderThreads) k_order_count(const __grid_cons
     if (h[b]) atomicAdd(hist + b, h[b]);
 }
 
-__global__ void __launch_bounds__(kOrderBuckets) k_order_scan(unsigned* hist) {
+static __global__ void __launch_bounds__(kOrderBuckets) k_order_scan(unsigned* hist) {
   __shared__ unsigned t[kOrderBuckets];
   const int i = threadIdx.x;
   const unsigned own = hist[i];
@@ -600,7 +600,7 @@ __global__ void __launch_bounds__(kOrderBuckets) k_order_scan(unsigned* hist) {
 // Same ranges as k_order_count: the block reserves its entries of every
 // bucket with one global atomic per bucket, then places them with
 // shared-memory atomics.
-__global__ void __launch_bounds__(kOrderThreads) k_order_place(const __grid_constant__ Plan P, const int li,
+static __global__ void __launch_bounds__(kOrderThreads) k_order_place(const __grid_constant__ Plan P, const int li,
                                                                const Queue Q, unsigned* cursor, unsigned* order) {
   __shared__ unsigned h[kOrderBuckets];
   for (int b = threadIdx.x; b < kOrderBuckets; b += blockDim.x) h[b] = 0;
@@ -1068,7 +1068,7 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_sweep_persist(const __gr
 // reads the final heads and writes only what lies within the last
 // capacity_rows rows / capacity_molecules entries, where positions are
 // distinct.  One thread per record slot or listed molecule.
-__global__ void __launch_bounds__(256) k_ring_reserve(const RunDev R, unsigned n_slots) {
+static __global__ void __launch_bounds__(256) k_ring_reserve(const RunDev R, unsigned n_slots) {
   const ctraj_ring& G = R.ring;
   const unsigned n_ent = *R.ent_count;
   const unsigned total = n_slots + n_ent;
