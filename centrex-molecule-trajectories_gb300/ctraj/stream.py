@@ -34,6 +34,10 @@ class StreamResult:
     kernels: int
     seconds: float
     chunk_ms: list = field(default_factory=list)
+    ring_rows: int = 0          # rows appended to the ring (with drain: over all runs)
+    ring_molecules: int = 0
+    rows_lost: int = 0          # with drain: rows overwritten before they could be drained
+    molecules_lost: int = 0
 
     def counter_dict(self) -> dict:
         names = list(self.labels) + ["Detected"]
@@ -41,13 +45,18 @@ class StreamResult:
 
 
 def run_streamed(cb, n_total: int, chunk: int = 134_000_000, xdist=None, vdist=None, seed: int = 0,
-                 offset: int = 0, g: float = G, ring=None, engine=None, timing: bool = True) -> StreamResult:
+                 offset: int = 0, g: float = G, ring=None, engine=None, timing: bool = True,
+                 drain=None) -> StreamResult:
     """n_total molecules in runs of at most `chunk`; molecule k of the stream
-    has Philox counter offset + k (so the result equals one run of n_total)."""
+    has Philox counter offset + k (so the result equals one run of n_total).
+    With a ring and ``drain`` (a consumer such as ctraj.ring.HostRingStore)
+    the ring is drained after every run, so it keeps every record as long as
+    one run's records fit it; the result counts what was appended and lost."""
     eng = engine or default_engine()
     counts = np.zeros(len(cb.labels) + 1, np.int64)
     steps = lsteps = kernels = 0
     chunk_ms = []
+    ring_tot = [0, 0, 0, 0]  # rows, molecules, rows lost, molecules lost
     t0 = time.perf_counter()
     k = 0
     for first in range(0, int(n_total), int(chunk)):
@@ -60,10 +69,18 @@ def run_streamed(cb, n_total: int, chunk: int = 134_000_000, xdist=None, vdist=N
         kernels += r.kernels
         if timing:
             chunk_ms.append(r.extra["front_ms"] + r.extra["lens_ms"])
+        if ring is not None and drain is not None:
+            d = ring.drain(drain)
+            ring_tot = [a + d[key] for a, key in zip(ring_tot, ("rows", "molecules", "rows_lost", "molecules_lost"))]
         k += 1
+    if ring is not None and drain is None:
+        ring_tot[0], ring_tot[1] = ring.counts()
+        ring_tot[2] = max(0, ring_tot[0] - ring.capacity_rows)
+        ring_tot[3] = max(0, ring_tot[1] - ring.capacity_molecules)
     return StreamResult(counts=counts, labels=list(cb.labels), molecules=int(n_total), molecule_steps=steps,
                         lens_steps=lsteps, chunks=k, kernels=kernels, seconds=time.perf_counter() - t0,
-                        chunk_ms=chunk_ms)
+                        chunk_ms=chunk_ms, ring_rows=ring_tot[0], ring_molecules=ring_tot[1],
+                        rows_lost=ring_tot[2], molecules_lost=ring_tot[3])
 
 
 def adam_tune(prob, which=("V", "lens_z0"), steps: int = 200, lr: float = 1e-2, params0=None,

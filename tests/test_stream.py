@@ -59,3 +59,37 @@ def test_adam_raises_the_soft_transmission(engine):
     lim = prob.param_bounds()
     assert (out["params"] >= lim[:, 0]).all() and (out["params"] <= lim[:, 1]).all()
     assert (out["trajectory"][:, 0] >= 0).all()  # the voltage stays physical
+
+
+def test_drained_ring_keeps_every_record_of_the_stream(engine):
+    """A ring half the size of the stream's records, drained to host memory
+    after every run, ends up with exactly the records one ring large enough
+    for the whole stream holds; a ring too small for one run reports its
+    losses."""
+    from ctraj.ring import HBMRing, HostRingStore
+    from ctraj.stream import run_streamed
+
+    cb = compile_beamline(lens_beamline())
+    xs, vs = _specs()
+    n, chunk = 300_000, 70_001
+    big = HBMRing(capacity_rows=2_000_000, capacity_molecules=200_000, stride=50)
+    whole = run_streamed(cb, n, chunk=chunk, xdist=xs, vdist=vs, seed=8, ring=big, engine=engine)
+    assert whole.rows_lost == 0 and whole.ring_rows > 0
+    ref = {r.molecule: r for r in big.read()}
+    assert len(ref) == whole.ring_molecules
+    small = HBMRing(capacity_rows=whole.ring_rows // 2, capacity_molecules=whole.ring_molecules // 2, stride=50)
+    store = HostRingStore()
+    st = run_streamed(cb, n, chunk=chunk, xdist=xs, vdist=vs, seed=8, ring=small, engine=engine, drain=store)
+    assert (st.ring_rows, st.ring_molecules, st.rows_lost, st.molecules_lost) == \
+           (whole.ring_rows, whole.ring_molecules, 0, 0)
+    np.testing.assert_array_equal(st.counts, whole.counts)
+    got = store.records()
+    assert len(got) == len(ref) and store.rows_total == whole.ring_rows
+    for rec in got:
+        r = ref[rec.molecule]
+        assert rec.label == r.label
+        np.testing.assert_array_equal(rec.rows, r.rows)
+    tiny = HBMRing(capacity_rows=500, capacity_molecules=50, stride=50)
+    lossy = run_streamed(cb, n, chunk=chunk, xdist=xs, vdist=vs, seed=8, ring=tiny, engine=engine,
+                         drain=HostRingStore(keep=False))
+    assert lossy.ring_rows == whole.ring_rows and lossy.rows_lost > 0 and lossy.molecules_lost > 0
