@@ -41,10 +41,14 @@ __all__ = ["DEBYE", "TLF_MASS", "TwoLevelStark", "StarkForce", "hexapole_force",
 
 @dataclass(frozen=True)
 class TwoLevelStark:
-    """W(E) = -(sqrt(a^2 + (d E)^2) - a) with a = h * splitting_hz, d = dipole_debye * D."""
+    """W(E) = sign (sqrt(a^2 + (d E)^2) - a) with a = h * splitting_hz, d =
+    dipole_debye * D; sign -1 (the workloads' curve) is the high-field-seeking
+    state, which a hexapole defocuses, +1 the low-field-seeking one, which it
+    focuses."""
 
     splitting_hz: float = 6.7e9
     dipole_debye: float = 4.2
+    sign: float = -1.0
 
     @property
     def a(self) -> float:
@@ -56,7 +60,7 @@ class TwoLevelStark:
 
     def __call__(self, E):
         E = np.asarray(E, dtype=np.float64)
-        return -(np.sqrt(self.a ** 2 + (self.d * E) ** 2) - self.a)
+        return self.sign * (np.sqrt(self.a ** 2 + (self.d * E) ** 2) - self.a)
 
     def spline(self, n_knots: int = 4096, E_max: float = 1e7) -> CubicSpline:
         """Cubic spline (scipy default not-a-knot) of W on n_knots uniform knots in [0, E_max]."""
@@ -129,10 +133,11 @@ class StarkForce:
 
 def hexapole_force(V: float = 30e3, R: float = 17.5e-3, splitting_hz: float = 6.7e9,
                    dipole_debye: float = 4.2, n_knots: int = 4096, E_max: float = 1e7,
-                   mass: float = TLF_MASS) -> StarkForce:
+                   mass: float = TLF_MASS, low_field_seeker: bool = False) -> StarkForce:
     """Hexapole lens, |E| = 3 V r^2 / R^3, with the two-level Stark table on
-    n_knots knots over 0..E_max V/m (the electrostatic-lens workload)."""
-    sp = TwoLevelStark(splitting_hz, dipole_debye).spline(n_knots, E_max)
+    n_knots knots over 0..E_max V/m (the electrostatic-lens workload; with
+    low_field_seeker the curve's other sign, a state the lens focuses)."""
+    sp = TwoLevelStark(splitting_hz, dipole_debye, 1.0 if low_field_seeker else -1.0).spline(n_knots, E_max)
     return StarkForce.from_spline(sp, V=V, R=R, mass=mass, field_order=2)
 
 

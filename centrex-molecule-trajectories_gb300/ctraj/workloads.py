@@ -38,13 +38,19 @@ def ballistic_beamline() -> Beamline:
 
 
 def lens_beamline(V: float = 30e3, splitting_hz: float = 6.7e9, z0: float = 0.80,
-                  aperture_d: float = 12e-3, force=None) -> Beamline:
+                  aperture_d: float = 12e-3, force=None, detector_d: float = INF,
+                  low_field_seeker: bool = False) -> Beamline:
+    """``detector_d``: the diameter of the detection plane at 3.0 m (infinite:
+    every molecule reaching it counts; finite: a detector aperture, e.g.
+    10 mm, whose misses are credited to "Detection plane").
+    ``low_field_seeker``: the Stark curve's other sign, a state the hexapole
+    focuses (the workloads' curve is a high-field seeker, which it defocuses)."""
     if force is None:
-        force = hexapole_force(V=V, R=17.5e-3, splitting_hz=splitting_hz)
+        force = hexapole_force(V=V, R=17.5e-3, splitting_hz=splitting_hz, low_field_seeker=low_field_seeker)
     return Beamline([
         CircularAperture(name="A1", z0=0.30, L=1e-3, d=aperture_d),
         ElectrostaticLens(name="ES lens", z0=z0, L=0.60, d=35e-3, V=V, dt=1e-6, a_interp=force),
-        CircularAperture(name="Detection plane", z0=3.00, L=0.0, d=INF),
+        CircularAperture(name="Detection plane", z0=3.00, L=0.0, d=detector_d),
     ])
 
 

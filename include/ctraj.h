@@ -277,7 +277,10 @@ int ctraj_set_beamline(ctraj_context* ctx, const ctraj_element* elements,
  *                 lens_threads above 512 and lens_molecules 2 apply to runs
  *                 without per-molecule outputs whose table is staged in
  *                 shared memory (lens_molecules 2: hexapole Stark tables);
- *                 others run 512 x 1. */
+ *                 others run 512 x 1.
+ *   batch_lens_threads lens_threads of the lens passes a batch group shares
+ *                 (a group's pass is long enough that more warps per SM pay,
+ *                 a single run's is set by its slowest molecule).  default 1024 */
 enum { CTRAJ_LENS_PERSISTENT = 0, CTRAJ_LENS_CHUNKED = 1 };
 
 #define CTRAJ_MAX_BATCH_GROUP 64
@@ -293,6 +296,7 @@ typedef struct ctraj_tuning {
   int32_t batch_group;
   int32_t lens_threads;
   int32_t lens_molecules;
+  int32_t batch_lens_threads;
 } ctraj_tuning;
 
 int ctraj_set_tuning(ctraj_context* ctx, const ctraj_tuning* tuning);
@@ -439,19 +443,23 @@ int ctraj_run_sweep(ctraj_context* ctx, const ctraj_sweep* sweep,
  * Soft transmission and its gradient.  No reference counterpart: the
  * reference has only hard counts (Counter, trajectory_simulator.py:106-158);
  * this makes the beamline differentiable so it can be tuned by gradient
- * descent.  Every hard aperture test up to the end of the lens (the circular
- * apertures in front of the lens at both planes, the lens entrance, the bore
+ * descent.  Every hard aperture test (the circular apertures in front of the
+ * lens and behind it, at both of their planes, the lens entrance, the bore
  * test after each RK4 step) becomes the weight sigmoid((R - r) / width); the
  * loss is the mean over molecules of the product of their weights.  Molecules
  * whose log weight falls below log_floor are dropped (counted as weight 0).
+ * Behind the lens a molecule flies with gravity alone from its state after
+ * the last RK4 step (z0 + N dz) to each aperture plane: the reference's exit
+ * snap to z1 with the last step's lens force (electrostatic_lens.py:74-77,
+ * at most dz / 2) is taken as part of that flight.
  *
  * Beamline: circular apertures, then exactly one electrostatic lens with a
  * Stark spline table and field order 2 (|E| = 3 V r^2 / R^3, R = p[4]), then
- * only planes of infinite diameter (e.g. the detection plane).
+ * circular apertures (any diameter; an infinite one is a plane without test).
  *
  * params[CTRAJ_SOFT_NPARAMS]: lens voltage, lens z0 (the lens moves, its
  * length stays), the radius of the circular aperture at element index
- * args->aperture (ignored when -1), the clip radius of the lens bore (the field
+ * args->aperture (in front of the lens or behind it; ignored when -1), the clip radius of the lens bore (the field
  * radius R stays fixed), and the standard deviations of vx and vy (replacing
  * those of args->vdist).  Initial conditions: Philox draws exactly as ctraj_run
  * (CTRAJ_IC_DEVICE_DRAW), or the caller's unit normals (CTRAJ_IC_HOST:

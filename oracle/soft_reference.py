@@ -13,6 +13,9 @@ float64 torch operations vectorised over molecules:
   sqrt(x^2 + y^2) <= d/2), of the lens entrance and of the bore after each RK4
   step (electrostatic_lens.py:60-66, 112-118) replaced by the log weight
   log sigmoid((R - r) / width);
+* behind the lens, circular apertures reached by a flight with a = (0, -g)
+  from the state after the last RK4 step at z0 + N dz (t = (z - z0 - N dz) /
+  vz), each plane with its soft test;
 * the lens interior as the reference's RK4 (electrostatic_lens.py:91-111:
   k1 = v, stage-2 point x + dt k1, stage-3 point x + dt/2 k2, stage-4 point
   x + dt k3; x' = x + dt/6 (k1 + 2 k2 + 2 k3 + k4), v' likewise) with
@@ -140,6 +143,20 @@ def soft_loss(cb, normals, xdist, vdist, params, aperture: int = -1, width: floa
         ls = _logsig((bore - torch.sqrt(x * x + y * y)) * inv_w)
         lw = lw + torch.where(act, ls, torch.zeros_like(ls))
         alive = alive & ~(act & (lw.detach() < log_floor))
+    # circular apertures behind the lens, from the state after the last step
+    zrel = torch.as_tensor(N * dz, dtype=f64)
+    for i in range(li + 1, len(els)):
+        e = els[i]
+        R = r_ap if i == aperture else torch.tensor(e.p[0] / 2, dtype=f64)
+        if not math.isfinite(float(R.detach())):
+            continue
+        for zp in (e.z0, e.z1):
+            t = (zp - z0 - zrel) / vz
+            xp = x + vx * t
+            yp = y + vy * t - 0.5 * g * t * t
+            ls = _logsig((R - torch.sqrt(xp * xp + yp * yp)) * inv_w)
+            lw = lw + torch.where(alive, ls, torch.zeros_like(ls))
+    alive = alive & (lw.detach() >= log_floor)
     return torch.where(alive, torch.exp(lw), torch.zeros_like(lw)).sum() / n
 
 

@@ -21,8 +21,12 @@ FP32_REL = 1e-4     # CUDA FP32 adjoint vs the FP64 reference
 V_TEST = 8e3        # lens voltage of the small cases: enough molecules pass to give a signal
 
 
-def problem(n, **kw):
-    return SoftProblem.from_beamline(lens_beamline(), n=n, aperture="A1", **kw)
+def problem(n, detector=False, aperture="A1", **kw):
+    """The lens beamline; detector: a 10 mm detector aperture at 3.0 m behind
+    a lens focusing the molecules onto it (the low-field-seeking state;
+    aperture="Detection plane" makes the detector's radius the parameter)."""
+    bl = lens_beamline(detector_d=10e-3, low_field_seeker=True) if detector else lens_beamline()
+    return SoftProblem.from_beamline(bl, n=n, aperture=aperture, **kw)
 
 
 def params(prob, V=V_TEST):
@@ -31,9 +35,15 @@ def params(prob, V=V_TEST):
     return p
 
 
-def rel_err(a, b):
+def rel_err(a, b, floor=1e-300):
+    """|a - b| relative to the larger magnitude; differences of two values both
+    below `floor` (a gradient that vanishes for the case) count as zero."""
     a, b = np.asarray(a), np.asarray(b)
-    return np.abs(a - b) / np.maximum(np.maximum(np.abs(a), np.abs(b)), 1e-300)
+    d = np.abs(a - b)
+    return np.where(d <= floor, 0.0, d / np.maximum(np.maximum(np.abs(a), np.abs(b)), 1e-300))
+
+
+NEGLIGIBLE = 1e-15  # a gradient below this (per unit of its parameter) is zero for these cases
 
 
 def test_initial_params_follow_the_beamline():
@@ -73,6 +83,29 @@ def engine():
     e.close()
 
 
+@pytest.mark.parametrize("aperture", ["A1", "Detection plane"])
+def test_torch_reference_behind_the_lens_matches_finite_differences(aperture):
+    """A detector aperture behind the lens: the reference's own gradient,
+    including the aperture-radius parameter on either side of the lens."""
+    from oracle import soft_reference as sr
+
+    n = 1500
+    prob = problem(n, detector=True, aperture=aperture)
+    p0 = params(prob)
+    nrm = np.random.default_rng(2).standard_normal((5, n))
+    kw = dict(aperture=prob.aperture, width=prob.width, log_floor=prob.log_floor)
+    loss, g = sr.soft_grad(prob.cb, nrm, prob.xdist, prob.vdist, p0, **kw)
+    fd = sr.soft_fd(prob.cb, nrm, prob.xdist, prob.vdist, p0, **kw)
+    import torch
+
+    open_plane = SoftProblem.from_beamline(lens_beamline(low_field_seeker=True), n=n, aperture="A1")
+    free = sr.soft_loss(open_plane.cb, nrm, prob.xdist, prob.vdist, torch.tensor(p0),
+                        aperture=open_plane.aperture, width=prob.width, log_floor=prob.log_floor)
+    assert 0 < loss < 0.5 * float(free)  # the detector takes part of what reaches 3 m
+    # (the bore radius does not limit a focused beam: its gradient vanishes)
+    assert rel_err(g, fd, NEGLIGIBLE).max() < FD_REL, (g, fd)
+
+
 @pytest.fixture(scope="module")
 def reference_1e4():
     from oracle import soft_reference as sr
@@ -95,6 +128,31 @@ def test_fp64_adjoint_matches_torch_autograd(engine, reference_1e4):
     out = soft_transmission(prob, p0, engine=engine)
     assert rel_err(out.loss, loss) < FP64_REL
     assert rel_err(out.grad, g).max() < FP64_REL, (out.grad, g)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("aperture", ["A1", "Detection plane"])
+def test_adjoint_behind_the_lens_matches_torch_autograd(engine, aperture):
+    """A 10 mm detector aperture behind the lens: the CUDA FP64 loss and
+    gradient against the torch FP64 reference, the FP32 gradient within its
+    tolerance."""
+    from ctraj.adjoint import soft_transmission
+    from oracle import soft_reference as sr
+
+    n = 10_000
+    prob = problem(n, detector=True, aperture=aperture)
+    nrm = np.random.default_rng(11).standard_normal((5, n))
+    p0 = params(prob)
+    kw = dict(aperture=prob.aperture, width=prob.width, log_floor=prob.log_floor)
+    loss, g = sr.soft_grad(prob.cb, nrm, prob.xdist, prob.vdist, p0, **kw)
+    out64 = soft_transmission(problem(n, detector=True, aperture=aperture, precision=64, normals=nrm), p0,
+                              engine=engine)
+    assert rel_err(out64.loss, loss) < FP64_REL
+    assert rel_err(out64.grad, g, NEGLIGIBLE).max() < FP64_REL, (out64.grad, g)
+    out32 = soft_transmission(problem(n, detector=True, aperture=aperture, precision=32, normals=nrm), p0,
+                              engine=engine)
+    assert rel_err(out32.grad, g, NEGLIGIBLE).max() < FP32_REL, (out32.grad, g)
+    assert abs(g[1]) > 0  # the lens position matters to the detector
 
 
 @pytest.mark.gpu
