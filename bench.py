@@ -597,7 +597,7 @@ def bench_large(eng, stream, flush, n_total: int = 1_000_000_000, chunk: int = 1
     from ctraj.adjoint import SoftProblem, soft_transmission
     from ctraj.compiler import compile_beamline
     from ctraj.distributions import device_spec
-    from ctraj.ring import HBMRing
+    from ctraj.ring import HBMRing, HostRingStore
     from ctraj.stream import adam_tune, run_streamed
     from ctraj.workloads import lens_beamline, source
 
@@ -605,36 +605,66 @@ def bench_large(eng, stream, flush, n_total: int = 1_000_000_000, chunk: int = 1
     xd, vd = source()
     xs, vs = device_spec(xd, "position"), device_spec(vd, "velocity")
     eng.set_tuning()  # default knobs (persistent lens pass), not the sweep's
-    ring = HBMRing(capacity_rows=200_000_000, capacity_molecules=20_000_000, stride=50)
-    run_streamed(cb, 2_000_000, chunk=chunk, xdist=xs, vdist=vs, seed=1, ring=ring, engine=eng)  # warm-up
+    # sized for one run's records (~4e7 rows of a 1.34e8-molecule run) and
+    # drained to pinned host memory after every run: nothing is overwritten
+    ring = HBMRing(capacity_rows=64_000_000, capacity_molecules=6_000_000, stride=50)
+    store = HostRingStore(keep=False)
+    run_streamed(cb, 2_000_000, chunk=chunk, xdist=xs, vdist=vs, seed=1, ring=ring, engine=eng, drain=store)  # warm-up
     ring.reset()
+    store = HostRingStore(keep=False)
     torch.cuda.synchronize()
     flush.zero_()
     t0 = time.perf_counter()
-    st = run_streamed(cb, n_total, chunk=chunk, xdist=xs, vdist=vs, seed=2, ring=ring, engine=eng)
+    st = run_streamed(cb, n_total, chunk=chunk, xdist=xs, vdist=vs, seed=2, ring=ring, engine=eng, drain=store)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
-    rows, mols = ring.counts()
-    # Adam on V and z0
-    prob = SoftProblem.from_beamline(lens_beamline(), n=1_000_000, aperture="A1", precision=32)
+    rows, mols = st.ring_rows, st.ring_molecules
+    # Adam on V and z0, focusing onto a detector aperture: the config-1
+    # geometry with a 10 mm aperture at 3.0 m and the Stark curve's
+    # low-field-seeking sign (the hexapole defocuses the workload's
+    # high-field-seeking state, for which switching the lens off is optimal)
+    det_bl = dict(detector_d=10e-3, low_field_seeker=True)
+    prob = SoftProblem.from_beamline(lens_beamline(**det_bl), n=1_000_000, aperture="A1", precision=32)
     p0 = prob.initial_params()
-    adam_tune(prob, steps=3, engine=eng)  # warm-up
-    opt = adam_tune(prob, which=("V", "lens_z0"), steps=200, lr=0.01, engine=eng, seed0=1000)
+    p0[0] = 10e3  # a detuned lens (10 kV) for Adam to tune
+    adam_tune(prob, steps=3, params0=p0, engine=eng)  # warm-up
+    opt = adam_tune(prob, which=("V", "lens_z0"), steps=200, lr=0.01, params0=p0, engine=eng, seed0=1000)
     prob.seed = 99
     before = soft_transmission(prob, p0, want_grad=False, engine=eng).loss
     after = soft_transmission(prob, opt["params"], want_grad=False, engine=eng).loss
+    lim = prob.param_bounds()
+
+    def hard_detected(V, z0, n=10_000_000):
+        r = eng.run(compile_beamline(lens_beamline(V=V, z0=z0, **det_bl)), n, xdist=xs, vdist=vs, seed=4242)
+        return int(r.counts[-1])
+
+    hard_before = hard_detected(p0[0], p0[1])
+    hard_design = hard_detected(30e3, 0.80)
+    hard_after = hard_detected(opt["params"][0], opt["params"][1])
     return {"workload": f"lens beamline, {n_total:.0e} molecules streamed in runs of {chunk:.3g}, "
-                        "molecules lost on the lens recorded every 50 RK4 steps into an HBM ring; "
-                        "then 200 Adam steps on (lens V, lens z0) at 1e6 molecules per step",
+                        "molecules lost on the lens recorded every 50 RK4 steps into an HBM ring "
+                        "drained to host memory after every run; then 200 Adam steps on (lens V, lens z0) "
+                        "at 1e6 molecules per step, focusing the low-field-seeking state onto a 10 mm "
+                        "detector aperture at 3.0 m",
             "molecules": n_total, "runs": st.chunks, "molecule_steps": st.molecule_steps,
             "seconds": wall, "molecule_steps_per_s": st.molecule_steps / wall,
             "kernel_ms_sum": float(sum(st.chunk_ms)), "gpu_launches": st.kernels,
             "counts": st.counter_dict(), "ring_rows": rows, "ring_molecules": mols,
-            "ring_capacity_rows": ring.capacity_rows,
+            "ring_capacity_rows": ring.capacity_rows, "ring_capacity_molecules": ring.capacity_molecules,
+            "rows_drained_to_host": store.rows_total, "molecules_drained_to_host": store.molecules_total,
+            "rows_lost": st.rows_lost, "molecules_lost": st.molecules_lost,
+            "ring_drain": "after every run the ring's records are copied to pinned host memory and the ring "
+                          "is emptied (inside the timed wall clock)",
             "adam": {"steps": 200, "seconds": opt["seconds"], "steps_per_s": 200 / opt["seconds"],
+                     "beamline": "A1 r=6mm@0.30m, hexapole lens (low-field-seeking two-level curve), "
+                                 "detector aperture r=5mm@3.0m",
                      "V_start": float(p0[0]), "V_end": float(opt["params"][0]),
                      "z0_start": float(p0[1]), "z0_end": float(opt["params"][1]),
-                     "soft_transmission_start": before, "soft_transmission_end": after},
+                     "z0_bounds": [float(lim[1, 0]), float(lim[1, 1])],
+                     "soft_transmission_start": before, "soft_transmission_end": after,
+                     "hard_detected_start": hard_before, "hard_detected_end": hard_after,
+                     "hard_detected_design_30kV_0.80m": hard_design,
+                     "hard_molecules": 10_000_000},
             "timing": "wall clock (perf_counter) around the streamed runs incl. host syncs between runs"}
 
 
@@ -686,7 +716,7 @@ def main():
     # launch knobs picked on this workload (outside the timed region), then re-warm
     run_kw = dict(precision=32, xdist=xs, vdist=vs, seed=7, offset=rank * n)
     tuned = autotune(eng, cb, n, run_kw, device_name=torch.cuda.get_device_name(local),
-                     batch=batch_measure(eng, cb, n, run_kw, runs=8, l2_flush_bytes=flush.numel()))
+                     batch=batch_measure(eng, cb, n, run_kw, runs=args.steps, l2_flush_bytes=flush.numel()))
     for k in range(args.warmup):
         step(seed=k)
     eng.run_batch(cb, n, list(range(max(2, args.warmup))), precision=32, xdist=xs, vdist=vs, offset=rank * n,

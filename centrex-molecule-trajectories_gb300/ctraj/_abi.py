@@ -150,6 +150,7 @@ class Tuning(ctypes.Structure):
         ("batch_group", ctypes.c_int32),
         ("lens_threads", ctypes.c_int32),
         ("lens_molecules", ctypes.c_int32),
+        ("batch_lens_threads", ctypes.c_int32),
     ]
 
 

@@ -27,7 +27,7 @@ import os
 from pathlib import Path
 
 DEFAULT = dict(chunk_first=64, chunk_growth=200, chunk_max=1024, front_waves=4, lens_mode=0, lens_interval=256,
-               front_threads=256, batch_group=4, lens_threads=512, lens_molecules=1)
+               front_threads=256, batch_group=4, lens_threads=512, lens_molecules=1, batch_lens_threads=1024)
 
 
 def axes():
@@ -46,13 +46,14 @@ def axes():
             [dict(front_threads=ft) for ft in (128, 256, 512)]]
 
 
-BATCH_GROUPS = (1, 2, 4, 8, 16)
+BATCH_GROUPS = (1, 2, 4, 8, 10, 16)
+BATCH_LENS_THREADS = (512, 768, 1024)
 
 
 def candidates():
     """Every setting the search may time (the axes' values on top of the defaults)."""
     out = [dict(DEFAULT, **v) for axis in axes() for v in axis]
-    out += [dict(DEFAULT, batch_group=g) for g in BATCH_GROUPS]
+    out += [dict(DEFAULT, batch_group=g, batch_lens_threads=t) for g in BATCH_GROUPS for t in BATCH_LENS_THREADS]
     return out
 
 
@@ -122,8 +123,9 @@ def autotune(engine, cb, n: int, run_kwargs: dict, device_name: str = "gpu", rep
     milliseconds under the engine's current tuning) times something else,
     e.g. a batched sweep, and ``key_extra`` keeps its cache entry apart.
     ``cands`` replaces the axis search by an explicit list of settings.
-    ``batch`` (a callable like ``batch_measure(...)``) adds the batch_group
-    axis, timed with it after the per-run knobs are fixed."""
+    ``batch`` (a callable like ``batch_measure(...)``) adds the batch axis
+    (batch_group x batch_lens_threads), timed with it after the per-run knobs
+    are fixed."""
     key = workload_key(cb, n, device_name) + key_extra + ("|batch" if batch is not None else "")
     cache = _load_cache() if use_cache else {}
     if use_cache and key in cache:
@@ -160,10 +162,14 @@ def autotune(engine, cb, n: int, run_kwargs: dict, device_name: str = "gpu", rep
     default_ms = next((t for t, c in trials if c == DEFAULT), None)
     result = {"tuning": best, "ms": ms, "trials": len(trials), "default_ms": default_ms}
     if batch is not None:
-        results = [(timed(dict(best, batch_group=g), batch), dict(best, batch_group=g)) for g in BATCH_GROUPS]
+        results = []
+        for g in BATCH_GROUPS:
+            for t in BATCH_LENS_THREADS:
+                setting = dict(best, batch_group=g, batch_lens_threads=t)
+                results.append((timed(setting, batch), setting))
         bms, best = min(results, key=lambda x: x[0])
         result.update(tuning=best, batch_ms_per_run=bms, trials=len(trials) + len(results),
-                      batch_trials={str(s["batch_group"]): t for t, s in results})
+                      batch_trials={f"{s['batch_group']}x{s['batch_lens_threads']}": t for t, s in results})
     engine.set_tuning(**best)
     if use_cache:
         cache[key] = result

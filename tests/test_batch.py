@@ -50,7 +50,7 @@ def test_grouped_batch_equals_single_runs(engine, group, lanes, mpt):
     seeds = [101 + 13 * k for k in range(7)]
     alone = [engine.run(cb, n + 1000 * k, xdist=xs, vdist=vs, seed=s, offset=3) for k, s in enumerate(seeds)]
     try:
-        engine.set_tuning(batch_group=group, front_threads=128 if group == 3 else 256, lens_threads=lanes,
+        engine.set_tuning(batch_group=group, front_threads=128 if group == 3 else 256, batch_lens_threads=lanes,
                           lens_molecules=mpt)
         batch = engine.run_batch(cb, [n + 1000 * k for k in range(7)], seeds, xdist=xs, vdist=vs, offset=3)
     finally:
