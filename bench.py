@@ -55,11 +55,11 @@ UNIT = "molecule-steps/s"
 # four table-driven force evaluations, stage points, RK4 combination, bore test).
 FLOP_PER_RK4_STEP = 114
 FLOP_PER_BALLISTIC_STEP = 12
-# dram__bytes_read.sum + dram__bytes_write.sum of the k_lens_persist launch of
-# one run of this workload, from the ncu capture summarised in
-# profiles/k_lens_persist_lens_beamline_1e7.md (the queue is read once; the
-# table and the molecule state stay on chip)
-LENS_DRAM_BYTES_PER_RUN = 10.98e6
+# dram__bytes_read.sum + dram__bytes_write.sum of a grouped k_lens_persist
+# launch per 1e7 molecules of the group, from the ncu capture summarised in
+# profiles/k_lens_persist_grouped_lens_beamline.md (the queue is read once;
+# the table and the molecule state stay on chip)
+LENS_DRAM_BYTES_PER_1E7 = 12.30e6
 # Shared-memory wavefronts per warp table lookup (the bench table goes to the
 # kernels in the 8-byte linear form: one LDS.64 per lane, random intervals,
 # bank-conflicted), from l1tex__data_pipe_lsu_wavefronts_mem_shared_op_ld of the
@@ -116,6 +116,10 @@ def parse():
     p.add_argument("--sweep-scale", type=float, default=1.0, help="molecule counts of --profile sweep x this")
     p.add_argument("--lens-mode", choices=["persistent", "chunked"], default="persistent",
                    help="--profile lens/sweep: the FP32 lens pass to run (ctraj_tuning.lens_mode)")
+    p.add_argument("--batch-group", type=int, default=10, help="--profile batch: runs per shared lens pass")
+    p.add_argument("--front-threads", type=int, default=128, help="--profile: threads per front block")
+    p.add_argument("--batch-lens-threads", type=int, default=1024,
+                   help="--profile batch: threads per CTA of the shared lens pass")
     return p.parse_args()
 
 
@@ -132,7 +136,8 @@ def run_profile(args):
     xd, vd = source()
     xs, vs = device_spec(xd, "position"), device_spec(vd, "velocity")
     eng = Engine(0)
-    eng.set_tuning(lens_mode=0 if args.lens_mode == "persistent" else 1)
+    eng.set_tuning(lens_mode=0 if args.lens_mode == "persistent" else 1, batch_group=args.batch_group,
+                   front_threads=args.front_threads, batch_lens_threads=args.batch_lens_threads)
     n = int(args.molecules)
     for k in range(args.steps):
         if args.profile == "sweep":
@@ -748,7 +753,7 @@ def main():
         # written on the lane's stream before every run inside the timed region
         ev0.record(stream)
         batch = eng.run_batch(cb, n, seeds, precision=32, xdist=xs, vdist=vs, offset=rank * n,
-                              l2_flush_bytes=flush.numel())
+                              l2_flush_bytes=flush.numel(), timing=True)
         ev1.record(stream)
         ev1.synchronize()
         batch_ms = ev0.elapsed_time(ev1)
@@ -846,33 +851,50 @@ def main():
                                                    torch.cuda.get_device_name(local))
     adjoint = None if args.no_adjoint else bench_adjoint(eng, stream, flush, args.steps, args.warmup)
     large = None if args.no_large else bench_large(eng, stream, flush)
-    achieved = lens_steps * FLOP_PER_RK4_STEP / (lens_ms / 1e3) / 1e12
-    roofline = {"bound": "fp32", "kernel": "k_lens_persist (RK4 through the hexapole lens; the lens pass = "
-                                          "entrant ordering + k_lens_persist, timed together)",
+    # the headline's dominant kernel: the lens pass a batch group shares (one
+    # k_lens_persist launch per group, after its three ordering launches),
+    # timed with CUDA events on the lane's stream inside the timed batch
+    tun = eng.get_tuning()
+    groups = -(-args.steps // tun["batch_group"]) if tun["lens_mode"] == 0 else args.steps
+    g_lens_ms = sum(r.extra.get("lens_ms", 0.0) for r in batch)
+    g_lens_steps = sum(r.lens_steps for r in batch)
+    achieved = g_lens_steps * FLOP_PER_RK4_STEP / (g_lens_ms / 1e3) / 1e12
+    mhz = clocks.get("sm_mhz") if clocks else None
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    roofline = {"bound": "fp32",
+                "kernel": f"k_lens_persist, grouped: the lens pass {tun['batch_group']} runs of the batch share "
+                          f"({tun['batch_lens_threads']} threads per CTA, one CTA per SM; with its entrant "
+                          f"ordering, timed together)",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
                 "peak_source": "measured in this run: FMA-chain kernel (bench_kernels/fp32_peak.cu), "
                                "MEASURED_PEAKS.json has no FP32 CUDA-core figure",
-                "flop_per_step": FLOP_PER_RK4_STEP, "lens_steps_per_launch": lens_steps / args.steps,
-                "lens_ms_per_launch": lens_ms / args.steps, "front_ms_per_launch": front_ms / args.steps,
-                "traffic": LENS_DRAM_BYTES_PER_RUN, "traffic_unit": "bytes per lens pass (ncu, the k_lens_persist launch)",
+                "flop_per_step": FLOP_PER_RK4_STEP, "launches": groups,
+                "lens_steps_per_launch": g_lens_steps / groups, "lens_ms_per_launch": g_lens_ms / groups,
+                "front_ms_per_run": sum(r.extra.get("front_ms", 0.0) for r in batch) / args.steps,
+                "traffic": LENS_DRAM_BYTES_PER_1E7 * n * tun["batch_group"] / 1e7,
+                "traffic_unit": "bytes per grouped lens pass: ncu DRAM bytes of one grouped k_lens_persist launch "
+                                "on a smaller group, scaled by molecules per launch",
                 "step_probe": probe}
-    # the lens pass is bound by its critical path, not by the FP32 pipe: the
-    # molecule with the most RK4 steps cannot finish before that many steps
-    # of one-warp latency (the step probe) at the clock seen in the timed region
+    if mhz:
+        roofline["shared_memory"] = shared_roof(g_lens_steps / (g_lens_ms / 1e3), sms, mhz)
+    # the single-run lens pass (one ctraj_run at a time): bound by its critical
+    # path, the molecule with the most RK4 steps, which cannot finish before
+    # that many steps of one-warp latency (the step probe)
+    single = {"kernel": "k_lens_persist of one run (512 threads per CTA)",
+              "achieved": lens_steps * FLOP_PER_RK4_STEP / (lens_ms / 1e3) / 1e12,
+              "lens_steps_per_launch": lens_steps / args.steps, "lens_ms_per_launch": lens_ms / args.steps,
+              "front_ms_per_launch": front_ms / args.steps}
+    single["frac"] = single["achieved"] / peak if peak else None
     max_steps = max(r.extra.get("max_lens_steps", 0) for r in results)
     cyc = probe.get("one_warp_cycles_per_step") if probe else None
-    mhz = clocks.get("sm_mhz") if clocks else None
     if max_steps and cyc and mhz:
         floor_ms = max_steps * cyc / (mhz * 1e3)
-        roofline["critical_path"] = {
+        single["critical_path"] = {
             "max_lens_steps": int(max_steps), "one_warp_cycles_per_step": cyc, "sm_mhz": mhz,
-            "floor_ms": floor_ms, "lens_ms_per_launch": lens_ms / args.steps,
-            "frac": floor_ms / (lens_ms / args.steps),
+            "floor_ms": floor_ms, "frac": floor_ms / (lens_ms / args.steps),
             "note": "latency floor of the slowest molecule (max_lens_steps x one-warp step latency); "
                     "frac = floor / measured lens pass"}
-    if mhz:
-        roofline["shared_memory"] = shared_roof(lens_steps / (lens_ms / 1e3), torch.cuda.get_device_properties(
-            local).multi_processor_count, mhz)
+    roofline["single_run"] = single
     cpu = None if args.no_cpu or world > 1 else cpu_baseline(int(args.cpu_sample or n), config0=cfg0)
     if parity is not None and cpu is not None and "config0_check" in cpu:
         parity["config0"]["oracle"] = cpu["config0_check"]
