@@ -94,7 +94,7 @@ WORKLOAD = ("lens beamline: aperture r=6mm@0.30m, hexapole lens z0=0.80m L=0.60m
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--molecules", type=float, default=1e7)
@@ -757,6 +757,7 @@ def main():
         ev1.record(stream)
         ev1.synchronize()
         batch_ms = ev0.elapsed_time(ev1)
+        tun = eng.get_tuning()  # the headline's knobs (the sweep and adjoint below set their own)
         torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
@@ -854,7 +855,6 @@ def main():
     # the headline's dominant kernel: the lens pass a batch group shares (one
     # k_lens_persist launch per group, after its three ordering launches),
     # timed with CUDA events on the lane's stream inside the timed batch
-    tun = eng.get_tuning()
     groups = -(-args.steps // tun["batch_group"]) if tun["lens_mode"] == 0 else args.steps
     g_lens_ms = sum(r.extra.get("lens_ms", 0.0) for r in batch)
     g_lens_steps = sum(r.lens_steps for r in batch)
@@ -871,7 +871,7 @@ def main():
                 "flop_per_step": FLOP_PER_RK4_STEP, "launches": groups,
                 "lens_steps_per_launch": g_lens_steps / groups, "lens_ms_per_launch": g_lens_ms / groups,
                 "front_ms_per_run": sum(r.extra.get("front_ms", 0.0) for r in batch) / args.steps,
-                "traffic": LENS_DRAM_BYTES_PER_1E7 * n * tun["batch_group"] / 1e7,
+                "traffic": LENS_DRAM_BYTES_PER_1E7 * n * args.steps / groups / 1e7,
                 "traffic_unit": "bytes per grouped lens pass: ncu DRAM bytes of one grouped k_lens_persist launch "
                                 "on a smaller group, scaled by molecules per launch",
                 "step_probe": probe}

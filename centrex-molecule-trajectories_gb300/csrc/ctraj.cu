@@ -275,7 +275,7 @@ int check_beamline(const ctraj_context* c) {
 }
 
 int enqueue_persistent(bool out, int mode, const Plan& P, const RunDev& R, int i, const Queue& Qin,
-                       const Queue& Qnext, unsigned* order_buf, int sms, int interval, cudaStream_t s,
+                       const Queue& Qnext, unsigned* order_buf, int sms, int interval, int service, cudaStream_t s,
                        int* launches, int lanes, int mpt) {
   const bool staged = P.lf[i].n_smem > 0;
   int kt = kPersistThreads, km = 1;
@@ -289,7 +289,7 @@ int enqueue_persistent(bool out, int mode, const Plan& P, const RunDev& R, int i
   k_order_count<<<sms, kOrderThreads, 0, s>>>(P, i, Qin, hist);
   k_order_scan<<<1, kOrderBuckets, 0, s>>>(hist);
   k_order_place<<<sms, kOrderThreads, 0, s>>>(P, i, Qin, hist, order);
-  k<<<sms, kt, smem, s>>>(P, R, i, Qin, Qnext, lens_args(P, i, true), order, interval);
+  k<<<sms, kt, smem, s>>>(P, R, i, Qin, Qnext, lens_args(P, i, true), order, interval, service);
   CT_CUDA(cudaGetLastError());
   *launches += 4;
   return CTRAJ_OK;
@@ -366,7 +366,7 @@ int launch_persistent(ctraj_context* c, bool out, int mode, const Plan& P, const
   int st = c->lens_order.ensure((size_t(kOrderBuckets) + count) * sizeof(unsigned), 25);
   if (st) return st;
   return enqueue_persistent(out, mode, P, R, i, Qin, Qnext, c->lens_order.as<unsigned>(), c->sm_count,
-                            c->lens_interval, c->stream, launches,
+                            c->lens_interval, c->lens_service, c->stream, launches,
                             mode == kModeBatch ? c->batch_lens_threads : c->lens_threads, c->lens_molecules);
 }
 
@@ -588,13 +588,15 @@ int ctraj_set_tuning(ctraj_context* c, const ctraj_tuning* t) {
       t->batch_group < 1 || t->batch_group > CTRAJ_MAX_BATCH_GROUP ||
       (t->lens_threads != 512 && t->lens_threads != 768 && t->lens_threads != 1024) ||
       (t->lens_molecules != 1 && t->lens_molecules != 2) ||
-      (t->batch_lens_threads != 512 && t->batch_lens_threads != 768 && t->batch_lens_threads != 1024))
+      (t->batch_lens_threads != 512 && t->batch_lens_threads != 768 && t->batch_lens_threads != 1024) ||
+      t->lens_service < 1 || t->lens_service > 100000)
     return fail(CTRAJ_EINVAL,
                 "tuning out of range (chunk_first %d, chunk_growth %d, chunk_max %d, front_waves %d, lens_mode %d, "
                 "lens_interval %d, front_threads %d, batch_group %d, lens_threads %d, lens_molecules %d, "
-                "batch_lens_threads %d)",
+                "batch_lens_threads %d, lens_service %d)",
                 t->chunk_first, t->chunk_growth, t->chunk_max, t->front_waves, t->lens_mode, t->lens_interval,
-                t->front_threads, t->batch_group, t->lens_threads, t->lens_molecules, t->batch_lens_threads);
+                t->front_threads, t->batch_group, t->lens_threads, t->lens_molecules, t->batch_lens_threads,
+                t->lens_service);
   c->chunk = t->chunk_first;
   c->chunk_growth = t->chunk_growth;
   c->chunk_max = t->chunk_max;
@@ -606,6 +608,7 @@ int ctraj_set_tuning(ctraj_context* c, const ctraj_tuning* t) {
   c->lens_threads = t->lens_threads;
   c->lens_molecules = t->lens_molecules;
   c->batch_lens_threads = t->batch_lens_threads;
+  c->lens_service = t->lens_service;
   ++c->generation;
   return CTRAJ_OK;
 }
@@ -623,6 +626,7 @@ int ctraj_get_tuning(ctraj_context* c, ctraj_tuning* t) {
   t->lens_threads = c->lens_threads;
   t->lens_molecules = c->lens_molecules;
   t->batch_lens_threads = c->batch_lens_threads;
+  t->lens_service = c->lens_service;
   return CTRAJ_OK;
 }
 
@@ -1056,6 +1060,7 @@ static int batch_peer(ctraj_context* c) {
     p->lens_threads = c->lens_threads;
     p->lens_molecules = c->lens_molecules;
     p->batch_lens_threads = c->batch_lens_threads;
+    p->lens_service = c->lens_service;
     ++p->generation;
     c->peer_generation = c->generation;
   }

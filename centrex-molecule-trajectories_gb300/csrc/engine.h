@@ -108,6 +108,7 @@ struct ctraj_context {
   int front_waves = 4;          // k_front grid in units of resident CTAs
   int lens_mode = CTRAJ_LENS_PERSISTENT;  // FP32 lens pass
   int lens_interval = 256;      // persistent mode: steps between CTA compactions
+  int lens_service = 64;        // persistent mode: steps between a warp's refills (kPersistService)
   int front_threads = 256;      // k_front block size
   int batch_group = 4;          // ctraj_run_batch: runs sharing one lens pass
   int lens_threads = 512;       // persistent FP32 lens pass: molecule lanes per CTA
@@ -225,7 +226,7 @@ LensKernel sweep_lens_kernel(int force, bool staged);
 // plain and batch passes without per-molecule outputs (the throughput path);
 // every other pass and setting runs 512 threads x 1.
 using PersistKernel = void (*)(const Plan, const RunDev, const int, const Queue, const Queue, const LensArgs,
-                               const unsigned*, const int);
+                               const unsigned*, const int, const int);
 PersistKernel persist_kernel(bool out, int force, int mode, bool staged, int lanes, int mpt, int* threads,
                              int* used_mpt);
 template <int F>  // one force law's configurations (k_persist_<law>.cu)
@@ -235,7 +236,7 @@ PersistKernel persist_kernel_for(bool out, int mode, bool staged, int lanes, int
 // the entrants ordered longest first into `order_buf` (kOrderBuckets + the
 // queue's entries), then one k_lens_persist launch, one CTA per SM.
 int enqueue_persistent(bool out, int mode, const Plan& P, const RunDev& R, int i, const Queue& Qin,
-                       const Queue& Qnext, unsigned* order_buf, int sms, int interval, cudaStream_t s,
+                       const Queue& Qnext, unsigned* order_buf, int sms, int interval, int service, cudaStream_t s,
                        int* launches, int lanes, int mpt);
 
 }  // namespace ctraj

@@ -37,7 +37,7 @@ namespace ctraj {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kThreads = 256;
 constexpr int kFrontMaxThreads = 512;  // k_front is launched with 128-512 threads (tuning)
-constexpr int kFrontSlack = 64;        // k_front: staged lens entrants flushed beyond this many
+constexpr int kFrontSlack = 64;        // k_front: staging entries beyond one per thread
 // Lens chunks: 512 threads, 2 CTAs per SM (<= 64 registers): 32 warps share
 // two copies of the staged table (2 x 64 KiB for 4096 knots).
 constexpr int kLensThreads = 512;
@@ -224,19 +224,22 @@ __device__ __forceinline__ void ring_entry(const ctraj_ring& G, unsigned long lo
 // run's own slots through R.counts / R.stats).  The block size is a launch
 // parameter (at most kFrontMaxThreads).
 //
-// Lens entrants are staged in shared memory (kFrontSlack beyond one entry per
-// thread) and appended to the queue by the CTA with one global atomic per
-// flush -- normally one flush per CTA, since few molecules reach a lens --
-// instead of one returning atomic per warp on the queue's single counter.
+// Lens entrants are staged in shared memory and appended to the queue by the
+// CTA at its end, with one global atomic, instead of one returning atomic
+// per warp on the queue's single counter.  The staging area holds
+// front_stage(threads) entries; a warp whose entrants do not all fit appends
+// the rest itself (queue_slot), so no warp waits for another before the end.
 template <class M>
 struct FrontEntry {
   M m;
   LensStep st;
 };
 
+__host__ __device__ constexpr unsigned front_stage(int threads) { return unsigned(threads + kFrontSlack); }
+
 template <class M>
 __host__ __device__ constexpr size_t front_smem(int threads) {
-  return size_t(threads + kFrontSlack) * sizeof(FrontEntry<M>);
+  return size_t(front_stage(threads)) * sizeof(FrontEntry<M>);
 }
 
 template <class M, bool kOut, int kMode = kModePlain>
@@ -251,30 +254,20 @@ __global__ void __launch_bounds__(kFrontMaxThreads) k_front(const __grid_constan
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const unsigned lanes_lt = (1u << lane) - 1u;
-  // the staged entrants to the queue (every thread calls; block-uniform)
-  auto flush = [&]() {
-    if (threadIdx.x == 0) {
-      s_base = s_n ? atomicAdd(Q.count, s_n) : 0u;
-      if (s_max) {
-        atomicMax(Q.max_steps, s_max);
-        if (kMode == kModeBatch) atomicMax(R.stats + kStatMaxSteps, (unsigned long long)s_max);
-      }
-    }
-    __syncthreads();
-    for (unsigned j = threadIdx.x; j < s_n; j += blockDim.x) {
-      const unsigned slot = s_base + j;
-      stage[j].m.store(Q, slot, stage[j].st);
-      if (kMode == kModeRing) Q.cfg[slot] = int(slot);  // the record slot
-      if (kMode == kModeBatch) Q.cfg[slot] = R.run_tag;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) s_n = s_max = 0;
-    __syncthreads();
+  const unsigned cap = front_stage(blockDim.x);
+  // the queue's (and a batch run's) largest remaining step count
+  auto raise_max = [&](unsigned v) {
+    atomicMax(Q.max_steps, v);
+    if (kMode == kModeBatch) atomicMax(R.stats + kStatMaxSteps, (unsigned long long)v);
+  };
+  auto tag = [&](unsigned slot) {
+    if (kMode == kModeRing) Q.cfg[slot] = int(slot);  // the record slot
+    if (kMode == kModeBatch) Q.cfg[slot] = R.run_tag;
   };
   unsigned long long steps = 0, band = 0, bad = 0;
   const int64_t stride = int64_t(gridDim.x) * blockDim.x;
-  for (int64_t base = int64_t(blockIdx.x) * blockDim.x; base < R.n; base += stride) {  // block-uniform
-    const int64_t i = base + threadIdx.x;
+  for (int64_t base = int64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31); base < R.n; base += stride) {
+    const int64_t i = base + lane;
     int label = kNone;
     M m;
     LensStep st;
@@ -295,7 +288,8 @@ __global__ void __launch_bounds__(kFrontMaxThreads) k_front(const __grid_constan
         if (label == R.rec_entrance_label && lens_at == R.rec_lens) R.ent_id[atomicAdd(R.ent_count, 1u)] = int32_t(i);
       }
     }
-    // stage this warp's lens entrants (one shared atomic per warp)
+    // this warp's lens entrants: staged while the area has room (one shared
+    // atomic per warp), the overflow appended to the queue directly
     const bool push = label == kQueued;
     const unsigned pm = __ballot_sync(kFull, push);
     if (pm) {
@@ -304,18 +298,39 @@ __global__ void __launch_bounds__(kFrontMaxThreads) k_front(const __grid_constan
       wb = __shfl_sync(kFull, wb, 0);
       const unsigned rem = push ? unsigned(st.n_total < 0 ? st.bound : st.n_total - st.n_done) : 0u;
       const unsigned wmax = __reduce_max_sync(kFull, rem);
-      if (push) {
-        FrontEntry<M>& e = stage[wb + __popc(pm & lanes_lt)];
+      const unsigned pos = wb + __popc(pm & lanes_lt);
+      const bool over = push && pos >= cap;
+      if (push && !over) {
+        FrontEntry<M>& e = stage[pos];
         e.m = m;
         e.st = st;
       }
-      if (lane == 0 && wmax) atomicMax(&s_max, wmax);
+      if (wb + unsigned(__popc(pm)) <= cap) {  // warp-uniform: all staged
+        if (lane == 0 && wmax) atomicMax(&s_max, wmax);
+      } else {
+        const unsigned slot = queue_slot(over, Q.count);
+        if (over) {
+          m.store(Q, slot, st);
+          tag(slot);
+        }
+        if (lane == 0 && wmax) raise_max(wmax);
+      }
     }
     tally_warp(S, label, P.n_labels);
-    __syncthreads();
-    if (s_n > unsigned(kFrontSlack)) flush();  // room for a full iteration stays
   }
-  flush();
+  // the staged entrants to the queue
+  __syncthreads();
+  const unsigned n_staged = min(s_n, cap);
+  if (threadIdx.x == 0) {
+    s_base = n_staged ? atomicAdd(Q.count, n_staged) : 0u;
+    if (s_max) raise_max(s_max);
+  }
+  __syncthreads();
+  for (unsigned j = threadIdx.x; j < n_staged; j += blockDim.x) {
+    const unsigned slot = s_base + j;
+    stage[j].m.store(Q, slot, stage[j].st);
+    tag(slot);
+  }
   stat_add(S, kStatSteps, steps);
   stat_add(S, kStatEdgeBand, band);
   stat_add(S, kStatBadSteps, bad);
@@ -623,7 +638,7 @@ static __global__ void __launch_bounds__(kOrderThreads) k_order_place(const __gr
 // CTA per SM, 16 warps (k_lens_persist; k_sweep_persist runs it per Stark
 // table of a batched sweep).
 //
-// Phase A (molecules left in the queue): every kPersistService steps a warp
+// Phase A (molecules left in the queue): every `service` steps a warp
 // finalises its lanes whose molecule was lost or left the lens (exit snap,
 // the elements after the lens, tally, next-lens queue) and refills them from
 // the queue in `order`, so lanes stay busy while work remains.
@@ -647,7 +662,7 @@ struct SwapSlot {
 };
 
 constexpr int kPersistThreads = 512;
-constexpr int kPersistService = 16;
+constexpr int kPersistService = 64;  // default steps between phase-A services
 
 struct PersistAcc {
   unsigned long long steps = 0, lsteps = 0, band = 0, bad = 0, range = 0, rerr = 0;
@@ -685,7 +700,8 @@ struct PersistSlot {
 template <class M, bool kOut, int F, bool kStaged, int kMode, int kT = kPersistThreads, int kMPT = 1>
 __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, const int li, const Queue& Qin,
                                              const Queue& Qnext, const LensArgs& L, const unsigned* order,
-                                             const int interval, const unsigned static_entries,
+                                             const int interval, const int service,
+                                             const unsigned static_entries,
                                              const float4* s_tab, SwapSlot* s_swap, unsigned* s_wcount,
                                              BlockTally& S, PersistAcc& acc) {
   constexpr bool kSweep = kMode == kModeSweep, kRing = kMode == kModeRing, kBatch = kMode == kModeBatch;
@@ -856,7 +872,7 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
   }
   // phase A
   for (bool exhausted = static_entries >= n_in && static_entries > 0; !exhausted;) {
-    run(kPersistService);
+    run(service);
     unsigned idle[kMPT], n_idle = 0;
 #pragma unroll
     for (int s = 0; s < kMPT; ++s) {
@@ -981,7 +997,7 @@ template <class M, bool kOut, int F, bool kStaged, int kMode = kModePlain, int k
 __global__ void __launch_bounds__(kT, 1) k_lens_persist(const __grid_constant__ Plan P, const RunDev R,
                                                         const int li, const Queue Qin, const Queue Qnext,
                                                         const LensArgs L, const unsigned* order,
-                                                        const int interval) {
+                                                        const int interval, const int service) {
   extern __shared__ float4 s_dyn[];
   __shared__ BlockTally S;
   __shared__ unsigned s_wcount[kT / 32];
@@ -993,7 +1009,7 @@ __global__ void __launch_bounds__(kT, 1) k_lens_persist(const __grid_constant__ 
   __syncthreads();
   PersistAcc acc;
   // a short queue spreads over all SMs through the interleaved first entries
-  persist_pass<M, kOut, F, kStaged, kMode, kT, kMPT>(P, R, li, Qin, Qnext, L, order, interval,
+  persist_pass<M, kOut, F, kStaged, kMode, kT, kMPT>(P, R, li, Qin, Qnext, L, order, interval, service,
                                                       gridDim.x * kT * kMPT, s_dyn, s_swap, s_wcount, S, acc);
   if (kMode != kModeBatch) persist_flush(S, R, P.n_labels, acc);  // a batch's tallies went to its runs
 }
@@ -1015,7 +1031,8 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_sweep_persist(const __gr
                                                                       const __grid_constant__ SweepQueues Qs,
                                                                       const int n_tab,
                                                                       const __grid_constant__ SweepTabs T,
-                                                                      const LensArgs L0, const int interval) {
+                                                                      const LensArgs L0, const int interval,
+                                                                      const int service) {
   using M = Mol32<false, false>;
   extern __shared__ float4 s_dyn[];
   __shared__ BlockTally S;
@@ -1054,8 +1071,8 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_sweep_persist(const __gr
     L.n_int = T.n_int[t];
     L.n_smem = kStaged ? T.n_int[t] : 0;
     // no interleaved first entries: each CTA takes from its table's queue in order
-    persist_pass<M, false, F, kStaged, kModeSweep>(P, R, li, Q, Q, L, T.order[t], interval, 0u, s_dyn, s_swap,
-                                                  s_wcount, S, acc);
+    persist_pass<M, false, F, kStaged, kModeSweep>(P, R, li, Q, Q, L, T.order[t], interval, service, 0u, s_dyn,
+                                                  s_swap, s_wcount, S, acc);
   }
   persist_flush(S, R, P.n_labels, acc);
 }

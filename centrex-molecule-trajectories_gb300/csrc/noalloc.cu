@@ -256,8 +256,8 @@ int noalloc_launch(const Plan& P, const RunDev& R, Queue* q, unsigned* order_buf
     if (count == 0) break;
     CT_CUDA(cudaMemsetAsync(q[nxt].count, 0, kCtlWords * sizeof(unsigned), s));
     // the persistent pass finishes every molecule: nothing stays inside the lens
-    int st = enqueue_persistent(kOut, kModePlain, P, R, i, q[cur], q[nxt], order_buf, sms, 256, s, launches,
-                                kPersistThreads, 1);
+    int st = enqueue_persistent(kOut, kModePlain, P, R, i, q[cur], q[nxt], order_buf, sms, 256, kPersistService, s,
+                                launches, kPersistThreads, 1);
     if (st) return st;
     std::swap(cur, nxt);
   }

@@ -85,7 +85,7 @@ struct SweepLaunch {
 
 // The persistent sweep lens kernel of a force law; staged when every table fits.
 using SweepPersistKernel = void (*)(const Plan, const RunDev, const int, const SweepQueues, const int,
-                                    const SweepTabs, const LensArgs, const int);
+                                    const SweepTabs, const LensArgs, const int, const int);
 SweepPersistKernel sweep_persist_kernel(int force, bool staged) {
   if (force == kForceStark2Lin)
     return staged ? k_sweep_persist<kForceStark2Lin, true> : k_sweep_persist<kForceStark2Lin, false>;
@@ -150,7 +150,7 @@ int sweep_enqueue(ctraj_context* c, const Plan& P, const RunDev& R, const SweepL
     }
     sweep_persist_kernel(W.force, sweep_staged(W))<<<c->sm_count, kPersistThreads,
                                                                   sweep_persist_smem(W), s>>>(
-        P, R, W.lens, Qs, W.n_tab, T, W.la[0], c->lens_interval);
+        P, R, W.lens, Qs, W.n_tab, T, W.la[0], c->lens_interval, c->lens_service);
     CT_CUDA(cudaGetLastError());
     ++launches;
     if (c->timing) CT_CUDA(record(c->ev[3]));
@@ -376,6 +376,7 @@ extern "C" int ctraj_run_sweep(ctraj_context* c, const ctraj_sweep* sw, const ct
   put(W.chunks.data(), W.chunks.size() * sizeof(int));
   put(&c->lens_mode, sizeof c->lens_mode);
   put(&c->lens_interval, sizeof c->lens_interval);
+  put(&c->lens_service, sizeof c->lens_service);
   put(&c->front_threads, sizeof c->front_threads);
   put(&W.force, sizeof W.force);
   const bool same = key == c->sweep_key;

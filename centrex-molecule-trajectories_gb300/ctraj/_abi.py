@@ -151,6 +151,7 @@ class Tuning(ctypes.Structure):
         ("lens_threads", ctypes.c_int32),
         ("lens_molecules", ctypes.c_int32),
         ("batch_lens_threads", ctypes.c_int32),
+        ("lens_service", ctypes.c_int32),
     ]
 
 

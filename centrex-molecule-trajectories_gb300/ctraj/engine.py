@@ -80,13 +80,13 @@ class Engine:
     def set_tuning(self, chunk_first: int = 64, chunk_growth: int = 200, chunk_max: int = 1024,
                    front_waves: int = 4, lens_mode: int = _abi.LENS_PERSISTENT, lens_interval: int = 256,
                    front_threads: int = 256, batch_group: int = 4, lens_threads: int = 512,
-                   lens_molecules: int = 1, batch_lens_threads: int = 1024):
+                   lens_molecules: int = 1, batch_lens_threads: int = 1024, lens_service: int = 64):
         """ctraj_set_tuning: chunked-lens knobs, front grid and block size, the
-        FP32 lens pass (persistent or chunked) with its compaction interval, and
-        the runs of a batch that share one lens pass."""
+        FP32 lens pass (persistent or chunked) with its compaction and service
+        intervals, and the runs of a batch that share one lens pass."""
         t = _abi.Tuning(int(chunk_first), int(chunk_growth), int(chunk_max), int(front_waves), int(lens_mode),
                         int(lens_interval), int(front_threads), int(batch_group), int(lens_threads),
-                        int(lens_molecules), int(batch_lens_threads))
+                        int(lens_molecules), int(batch_lens_threads), int(lens_service))
         _abi.check(self.lib.ctraj_set_tuning(self.ctx, ctypes.byref(t)), self.lib)
 
     def get_tuning(self) -> dict:

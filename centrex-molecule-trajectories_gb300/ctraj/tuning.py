@@ -6,7 +6,8 @@ launch that refills lanes and compacts the last molecules every
 chunk, the growth of later chunks and their maximum (how often molecules still
 inside a lens are compacted into full warps in chunked mode, which FP64 runs
 always use), the persistent pass's molecules per CTA (``lens_threads``) and
-per thread (``lens_molecules``), the front kernel's grid (``front_waves``)
+per thread (``lens_molecules``) and the steps between a warp's refills of
+its finished lanes (``lens_service``), the front kernel's grid (``front_waves``)
 and block size
 (``front_threads``), and how many consecutive runs of a batch share one lens
 pass (``batch_group``).  None of them changes a result.
@@ -27,20 +28,23 @@ import os
 from pathlib import Path
 
 DEFAULT = dict(chunk_first=64, chunk_growth=200, chunk_max=1024, front_waves=4, lens_mode=0, lens_interval=256,
-               front_threads=256, batch_group=4, lens_threads=512, lens_molecules=1, batch_lens_threads=1024)
+               front_threads=256, batch_group=4, lens_threads=512, lens_molecules=1, batch_lens_threads=1024,
+               lens_service=64)
 
 
 def axes():
     """The search axes, in order: each is a list of partial settings tried on
     top of the best setting found so far.  First the lens pass (persistent, or
-    chunked with each chunk schedule), then the persistent pass's CTA size and
-    compaction interval, then the front kernel's grid and block size."""
+    chunked with each chunk schedule), then the persistent pass's CTA size,
+    service and compaction intervals, then the front kernel's grid and block
+    size."""
     lens = [dict(lens_mode=0)]
     for cf, g, cm in itertools.product((32, 64, 128), (150, 200, 300), (256, 512, 1024, 2048)):
         if cm >= cf:
             lens.append(dict(lens_mode=1, chunk_first=cf, chunk_growth=g, chunk_max=cm))
     return [lens,
             [dict(lens_threads=lt, lens_molecules=m) for lt in (512, 768, 1024) for m in (1, 2)],
+            [dict(lens_service=sv) for sv in (16, 32, 64, 128, 256)],
             [dict(lens_interval=iv) for iv in (64, 128, 256, 512, 1024)],
             [dict(front_waves=fw) for fw in (1, 2, 4, 8)],
             [dict(front_threads=ft) for ft in (128, 256, 512)]]
@@ -48,12 +52,14 @@ def axes():
 
 BATCH_GROUPS = (1, 2, 4, 8, 10, 16)
 BATCH_LENS_THREADS = (512, 768, 1024)
+BATCH_SERVICE = (32, 64, 128, 256)
 
 
 def candidates():
     """Every setting the search may time (the axes' values on top of the defaults)."""
     out = [dict(DEFAULT, **v) for axis in axes() for v in axis]
     out += [dict(DEFAULT, batch_group=g, batch_lens_threads=t) for g in BATCH_GROUPS for t in BATCH_LENS_THREADS]
+    out += [dict(DEFAULT, lens_service=sv) for sv in BATCH_SERVICE]
     return out
 
 
@@ -123,9 +129,10 @@ def autotune(engine, cb, n: int, run_kwargs: dict, device_name: str = "gpu", rep
     milliseconds under the engine's current tuning) times something else,
     e.g. a batched sweep, and ``key_extra`` keeps its cache entry apart.
     ``cands`` replaces the axis search by an explicit list of settings.
-    ``batch`` (a callable like ``batch_measure(...)``) adds the batch axis
-    (batch_group x batch_lens_threads), timed with it after the per-run knobs
-    are fixed."""
+    ``batch`` (a callable like ``batch_measure(...)``) adds the batch axes
+    (batch_group x batch_lens_threads, then lens_service, which the batch's
+    lens passes share with single runs), timed with it after the per-run
+    knobs are fixed."""
     key = workload_key(cb, n, device_name) + key_extra + ("|batch" if batch is not None else "")
     cache = _load_cache() if use_cache else {}
     if use_cache and key in cache:
@@ -168,8 +175,14 @@ def autotune(engine, cb, n: int, run_kwargs: dict, device_name: str = "gpu", rep
                 setting = dict(best, batch_group=g, batch_lens_threads=t)
                 results.append((timed(setting, batch), setting))
         bms, best = min(results, key=lambda x: x[0])
-        result.update(tuning=best, batch_ms_per_run=bms, trials=len(trials) + len(results),
-                      batch_trials={f"{s['batch_group']}x{s['batch_lens_threads']}": t for t, s in results})
+        service = []
+        for sv in BATCH_SERVICE:
+            setting = dict(best, lens_service=sv)
+            service.append((bms if sv == best["lens_service"] else timed(setting, batch), setting))
+        bms, best = min(service, key=lambda x: x[0])
+        result.update(tuning=best, batch_ms_per_run=bms, trials=len(trials) + len(results) + len(service),
+                      batch_trials={f"{s['batch_group']}x{s['batch_lens_threads']}": t for t, s in results},
+                      batch_service_trials={str(s["lens_service"]): t for t, s in service})
     engine.set_tuning(**best)
     if use_cache:
         cache[key] = result

@@ -258,6 +258,10 @@ int ctraj_set_beamline(ctraj_context* ctx, const ctraj_element* elements,
  *                 records) do not depend on it.             default persistent
  *   lens_interval persistent mode: RK4 steps between the CTA's compactions
  *                 once the lens queue is empty                   default 256
+ *   lens_service  persistent mode: RK4 steps between a warp's finalisations
+ *                 and refills of its finished lanes while the queue lasts
+ *                 (longer: fewer, fuller finalisation rounds; shorter: less
+ *                 idle time of finished lanes)                    default 64
  *   front_threads threads per block of the ballistic front kernel: 128, 256
  *                 or 512                                          default 256
  *   batch_group   ctraj_run_batch: consecutive runs (1-64) whose molecules
@@ -297,6 +301,7 @@ typedef struct ctraj_tuning {
   int32_t lens_threads;
   int32_t lens_molecules;
   int32_t batch_lens_threads;
+  int32_t lens_service;
 } ctraj_tuning;
 
 int ctraj_set_tuning(ctraj_context* ctx, const ctraj_tuning* tuning);

@@ -39,8 +39,9 @@ def _same(batch, alone):
         assert b.extra["max_lens_steps"] == a.extra["max_lens_steps"]
 
 
-@pytest.mark.parametrize("group,lanes,mpt", [(1, 512, 1), (2, 768, 1), (3, 512, 2), (16, 768, 2), (4, 1024, 1)])
-def test_grouped_batch_equals_single_runs(engine, group, lanes, mpt):
+@pytest.mark.parametrize("group,lanes,mpt,service", [(1, 512, 1, 64), (2, 768, 1, 5), (3, 512, 2, 64),
+                                                     (16, 768, 2, 300), (4, 1024, 1, 16)])
+def test_grouped_batch_equals_single_runs(engine, group, lanes, mpt, service):
     """Runs sharing lens passes (batch_group > 1) give each run's own results,
     whatever the lens pass's CTA shape; groups of 2 and 3 over 7 runs leave a
     partial last group, 16 takes them all."""
@@ -51,7 +52,7 @@ def test_grouped_batch_equals_single_runs(engine, group, lanes, mpt):
     alone = [engine.run(cb, n + 1000 * k, xdist=xs, vdist=vs, seed=s, offset=3) for k, s in enumerate(seeds)]
     try:
         engine.set_tuning(batch_group=group, front_threads=128 if group == 3 else 256, batch_lens_threads=lanes,
-                          lens_molecules=mpt)
+                          lens_molecules=mpt, lens_service=service)
         batch = engine.run_batch(cb, [n + 1000 * k for k in range(7)], seeds, xdist=xs, vdist=vs, offset=3)
     finally:
         engine.set_tuning()

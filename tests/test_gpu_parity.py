@@ -253,7 +253,8 @@ def test_results_do_not_depend_on_tuning(engine):
                   dict(chunk_first=2048, chunk_growth=150, chunk_max=8192, front_waves=8, lens_mode=1),
                   dict(lens_interval=1), dict(lens_interval=5000, front_waves=2),
                   dict(front_threads=128, front_waves=8), dict(front_threads=512, front_waves=1),
-                  dict(lens_threads=768), dict(lens_threads=1024, lens_interval=64)):
+                  dict(lens_threads=768), dict(lens_threads=1024, lens_interval=64),
+                  dict(lens_service=1), dict(lens_service=16), dict(lens_service=1000, lens_interval=100)):
             engine.set_tuning(**t)
             r = engine.run(cb, 200_000, xdist=xd, vdist=vd, seed=9, outputs=True)
             np.testing.assert_array_equal(r.counts, ref.counts)
@@ -272,7 +273,8 @@ def test_results_do_not_depend_on_tuning(engine):
         np.testing.assert_array_equal(plain.counts, ref.counts)
         for t in (dict(lens_threads=768), dict(lens_threads=1024, lens_interval=64),
                   dict(lens_threads=768, lens_molecules=2), dict(lens_threads=512, lens_molecules=2, lens_interval=32),
-                  dict(lens_threads=1024, lens_molecules=2, lens_interval=1000)):
+                  dict(lens_threads=1024, lens_molecules=2, lens_interval=1000),
+                  dict(lens_threads=1024, lens_service=256), dict(lens_threads=768, lens_molecules=2, lens_service=7)):
             engine.set_tuning(**t)
             r = engine.run(cb, 200_000, xdist=xd, vdist=vd, seed=9)
             np.testing.assert_array_equal(r.counts, ref.counts)
@@ -283,6 +285,8 @@ def test_results_do_not_depend_on_tuning(engine):
             engine.set_tuning(front_threads=300)
         with pytest.raises(ValueError):
             engine.set_tuning(batch_group=65)
+        with pytest.raises(ValueError):
+            engine.set_tuning(lens_service=0)
     finally:
         engine.set_tuning()
 
@@ -298,3 +302,51 @@ def test_stark_table_form(engine, case, linear):
     n = fx["ics"].shape[1]
     assert engine.run(cb, n, precision=32, ics=fx["ics"]).extra["linear_tables"] == linear
     assert engine.run(cb, n, precision=64, ics=fx["ics"]).extra["linear_tables"] == 0
+
+
+def test_front_staging_overflow(engine):
+    """A beam that mostly reaches the lens: a front CTA of 128 threads meets
+    more lens entrants than its staging area holds (192), and its warps append
+    the rest to the queue themselves.  Per-molecule results, counts and step
+    totals equal those of a launch shape that stages every entrant (512
+    threads, one iteration per CTA), in a plain run, a grouped batch and a run
+    with ring recording."""
+    import ctraj
+    from ctraj.distributions import device_spec
+    from ctraj.ring import HBMRing
+    from ctraj.workloads import lens_beamline
+
+    cb = compile_beamline(lens_beamline(aperture_d=0.1))
+    xd = device_spec(ctraj.GaussianPositionDistribution(1.5e-3, 1.5e-3, 0.0), "position")
+    vd = device_spec(ctraj.CeNTREXVelocityDistribution(sigmax=1.0, sigmay=1.0), "velocity")
+    n = 400_000
+    try:
+        engine.set_tuning(front_threads=512, front_waves=8)  # ceil(n / 512) CTAs of one iteration
+        ref = engine.run(cb, n, xdist=xd, vdist=vd, seed=5, outputs=True)
+        reached = 1.0 - ref.counts[cb.labels.index("A1")] / n
+        assert reached > 0.9  # > 0.58 of 329 molecules per CTA overflow 192 entries
+        ring_ref = HBMRing(capacity_rows=28_000_000, capacity_molecules=n, stride=50)  # holds every record
+        rr = engine.run(cb, n, xdist=xd, vdist=vd, seed=5, ring=ring_ref)
+        assert ring_ref.counts()[0] <= ring_ref.capacity_rows
+        batch_ref = engine.run_batch(cb, n, [5, 6], xdist=xd, vdist=vd)
+        engine.set_tuning(front_threads=128, front_waves=1, batch_group=2)  # 1216 CTAs: ~329 molecules each
+        r = engine.run(cb, n, xdist=xd, vdist=vd, seed=5, outputs=True)
+        np.testing.assert_array_equal(r.counts, ref.counts)
+        np.testing.assert_array_equal(r.label, ref.label)
+        np.testing.assert_array_equal(r.final, ref.final)
+        assert (r.molecule_steps, r.lens_steps) == (ref.molecule_steps, ref.lens_steps)
+        ring = HBMRing(capacity_rows=28_000_000, capacity_molecules=n, stride=50)
+        rg = engine.run(cb, n, xdist=xd, vdist=vd, seed=5, ring=ring)
+        np.testing.assert_array_equal(rg.counts, rr.counts)
+        want = {q.molecule: q for q in ring_ref.read()}
+        got = ring.read()
+        assert len(got) == len(want) > 0
+        for q in got:
+            np.testing.assert_array_equal(q.rows, want[q.molecule].rows)
+        batch = engine.run_batch(cb, n, [5, 6], xdist=xd, vdist=vd)
+        for a, b in zip(batch, batch_ref):
+            np.testing.assert_array_equal(a.counts, b.counts)
+            assert (a.molecule_steps, a.lens_steps) == (b.molecule_steps, b.lens_steps)
+        np.testing.assert_array_equal(batch[0].counts, ref.counts)
+    finally:
+        engine.set_tuning()

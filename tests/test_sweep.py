@@ -137,8 +137,8 @@ def test_persistent_and_chunked_sweeps_agree(engine, use_graph):
     try:
         engine.set_tuning(lens_mode=1)
         chunked = run_sweep(bl, cfg, xdist=xs, vdist=vs, seed=4, use_graph=use_graph, engine=engine)
-        for interval in (256, 7):
-            engine.set_tuning(lens_interval=interval)
+        for interval, service in ((256, 64), (7, 3), (256, 500)):
+            engine.set_tuning(lens_interval=interval, lens_service=service)
             pers = run_sweep(bl, cfg, xdist=xs, vdist=vs, seed=4, use_graph=use_graph, engine=engine)
             np.testing.assert_array_equal(pers.counts, chunked.counts)
             assert pers.molecule_steps == chunked.molecule_steps and pers.lens_steps == chunked.lens_steps
