@@ -2,7 +2,8 @@
 // kernels and the linear-table lens lookups (table_interval in molecule.cuh) against the truncating float-to-unsigned
 // conversion and its inverse it replaces, over generated arguments: random
 // bit patterns (negative, NaN, infinite, subnormal and huge values), quarter
-// steps across the table and the neighbours of every integer.
+// steps across the table and the neighbours of every integer; the form for
+// non-negative arguments (table_interval<true>) on those >= 0.
 #include <cuda_runtime.h>
 
 #include "molecule.cuh"
@@ -37,6 +38,12 @@ __global__ void k_interval_check(const long long n, const unsigned last, unsigne
     const float u_ref = __fadd_rn(s, -__uint2float_rn(i_ref));
     const bool same_u = __float_as_uint(u) == __float_as_uint(u_ref) || (isnan(u) && isnan(u_ref));
     bad += (i != i_ref || !same_u) ? 1 : 0;
+    if (s >= 0.0f) {  // the form without max(s, 0), on the arguments it is given
+      unsigned i2;
+      float u2;
+      ctraj::table_interval<true>(s, last, last_f, i2, u2);
+      bad += (i2 != i_ref || __float_as_uint(u2) != __float_as_uint(u_ref)) ? 1 : 0;
+    }
   }
   if (bad) atomicAdd(mismatches, bad);
 }

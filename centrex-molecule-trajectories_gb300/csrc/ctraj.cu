@@ -276,7 +276,7 @@ int check_beamline(const ctraj_context* c) {
 
 int enqueue_persistent(bool out, int mode, const Plan& P, const RunDev& R, int i, const Queue& Qin,
                        const Queue& Qnext, unsigned* order_buf, int sms, int interval, int service, cudaStream_t s,
-                       int* launches, int lanes, int mpt) {
+                       int* launches, int lanes, int mpt, DoneRec* done) {
   const bool staged = P.lf[i].n_smem > 0;
   int kt = kPersistThreads, km = 1;
   const PersistKernel k = persist_kernel(out, P.lf[i].force, mode, staged, lanes, mpt, &kt, &km);
@@ -289,9 +289,14 @@ int enqueue_persistent(bool out, int mode, const Plan& P, const RunDev& R, int i
   k_order_count<<<sms, kOrderThreads, 0, s>>>(P, i, Qin, hist);
   k_order_scan<<<1, kOrderBuckets, 0, s>>>(hist);
   k_order_place<<<sms, kOrderThreads, 0, s>>>(P, i, Qin, hist, order);
-  k<<<sms, kt, smem, s>>>(P, R, i, Qin, Qnext, lens_args(P, i, true), order, interval, service);
+  k<<<sms, kt, smem, s>>>(P, R, i, Qin, Qnext, lens_args(P, i, true), order, interval, service, done);
   CT_CUDA(cudaGetLastError());
   *launches += 4;
+  if (done) {  // the molecules' ends, in full warps
+    finish_kernel(mode)<<<sms * 8, kFinishThreads, 0, s>>>(P, R, i, Qin, Qnext, done);
+    CT_CUDA(cudaGetLastError());
+    *launches += 1;
+  }
   return CTRAJ_OK;
 }
 
@@ -365,9 +370,15 @@ int launch_persistent(ctraj_context* c, bool out, int mode, const Plan& P, const
                       const Queue& Qnext, unsigned count, int* launches) {
   int st = c->lens_order.ensure((size_t(kOrderBuckets) + count) * sizeof(unsigned), 25);
   if (st) return st;
+  // plain and batch passes without per-molecule outputs defer their molecules' ends
+  DoneRec* done = nullptr;
+  if (!out && (mode == kModePlain || mode == kModeBatch)) {
+    if ((st = c->lens_done.ensure(size_t(count) * kDoneRecBytes, 25))) return st;
+    done = c->lens_done.as<DoneRec>();
+  }
   return enqueue_persistent(out, mode, P, R, i, Qin, Qnext, c->lens_order.as<unsigned>(), c->sm_count,
                             c->lens_interval, c->lens_service, c->stream, launches,
-                            mode == kModeBatch ? c->batch_lens_threads : c->lens_threads, c->lens_molecules);
+                            mode == kModeBatch ? c->batch_lens_threads : c->lens_threads, c->lens_molecules, done);
 }
 
 // k_front, then for each lens: read the lens queue's size and largest
@@ -544,6 +555,7 @@ int ctraj_destroy(ctraj_context* c) {
   c->rec_stage.release();
   c->ring_ent.release();
   c->lens_order.release();
+  c->lens_done.release();
   c->sweep_order.release();
   if (c->sweep_exec) cudaGraphExecDestroy(c->sweep_exec);
   for (int t = 0; t < CTRAJ_MAX_TABLES; ++t) {

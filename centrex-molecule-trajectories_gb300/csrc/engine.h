@@ -101,6 +101,7 @@ struct ctraj_context {
   ctraj::DevBuf rec_stage;             // ring recording: staged records of the recorded lens
   ctraj::DevBuf ring_ent;              // ring recording: molecules stopped by the entrance test
   ctraj::DevBuf lens_order;            // persistent lens pass: bucket counts | entrant order
+  ctraj::DevBuf lens_done;             // persistent lens pass: DoneRec per entrant (deferred ends)
   ctraj::DevBuf sweep_order;           // persistent sweep: per table bucket counts | entrant order
   int chunk = 64;               // RK4 steps of the first lens chunk (compaction interval)
   int chunk_growth = 200;       // percent: each chunk's length relative to the previous
@@ -225,18 +226,27 @@ LensKernel sweep_lens_kernel(int force, bool staged);
 // for the hexapole Stark forms also at two, are compiled for the staged-table
 // plain and batch passes without per-molecule outputs (the throughput path);
 // every other pass and setting runs 512 threads x 1.
+struct DoneRec;  // kernels.cuh: a molecule's state after its last step, for k_lens_finish
 using PersistKernel = void (*)(const Plan, const RunDev, const int, const Queue, const Queue, const LensArgs,
-                               const unsigned*, const int, const int);
+                               const unsigned*, const int, const int, DoneRec*);
 PersistKernel persist_kernel(bool out, int force, int mode, bool staged, int lanes, int mpt, int* threads,
                              int* used_mpt);
 template <int F>  // one force law's configurations (k_persist_<law>.cu)
 PersistKernel persist_kernel_for(bool out, int mode, bool staged, int lanes, int mpt, int* threads, int* used_mpt);
 
+// k_lens_finish for a plain or batch pass (k_persist.cu).
+using FinishKernel = void (*)(const Plan, const RunDev, const int, const Queue, const Queue, const DoneRec*);
+FinishKernel finish_kernel(int mode);
+constexpr size_t kDoneRecBytes = 64;
+
 // The persistent FP32 lens pass of lens element i over queue Qin (ctraj.cu):
 // the entrants ordered longest first into `order_buf` (kOrderBuckets + the
-// queue's entries), then one k_lens_persist launch, one CTA per SM.
+// queue's entries), then one k_lens_persist launch, one CTA per SM.  With
+// `done` (kDoneRecBytes per queue entry; plain or batch passes without
+// per-molecule outputs) the molecules' ends are deferred to one k_lens_finish
+// launch after the pass.
 int enqueue_persistent(bool out, int mode, const Plan& P, const RunDev& R, int i, const Queue& Qin,
                        const Queue& Qnext, unsigned* order_buf, int sms, int interval, int service, cudaStream_t s,
-                       int* launches, int lanes, int mpt);
+                       int* launches, int lanes, int mpt, DoneRec* done = nullptr);
 
 }  // namespace ctraj

@@ -2,8 +2,16 @@
 // the dispatch over force laws; each law's configurations are compiled in a
 // translation unit of its own (k_persist_<law>.cu, from k_persist.cuh).
 #include "engine.h"
+#include "kernels.cuh"
 
 namespace ctraj {
+
+static_assert(sizeof(DoneRec) == kDoneRecBytes, "DoneRec layout");
+
+FinishKernel finish_kernel(int mode) {
+  using M = Mol32<false, false>;
+  return mode == kModeBatch ? k_lens_finish<M, kModeBatch> : k_lens_finish<M, kModePlain>;
+}
 
 PersistKernel persist_kernel(bool out, int force, int mode, bool staged, int lanes, int mpt, int* threads,
                              int* used_mpt) {

@@ -668,6 +668,112 @@ struct PersistAcc {
   unsigned long long steps = 0, lsteps = 0, band = 0, bad = 0, range = 0, rerr = 0;
 };
 
+// The end of a molecule's pass through lens li, after its last RK4 step (all
+// lanes call; `fin`: this lane has such a molecule): the rest of its queue
+// entry, the exit snap, the elements after the lens, its tally and stats, or
+// its entry into the next lens's queue.  phase is kLost, kExit or kBad;
+// flags the table-range bits of its steps; idx its queue position; n0 its
+// step count when the pass took it; fresh: its step setup was done in this
+// pass (st.snap holds the exit-snap time, not the queue).  The persistent
+// pass calls it as its lanes finish, or k_lens_finish afterwards from the
+// pass's DoneRec records.
+template <class M, bool kOut, int kMode>
+__device__ __forceinline__ void lens_finish(const Plan& P, const RunDev& R, const int li, const Queue& Qin,
+                                            const Queue& Qnext, const bool fin, M& m, LensStep& st,
+                                            const int phase, const unsigned flags, const unsigned idx,
+                                            const int n0, const bool fresh, const int cfg, BlockTally& S,
+                                            PersistAcc& acc) {
+  constexpr bool kSweep = kMode == kModeSweep, kRing = kMode == kModeRing, kBatch = kMode == kModeBatch;
+  constexpr int kNextTag = kMode == kModePlain ? kTagNone : kTagCarry;
+  const ctraj_element& e = P.el[li];
+  const bool rec_on = kRing && li == R.rec_lens;
+  LensStep nst;
+  int label = kNone;
+  bool enter = false;
+  // this lane's additions to the stats (kStat* order up to kStatRangeError)
+  unsigned d[kStatMaxSteps] = {0u, 0u, 0u, 0u, 0u, 0u};
+  if (fin) {
+    m.load_rest(Qin, idx, st, !fresh);
+    if constexpr (kRing) {
+      if (rec_on) {  // close the record (the state after the losing step) before the exit snap
+        int n_rec = 0;
+        if (phase == kLost) {
+          const int rs = R.rec_stride, k = st.n_done;
+          if (k % rs != 0) R.rec[size_t(cfg) * R.rec_max + k / rs + 1] = make_float4(m.x, m.y, m.vx, m.vy);
+          n_rec = k / rs + 1 + (k % rs != 0 ? 1 : 0);
+          R.rec_last[cfg] = k;
+        }
+        R.rec_n[cfg] = n_rec;  // 0: left the lens (or unusable step count), not recorded
+        if (fresh) {
+          R.rec_id[cfg] = m.id;
+          R.rec_t0[cfg] = m.t;
+          R.rec_vz[cfg] = m.vz;
+        }
+      }
+    }
+    d[kStatLensSteps] = unsigned(st.n_done - n0);
+    if (phase == kBad) {  // rint(L/dz) not usable: the reference raises here
+      label = e.label_inside;
+      d[kStatBadSteps] = 1;
+      d[kStatSteps] = unsigned(m.rows);
+      write_outputs<M, kOut>(R, m, label);
+    } else {
+      d[kStatTableRange] = (flags & 1u) ? 1 : 0;
+      d[kStatRangeError] = (flags & 2u) ? 1 : 0;
+      m.lens_end(P, li, st, phase == kLost);
+      if (phase == kLost) {
+        label = e.label_inside;
+      } else {
+        int lens_at = -1;
+        label = walk(m, P, li + 1, &lens_at);
+        if (label == kQueued) {
+          enter = enter_lens(m, P, lens_at, nst);
+          if (!enter) {
+            label = P.el[lens_at].label_inside;
+            d[kStatBadSteps] += 1;
+          }
+        }
+      }
+      if (label != kQueued) {
+        d[kStatSteps] = unsigned(m.rows);
+        d[kStatEdgeBand] = (m.margin < kEdgeBand) ? 1 : 0;
+        write_outputs<M, kOut>(R, m, label);
+      }
+    }
+  }
+  if constexpr (kBatch) {
+    push_lens<kNextTag>(Qnext, enter, m, nst, cfg,
+                        enter ? R.cfg_stats + size_t(cfg) * kStatCount + kStatMaxSteps : nullptr);
+    const bool done = label != kNone;
+    stats_run(R, done ? cfg : -1, d);
+    tally_cfg(R, cfg, label, P.n_labels);
+  } else {
+    acc.steps += d[kStatSteps];
+    acc.lsteps += d[kStatLensSteps];
+    acc.band += d[kStatEdgeBand];
+    acc.bad += d[kStatBadSteps];
+    acc.range += d[kStatTableRange];
+    acc.rerr += d[kStatRangeError];
+    push_lens<kNextTag>(Qnext, enter, m, nst, cfg);
+    tally_warp(S, label, P.n_labels);
+    if (kSweep) tally_cfg(R, cfg, label, P.n_labels);
+  }
+}
+
+// A molecule's state after its last RK4 step in a persistent pass whose end
+// (lens_finish) is deferred to k_lens_finish: written at its queue position,
+// 64 bytes, read back coalesced.  word = phase | flags << 3 | n0 << 5.
+struct __align__(16) DoneRec {
+  float4 a;          // x, y, vx, vy
+  float4 b;          // cx, cy, cvx, cvy: carried rounding errors
+  double dt;         // lens step time (set in the pass for fresh entries)
+  float ax, ay;      // stored acceleration: the exit snap's
+  int n_done, n_total;
+  float snap;        // exit-snap time
+  unsigned word;
+};
+static_assert(sizeof(DoneRec) == 64, "DoneRec is four 16-byte stores");
+
 // One CTA's share of a persistent pass over Qin.  The first static_entries
 // queue positions are dealt out interleaved across CTAs (entry (w * grid +
 // b) * 32 + lane to lane `lane` of warp w of CTA b); the rest are taken in
@@ -703,9 +809,8 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
                                              const int interval, const int service,
                                              const unsigned static_entries,
                                              const float4* s_tab, SwapSlot* s_swap, unsigned* s_wcount,
-                                             BlockTally& S, PersistAcc& acc) {
-  constexpr bool kSweep = kMode == kModeSweep, kRing = kMode == kModeRing, kBatch = kMode == kModeBatch;
-  constexpr int kNextTag = kMode == kModePlain ? kTagNone : kTagCarry;
+                                             BlockTally& S, PersistAcc& acc, DoneRec* done = nullptr) {
+  constexpr bool kSweep = kMode == kModeSweep, kRing = kMode == kModeRing;
   const unsigned n_in = *(volatile unsigned*)Qin.count;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned lanes_lt = (1u << lane) - 1u;
@@ -786,81 +891,35 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
     }
   };
   // all lanes: the slot-x molecules that were lost or left the lens are
-  // tallied (or queued at the next lens) and the slot becomes idle
+  // finished (tallied, or queued at the next lens) and the slot becomes idle;
+  // with `done`, only their state is written to their DoneRec and
+  // k_lens_finish finishes them after the pass in full warps.
   auto finalize = [&](PersistSlot<M>& x) {
-    if (!__any_sync(kFull, x.phase == kLost || x.phase == kExit || x.phase == kBad)) return;
-    M& m = x.m;
-    LensStep nst;
-    int label = kNone;
-    bool enter = false;
-    // this lane's additions to the stats (kStat* order up to kStatRangeError)
-    unsigned d[kStatMaxSteps] = {0u, 0u, 0u, 0u, 0u, 0u};
-    if (x.phase == kLost || x.phase == kExit || x.phase == kBad) {
-      m.load_rest(Qin, x.idx, x.st, !x.fresh);
-      if constexpr (kRing) {
-        if (rec_on) {  // close the record (the state after the losing step) before the exit snap
-          int n_rec = 0;
-          if (x.phase == kLost) {
-            const int rs = R.rec_stride, k = x.st.n_done;
-            if (k % rs != 0) R.rec[size_t(x.cfg) * R.rec_max + k / rs + 1] = make_float4(m.x, m.y, m.vx, m.vy);
-            n_rec = k / rs + 1 + (k % rs != 0 ? 1 : 0);
-            R.rec_last[x.cfg] = k;
-          }
-          R.rec_n[x.cfg] = n_rec;  // 0: left the lens (or unusable step count), not recorded
-          if (x.fresh) {
-            R.rec_id[x.cfg] = m.id;
-            R.rec_t0[x.cfg] = m.t;
-            R.rec_vz[x.cfg] = m.vz;
-          }
+    const bool fin = x.phase == kLost || x.phase == kExit || x.phase == kBad;
+    if (!__any_sync(kFull, fin)) return;
+    if constexpr (!kOut && (kMode == kModePlain || kMode == kModeBatch)) {
+      // a batch pass always defers (its host always passes `done`); a plain
+      // pass when given `done`
+      if (kMode == kModeBatch || done) {
+        if (fin) {
+          int4* r = reinterpret_cast<int4*>(done + x.idx);
+          r[0] = make_int4(__float_as_int(x.m.x), __float_as_int(x.m.y), __float_as_int(x.m.vx),
+                           __float_as_int(x.m.vy));
+          r[1] = make_int4(__float_as_int(x.m.cx), __float_as_int(x.m.cy), __float_as_int(x.m.cvx),
+                           __float_as_int(x.m.cvy));
+          const long long dtb = __double_as_longlong(x.st.dt);
+          r[2] = make_int4(int(dtb), int(dtb >> 32), __float_as_int(x.m.ax), __float_as_int(x.m.ay));
+          r[3] = make_int4(x.st.n_done, x.st.n_total, __float_as_int(float(x.st.snap)),
+                           int(unsigned(x.phase) | (x.flags & 3u) << 3 | unsigned(x.n0) << 5));
+          x.phase = kIdle;
         }
+        return;
       }
-      d[kStatLensSteps] = unsigned(x.st.n_done - x.n0);
-      if (x.phase == kBad) {  // rint(L/dz) not usable: the reference raises here
-        label = e.label_inside;
-        d[kStatBadSteps] = 1;
-        d[kStatSteps] = unsigned(m.rows);
-        write_outputs<M, kOut>(R, m, label);
-      } else {
-        d[kStatTableRange] = (x.flags & 1u) ? 1 : 0;
-        d[kStatRangeError] = (x.flags & 2u) ? 1 : 0;
-        m.lens_end(P, li, x.st, x.phase == kLost);
-        if (x.phase == kLost) {
-          label = e.label_inside;
-        } else {
-          int lens_at = -1;
-          label = walk(m, P, li + 1, &lens_at);
-          if (label == kQueued) {
-            enter = enter_lens(m, P, lens_at, nst);
-            if (!enter) {
-              label = P.el[lens_at].label_inside;
-              d[kStatBadSteps] += 1;
-            }
-          }
-        }
-        if (label != kQueued) {
-          d[kStatSteps] = unsigned(m.rows);
-          d[kStatEdgeBand] = (m.margin < kEdgeBand) ? 1 : 0;
-          write_outputs<M, kOut>(R, m, label);
-        }
-      }
-      x.phase = kIdle;
     }
-    if constexpr (kBatch) {
-      push_lens<kNextTag>(Qnext, enter, m, nst, x.cfg,
-                          enter ? R.cfg_stats + size_t(x.cfg) * kStatCount + kStatMaxSteps : nullptr);
-      const bool done = label != kNone;
-      stats_run(R, done ? x.cfg : -1, d);
-      tally_cfg(R, x.cfg, label, P.n_labels);
-    } else {
-      acc.steps += d[kStatSteps];
-      acc.lsteps += d[kStatLensSteps];
-      acc.band += d[kStatEdgeBand];
-      acc.bad += d[kStatBadSteps];
-      acc.range += d[kStatTableRange];
-      acc.rerr += d[kStatRangeError];
-      push_lens<kNextTag>(Qnext, enter, m, nst, x.cfg);
-      tally_warp(S, label, P.n_labels);
-      if (kSweep) tally_cfg(R, x.cfg, label, P.n_labels);
+    if constexpr (kOut || kMode != kModeBatch) {
+      lens_finish<M, kOut, kMode>(P, R, li, Qin, Qnext, fin, x.m, x.st, x.phase, x.flags, x.idx, x.n0, x.fresh,
+                                  x.cfg, S, acc);
+      if (fin) x.phase = kIdle;
     }
   };
 
@@ -997,7 +1056,7 @@ template <class M, bool kOut, int F, bool kStaged, int kMode = kModePlain, int k
 __global__ void __launch_bounds__(kT, 1) k_lens_persist(const __grid_constant__ Plan P, const RunDev R,
                                                         const int li, const Queue Qin, const Queue Qnext,
                                                         const LensArgs L, const unsigned* order,
-                                                        const int interval, const int service) {
+                                                        const int interval, const int service, DoneRec* done) {
   extern __shared__ float4 s_dyn[];
   __shared__ BlockTally S;
   __shared__ unsigned s_wcount[kT / 32];
@@ -1010,8 +1069,62 @@ __global__ void __launch_bounds__(kT, 1) k_lens_persist(const __grid_constant__ 
   PersistAcc acc;
   // a short queue spreads over all SMs through the interleaved first entries
   persist_pass<M, kOut, F, kStaged, kMode, kT, kMPT>(P, R, li, Qin, Qnext, L, order, interval, service,
-                                                      gridDim.x * kT * kMPT, s_dyn, s_swap, s_wcount, S, acc);
-  if (kMode != kModeBatch) persist_flush(S, R, P.n_labels, acc);  // a batch's tallies went to its runs
+                                                      gridDim.x * kT * kMPT, s_dyn, s_swap, s_wcount, S, acc,
+                                                      done);
+  // a batch's tallies went to its runs; deferred ends are tallied by k_lens_finish
+  if (kMode != kModeBatch && !done) persist_flush(S, R, P.n_labels, acc);
+}
+
+// The deferred ends of a persistent pass's molecules (lens_finish), one
+// thread per queue position of Qin, in full warps, from the DoneRec records
+// the pass wrote (k_lens_persist with `done`; runs without per-molecule
+// outputs, plain or batch mode).  Grid-stride over the queue.
+constexpr int kFinishThreads = 256;
+
+template <class M, int kMode>
+__global__ void __launch_bounds__(kFinishThreads) k_lens_finish(const __grid_constant__ Plan P, const RunDev R,
+                                                                const int li, const Queue Qin, const Queue Qnext,
+                                                                const DoneRec* done) {
+  __shared__ BlockTally S;
+  tally_init(S);
+  __syncthreads();
+  PersistAcc acc;
+  const unsigned n = *(volatile unsigned*)Qin.count;
+  const unsigned stride = gridDim.x * blockDim.x;
+  for (unsigned base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {  // warp-uniform
+    const unsigned j = base + (threadIdx.x & 31);
+    const bool fin = j < n;
+    M m;
+    LensStep st;
+    int phase = kIdle, n0 = 0, cfg = 0;
+    unsigned flags = 0;
+    if (fin) {
+      const int4* r = reinterpret_cast<const int4*>(done + j);
+      const int4 r0 = r[0], r1 = r[1], r2 = r[2], r3 = r[3];
+      m.x = __int_as_float(r0.x);
+      m.y = __int_as_float(r0.y);
+      m.vx = __int_as_float(r0.z);
+      m.vy = __int_as_float(r0.w);
+      m.cx = __int_as_float(r1.x);
+      m.cy = __int_as_float(r1.y);
+      m.cvx = __int_as_float(r1.z);
+      m.cvy = __int_as_float(r1.w);
+      st.dt = __longlong_as_double((long long)(unsigned(r2.x)) | (long long)(r2.y) << 32);
+      m.ax = __int_as_float(r2.z);
+      m.ay = __int_as_float(r2.w);
+      st.n_done = r3.x;
+      st.n_total = r3.y;
+      st.snap = double(__int_as_float(r3.z));
+      phase = int(unsigned(r3.w) & 7u);
+      flags = (unsigned(r3.w) >> 3) & 3u;
+      n0 = int(unsigned(r3.w) >> 5);
+      m.margin = INFINITY;
+      if (kMode == kModeBatch) cfg = Qin.cfg[j];
+    }
+    // fresh = true: the exit-snap time comes from the record, not the queue
+    lens_finish<M, false, kMode>(P, R, li, Qin, Qnext, fin, m, st, phase, flags, j, n0, true, cfg, S, acc);
+  }
+  if (kMode != kModeBatch) persist_flush(S, R, P.n_labels, acc);
 }
 
 // Batched sweep: the Stark tables' lens queues in one launch.  Each CTA

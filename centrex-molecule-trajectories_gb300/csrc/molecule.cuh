@@ -216,10 +216,15 @@ __device__ inline int mesh_nearest32(const LensF& L, const ElemF& f, float px, f
 // kernels (4 % faster) and the linear-table lens lookups (one warp's step
 // 323 -> 231 cycles) use it; the quadratic-table lookups keep the
 // conversions, which measured as fast there.
+// kNonNeg: s is known to be >= 0 or NaN (a linear Stark table starts at
+// |E| = 0 and its coordinate scale is not negative), so max(s, 0) is left
+// out; only a NaN s then takes the last interval instead of the first, and
+// u, hence the force, is NaN either way.
 // ---------------------------------------------------------------------------
+template <bool kNonNeg = false>
 __device__ __forceinline__ void table_interval(const float s, const unsigned last, const float last_f,
                                                unsigned& i, float& u) {
-  const float t = __fadd_rd(fmaxf(s, 0.0f), 8388608.0f);
+  const float t = __fadd_rd(kNonNeg ? s : fmaxf(s, 0.0f), 8388608.0f);
   i = min(__float_as_uint(t) - 0x4B000000u, last);
   u = __fadd_rn(s, -fminf(__fadd_rn(t, -8388608.0f), last_f));
 }
@@ -232,7 +237,9 @@ __device__ __forceinline__ void table_interval(const float s, const unsigned las
 // interval extrapolate it (as scipy CubicSpline does); s < 0 uses interval 0.
 // `beta` is the table-coordinate scale (L.beta, or a molecule's own in a
 // batched sweep where each configuration has its lens voltage).
-template <int F, bool kStaged>
+// kScaled: beta is a molecule's own (a batched sweep's configuration), not
+// the table's L.beta, which the host checked to be >= 0.
+template <int F, bool kStaged, bool kScaled = false>
 __device__ __forceinline__ float wforce(float px, float py, const LensArgs& L, const float4* s_tab,
                                         unsigned& flags, const float beta) {
   const float r2 = __fmaf_rn(py, py, __fmul_rn(px, px));
@@ -245,7 +252,8 @@ __device__ __forceinline__ float wforce(float px, float py, const LensArgs& L, c
     // instead of 323 cycles, bit-identical)
     unsigned i;
     float u;
-    table_interval(s, unsigned(2 * L.n_int - 1), __int2float_rn(2 * L.n_int - 1), i, u);
+    // s >= 0: the linear form's table starts at |E| = 0 (s0 <= 0) and L.beta >= 0
+    table_interval<!kScaled>(s, unsigned(2 * L.n_int - 1), __int2float_rn(2 * L.n_int - 1), i, u);
     const float2 q = kStaged ? reinterpret_cast<const float2*>(s_tab)[i]
                              : __ldg(reinterpret_cast<const float2*>(L.q) + i);
     return __fmaf_rn(u, q.y, q.x);
@@ -722,7 +730,7 @@ struct Mol32 {
     const float g = L.g;
     const float b = kScaled ? beta : L.beta;
     auto force = [&](float px, float py) {
-      const float w = wforce<F, kStaged>(px, py, L, s_tab, flags, b);
+      const float w = wforce<F, kStaged, kScaled>(px, py, L, s_tab, flags, b);
       return kScaled ? __fmul_rn(kappa, w) : w;
     };
     // The (x, y) pairs go through the packed FP32 instructions of sm_100+

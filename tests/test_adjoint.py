@@ -214,7 +214,7 @@ def test_autograd_function(engine):
     loss = soft_loss(p, prob, engine)
     (2.0 * loss).backward()
     ref = soft_transmission(prob, params(prob), engine=engine)
-    assert float(loss) == ref.loss
+    assert float(loss.detach()) == ref.loss
     np.testing.assert_array_equal(p.grad.numpy(), 2.0 * ref.grad)
     with torch.no_grad():
         assert float(soft_loss(p, prob, engine)) == ref.loss
