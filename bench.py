@@ -59,7 +59,7 @@ FLOP_PER_BALLISTIC_STEP = 12
 # launch per 1e7 molecules of the group, from the ncu capture summarised in
 # profiles/k_lens_persist_grouped_lens_beamline.md (the queue is read once;
 # the table and the molecule state stay on chip)
-LENS_DRAM_BYTES_PER_1E7 = 12.30e6
+LENS_DRAM_BYTES_PER_1E7 = 9.72e6
 # Shared-memory wavefronts per warp table lookup (the bench table goes to the
 # kernels in the 8-byte linear form: one LDS.64 per lane, random intervals,
 # bank-conflicted), from l1tex__data_pipe_lsu_wavefronts_mem_shared_op_ld of the
@@ -77,7 +77,7 @@ def shared_roof(lens_steps_per_s: float, sms: int, mhz: float) -> dict:
             "wavefronts_per_lookup": SHARED_WAVEFRONTS_PER_LOOKUP, "lookups_per_step": LOOKUPS_PER_RK4_STEP,
             "roof": roof, "achieved": lens_steps_per_s, "frac": lens_steps_per_s / roof,
             "note": "1 shared-memory wavefront per cycle per SM; wavefronts per lookup from ncu"}
-L2_NOTE = ("GPU arm: 256 MiB written before every run on the run's stream inside the timed region; "
+L2_NOTE = ("GPU arm: 160 MiB (1.3 x the 126 MiB L2) written before every run on the run's stream inside the timed region; "
            "CPU arm: not applicable")
 
 
@@ -711,7 +711,7 @@ def main():
     eng = default_engine(local)  # the engine the drop-in TrajectorySimulator uses too
     stream = torch.cuda.current_stream()
     eng.set_stream(stream.cuda_stream)
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB of L2
+    flush = torch.empty(160 << 20, dtype=torch.uint8, device="cuda")  # 1.3 x the 126 MiB (129 MB) L2
 
     def step(seed):
         return eng.run(cb, n, precision=32, xdist=xs, vdist=vs, seed=seed, offset=rank * n, timing=True)
@@ -758,6 +758,15 @@ def main():
         ev1.synchronize()
         batch_ms = ev0.elapsed_time(ev1)
         tun = eng.get_tuning()  # the headline's knobs (the sweep and adjoint below set their own)
+        # the dominant kernel alone: one group of batch_group runs (one lane,
+        # nothing beside it); its lens pass (ordering, k_lens_persist,
+        # k_lens_finish) timed with CUDA events on the lane's stream
+        iso = []
+        for rep in range(3):
+            flush.zero_()
+            rs = eng.run_batch(cb, n, seeds[:tun["batch_group"]], precision=32, xdist=xs, vdist=vs,
+                               offset=rank * n, timing=True)
+            iso.append((sum(r.extra.get("lens_ms", 0.0) for r in rs), sum(r.lens_steps for r in rs), len(rs)))
         torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
@@ -858,25 +867,33 @@ def main():
     groups = -(-args.steps // tun["batch_group"]) if tun["lens_mode"] == 0 else args.steps
     g_lens_ms = sum(r.extra.get("lens_ms", 0.0) for r in batch)
     g_lens_steps = sum(r.lens_steps for r in batch)
-    achieved = g_lens_steps * FLOP_PER_RK4_STEP / (g_lens_ms / 1e3) / 1e12
+    iso_ms = sum(t for t, _, _ in iso) / len(iso)
+    iso_steps, iso_runs = iso[-1][1], iso[-1][2]
+    achieved = iso_steps * FLOP_PER_RK4_STEP / (iso_ms / 1e3) / 1e12
     mhz = clocks.get("sm_mhz") if clocks else None
     sms = torch.cuda.get_device_properties(local).multi_processor_count
     roofline = {"bound": "fp32",
                 "kernel": f"k_lens_persist, grouped: the lens pass {tun['batch_group']} runs of the batch share "
                           f"({tun['batch_lens_threads']} threads per CTA, one CTA per SM; with its entrant "
-                          f"ordering, timed together)",
+                          f"ordering and k_lens_finish, timed together)",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
                 "peak_source": "measured in this run: FMA-chain kernel (bench_kernels/fp32_peak.cu), "
                                "MEASURED_PEAKS.json has no FP32 CUDA-core figure",
-                "flop_per_step": FLOP_PER_RK4_STEP, "launches": groups,
-                "lens_steps_per_launch": g_lens_steps / groups, "lens_ms_per_launch": g_lens_ms / groups,
-                "front_ms_per_run": sum(r.extra.get("front_ms", 0.0) for r in batch) / args.steps,
-                "traffic": LENS_DRAM_BYTES_PER_1E7 * n * args.steps / groups / 1e7,
+                "flop_per_step": FLOP_PER_RK4_STEP, "runs_per_launch": iso_runs,
+                "lens_steps_per_launch": iso_steps, "lens_ms_per_launch": iso_ms,
+                "timing": "CUDA events on the lane's stream around one group's lens pass, the group run alone "
+                          "(a batch of batch_group runs) right after the timed region, mean of 3",
+                "in_batch": {"launches": groups, "lens_span_ms_per_launch": g_lens_ms / groups,
+                             "lens_steps_per_launch": g_lens_steps / groups,
+                             "front_span_ms_per_run": sum(r.extra.get("front_ms", 0.0) for r in batch) / args.steps,
+                             "note": "event spans on each lane's stream inside the timed batch: a lens pass's span "
+                                     "includes waiting for SMs the other lane's kernels hold"},
+                "traffic": LENS_DRAM_BYTES_PER_1E7 * n * iso_runs / 1e7,
                 "traffic_unit": "bytes per grouped lens pass: ncu DRAM bytes of one grouped k_lens_persist launch "
-                                "on a smaller group, scaled by molecules per launch",
+                                "on a 1e7-molecule group, scaled by molecules per launch",
                 "step_probe": probe}
     if mhz:
-        roofline["shared_memory"] = shared_roof(g_lens_steps / (g_lens_ms / 1e3), sms, mhz)
+        roofline["shared_memory"] = shared_roof(iso_steps / (iso_ms / 1e3), sms, mhz)
     # the single-run lens pass (one ctraj_run at a time): bound by its critical
     # path, the molecule with the most RK4 steps, which cannot finish before
     # that many steps of one-warp latency (the step probe)
@@ -908,7 +925,7 @@ def main():
                        "pipelining": "ctraj_run_batch: the K runs alternate between two lanes (contexts with "
                                      "their own streams and buffers, one host thread each); a run's front "
                                      "overlaps the other lane's lens pass",
-                       "l2": "flushed before every run: 256 MiB written on the run's lane stream inside the "
+                       "l2": "flushed before every run: 160 MiB written on the run's lane stream inside the "
                              "timed region (pipelined batch); between steps outside the events (sequential)",
                        "parallelism": f"replicas x{world}",
                        "tuning": tuned["tuning"], "tuning_cached": tuned.get("cached", False)},
