@@ -366,6 +366,9 @@ int prepare(ctraj_context* c, const ctraj_run_args* a, Plan& P, RunDev& R) {
 namespace {
 
 // The persistent lens pass of a run on context c (its order buffer and tuning).
+// count: the most entries Qin can hold (its count, or its capacity when the
+// pass is enqueued without reading the count back); it sizes the entrant
+// order and the molecules' end records.
 int launch_persistent(ctraj_context* c, bool out, int mode, const Plan& P, const RunDev& R, int i, const Queue& Qin,
                       const Queue& Qnext, unsigned count, int* launches) {
   int st = c->lens_order.ensure((size_t(kOrderBuckets) + count) * sizeof(unsigned), 25);
@@ -403,8 +406,25 @@ int launch_all(ctraj_context* c, const Plan& P, const RunDev& R0, Queue* q, int*
   if (c->timing) CT_CUDA(cudaEventRecord(c->ev[1], s));
   bool started = false;
   int cur = 0, alt = 1, nxt = 2;
+  // The FP32 persistent pass needs nothing from the host mid-run: its
+  // kernels read the lens queue's count on the device (and return at once
+  // when it is 0), its buffers are sized for the queue's capacity, and the
+  // largest step bound (a statistic) is copied back with the counts.  The
+  // whole run is enqueued without a synchronisation.
+  const bool async = !k64 && !kRing && c->lens_mode == CTRAJ_LENS_PERSISTENT;
+  c->lens_async = async;
   for (int i = 0; i < P.n_el && n > 0; ++i) {
     if (P.el[i].type != CTRAJ_ELECTROSTATIC_LENS) continue;
+    if (async) {
+      if (c->timing && !started) CT_CUDA(cudaEventRecord(c->ev[2], s));
+      started = true;
+      CT_CUDA(cudaMemcpyAsync(c->host_lens + i, q[cur].max_steps, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+      CT_CUDA(cudaMemsetAsync(q[nxt].count, 0, kCtlWords * sizeof(unsigned), s));
+      int st = launch_persistent(c, kOut, kModePlain, P, R, i, q[cur], q[nxt], unsigned(n), launches);
+      if (st) return st;
+      std::swap(cur, nxt);
+      continue;
+    }
     CT_CUDA(cudaMemcpyAsync(c->host_max, q[cur].count, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     CT_CUDA(cudaStreamSynchronize(s));
     const unsigned count = c->host_max[0], max_steps = c->host_max[1];
@@ -479,13 +499,19 @@ int launch_all(ctraj_context* c, const Plan& P, const RunDev& R0, Queue* q, int*
     std::swap(cur, nxt);  // the next lens starts from the molecules queued at its entrance
   }
   if (kRing && n > 0) {  // also when no molecule reached the lens: entrance losses
-    k_ring_reserve<<<c->sm_count * 8, 256, 0, s>>>(R, ring_slots);
+    int st = c->ring_part.ensure(2 * kRingBlocks * sizeof(unsigned long long));
+    if (st) return st;
+    unsigned long long* part = c->ring_part.as<unsigned long long>();
+    k_ring_count<<<kRingBlocks, kRingThreads, 0, s>>>(R, ring_slots, part);
+    k_ring_scan<<<1, kRingBlocks, 0, s>>>(R, part);
+    k_ring_reserve<<<kRingBlocks, kRingThreads, 0, s>>>(R, ring_slots, part);
     CT_CUDA(cudaGetLastError());
     if constexpr (!k64) {
       k_ring_write<Mol32<false, false>><<<c->sm_count * 8, 256, 0, s>>>(P, R, ring_slots);
       CT_CUDA(cudaGetLastError());
+      *launches += 1;
     }
-    *launches += 2;
+    *launches += 3;
   }
   if (c->timing) {
     if (!started) CT_CUDA(cudaEventRecord(c->ev[2], s));
@@ -521,6 +547,7 @@ int ctraj_create(int device, ctraj_context** out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
   for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
   if (e == cudaSuccess) e = cudaMallocHost(&c->host_max, (2 + CTRAJ_MAX_ELEMENTS) * sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMallocHost(&c->host_lens, CTRAJ_MAX_ELEMENTS * sizeof(unsigned));
   c->stream = c->own_stream;
   if (e != cudaSuccess) {
     ctraj_destroy(c);
@@ -556,6 +583,7 @@ int ctraj_destroy(ctraj_context* c) {
   c->ring_ent.release();
   c->lens_order.release();
   c->lens_done.release();
+  c->ring_part.release();
   c->sweep_order.release();
   if (c->sweep_exec) cudaGraphExecDestroy(c->sweep_exec);
   for (int t = 0; t < CTRAJ_MAX_TABLES; ++t) {
@@ -586,6 +614,7 @@ int ctraj_destroy(ctraj_context* c) {
   if (c->group_host) cudaFreeHost(c->group_host);
   if (c->batch_ev) cudaEventDestroy(c->batch_ev);
   if (c->host_max) cudaFreeHost(c->host_max);
+  if (c->host_lens) cudaFreeHost(c->host_lens);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
   return CTRAJ_OK;
@@ -779,6 +808,8 @@ static int run_impl(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* 
   }
   int launches = 0;
   std::memset(c->host_max, 0, (2 + CTRAJ_MAX_ELEMENTS) * sizeof(unsigned));
+  std::memset(c->host_lens, 0, CTRAJ_MAX_ELEMENTS * sizeof(unsigned));
+  c->lens_async = false;
   c->timing = a->timing != 0;
   if (ring)
     st = out ? launch_all<false, true, true>(c, P, R, q, &launches)
@@ -798,6 +829,8 @@ static int run_impl(ctraj_context* c, const ctraj_run_args* a, ctraj_run_stats* 
     if (a->out_final) CT_CUDA(cudaMemcpyAsync(a->out_final, R.out_final, n * 80, cudaMemcpyDeviceToHost, c->stream));
   }
   CT_CUDA(cudaStreamSynchronize(c->stream));
+  if (c->lens_async)
+    for (int i = 0; i < P.n_el; ++i) c->run_max_steps = std::max(c->run_max_steps, c->host_lens[i]);
   for (int i = 0; i < P.n_el; ++i)
     if (c->host_max[2 + i] != 0)
       return fail(CTRAJ_ECUDA, "internal error: %u molecules left inside lens element %d",
@@ -940,16 +973,15 @@ static int run_group(ctraj_context* c, const ctraj_run_args* a, int g, ctraj_run
   Rg.stats = nullptr;
   bool started = false;
   int cur = 0, nxt = 2;
+  // enqueued without a synchronisation, as a single run's persistent pass
+  // (launch_all): the kernels read the queue counts on the device
   for (int i = 0; i < P.n_el && total > 0; ++i) {
     if (P.el[i].type != CTRAJ_ELECTROSTATIC_LENS) continue;
-    CT_CUDA(cudaMemcpyAsync(c->host_max, q[cur].count, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-    CT_CUDA(cudaStreamSynchronize(s));
-    const unsigned count = c->host_max[0];
-    if (count == 0) break;
     if (timing && !started) CT_CUDA(cudaEventRecord(c->ev[2], s));
     started = true;
     CT_CUDA(cudaMemsetAsync(q[nxt].count, 0, kCtlWords * sizeof(unsigned), s));
-    if ((st = launch_persistent(c, false, kModeBatch, P, Rg, i, q[cur], q[nxt], count, &launches))) return st;
+    if ((st = launch_persistent(c, false, kModeBatch, P, Rg, i, q[cur], q[nxt], unsigned(total), &launches)))
+      return st;
     std::swap(cur, nxt);
   }
   if (timing) {

@@ -97,11 +97,14 @@ struct ctraj_context {
   ctraj::DevBuf outs;
   ctraj::DevBuf rec_rows, rec_ids, rec_count;
   unsigned* host_max = nullptr; // pinned: largest remaining lens step count of a queue
+  unsigned* host_lens = nullptr; // pinned: per element, its lens queue's largest step bound (async pass)
+  bool lens_async = false;      // the last run's lens passes were enqueued without a sync
   ctraj::DevBuf chunk_ctl;             // (count, max_steps) of the queue each lens chunk writes
   ctraj::DevBuf rec_stage;             // ring recording: staged records of the recorded lens
   ctraj::DevBuf ring_ent;              // ring recording: molecules stopped by the entrance test
   ctraj::DevBuf lens_order;            // persistent lens pass: bucket counts | entrant order
   ctraj::DevBuf lens_done;             // persistent lens pass: DoneRec per entrant (deferred ends)
+  ctraj::DevBuf ring_part;             // ring recording: per-block row / entry sums and bases
   ctraj::DevBuf sweep_order;           // persistent sweep: per table bucket counts | entrant order
   int chunk = 64;               // RK4 steps of the first lens chunk (compaction interval)
   int chunk_growth = 200;       // percent: each chunk's length relative to the previous

@@ -1191,43 +1191,123 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_sweep_persist(const __gr
 }
 
 // ---------------------------------------------------------------------------
-// Ring recording, appended in two launches so that no write lands on a newer
-// one: k_ring_reserve takes each record's rows and index entry from the heads
-// (molecules lost inside the recorded lens: rec_n > 0 staged records;
-// molecules stopped by its entrance test: one record each), k_ring_write then
-// reads the final heads and writes only what lies within the last
-// capacity_rows rows / capacity_molecules entries, where positions are
-// distinct.  One thread per record slot or listed molecule.
-static __global__ void __launch_bounds__(256) k_ring_reserve(const RunDev R, unsigned n_slots) {
-  const ctraj_ring& G = R.ring;
-  const unsigned n_ent = *R.ent_count;
-  const unsigned total = n_slots + n_ent;
-  const int lane = threadIdx.x & 31;
-  const unsigned stride = gridDim.x * blockDim.x;
-  // warp-uniform loop; one pair of atomics per warp (prefix sums over the lanes)
-  for (unsigned base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total; base += stride) {
-    const unsigned s = base + lane;
-    const bool lens = s < n_slots;
-    const int n_rec = s < total ? (lens ? R.rec_n[s] : 1) : 0;
-    const bool take = n_rec > 0;
-    unsigned long long rows = (unsigned long long)(take ? n_rec : 0);
+// Ring recording, appended so that no write lands on a newer one and the
+// rows and index entries of a run are taken in one order: records are
+// numbered by slot (molecules lost inside the recorded lens: their record
+// slot, rec_n > 0 staged records; then the molecules stopped by its entrance
+// test: one record each), k_ring_count sums each block's contiguous range of
+// records, k_ring_scan turns the sums into each block's first row and index
+// entry after the ring's heads (and advances the heads), k_ring_reserve gives
+// every record its rows and entry in slot order, and k_ring_write reads the
+// final heads and writes only what lies within the last capacity_rows rows /
+// capacity_molecules entries, where positions are distinct.  Because rows and
+// entries follow one order, the latest index entries hold the latest rows.
+constexpr int kRingBlocks = 512, kRingThreads = 256;
+
+__device__ __forceinline__ int ring_record_rows(const RunDev& R, unsigned s, unsigned n_slots) {
+  return s < n_slots ? R.rec_n[s] : 1;
+}
+
+// Block-wide inclusive scan of (a, b) over the threads of a kRingThreads block.
+__device__ __forceinline__ void ring_block_scan(unsigned long long& a, unsigned long long& b,
+                                                unsigned long long* s_a, unsigned long long* s_b) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {  // inclusive scan of the row counts
-      const unsigned long long v = __shfl_up_sync(kFull, rows, o);
-      if (lane >= o) rows += v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long va = __shfl_up_sync(kFull, a, o), vb = __shfl_up_sync(kFull, b, o);
+    if (lane >= o) {
+      a += va;
+      b += vb;
     }
-    const unsigned mask = __ballot_sync(kFull, take);
-    unsigned long long rbase = 0, mbase = 0;
-    if (lane == 31) {
-      if (rows) rbase = atomicAdd(&G.heads[0], rows);
-      if (mask) mbase = atomicAdd(&G.heads[1], (unsigned long long)__popc(mask));
+  }
+  if (lane == 31) {
+    s_a[warp] = a;
+    s_b[warp] = b;
+  }
+  __syncthreads();
+  unsigned long long pa = 0, pb = 0;
+  for (int w = 0; w < warp; ++w) {
+    pa += s_a[w];
+    pb += s_b[w];
+  }
+  a += pa;
+  b += pb;
+  __syncthreads();
+}
+
+static __global__ void __launch_bounds__(kRingThreads) k_ring_count(const RunDev R, unsigned n_slots,
+                                                                    unsigned long long* part) {
+  __shared__ unsigned long long s_a[kRingThreads / 32], s_b[kRingThreads / 32];
+  unsigned lo, hi;
+  order_range(n_slots + *R.ent_count, lo, hi);
+  unsigned long long rows = 0, recs = 0;
+  for (unsigned s = lo + threadIdx.x; s < hi; s += blockDim.x) {
+    const int k = ring_record_rows(R, s, n_slots);
+    if (k > 0) {
+      rows += (unsigned long long)k;
+      ++recs;
     }
-    rbase = __shfl_sync(kFull, rbase, 31);
-    mbase = __shfl_sync(kFull, mbase, 31);
+  }
+  ring_block_scan(rows, recs, s_a, s_b);
+  if (threadIdx.x == blockDim.x - 1) {
+    part[2 * blockIdx.x] = rows;
+    part[2 * blockIdx.x + 1] = recs;
+  }
+}
+
+static __global__ void __launch_bounds__(kRingBlocks) k_ring_scan(const RunDev R, unsigned long long* part) {
+  __shared__ unsigned long long s_a[kRingBlocks / 32], s_b[kRingBlocks / 32];
+  const ctraj_ring& G = R.ring;
+  const int t = threadIdx.x;
+  const unsigned long long own_r = part[2 * t], own_m = part[2 * t + 1];
+  unsigned long long r = own_r, m = own_m;
+  // inclusive scan over the kRingBlocks blocks (warp scans, then the warps' totals)
+  const int lane = t & 31, warp = t >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long vr = __shfl_up_sync(kFull, r, o), vm = __shfl_up_sync(kFull, m, o);
+    if (lane >= o) {
+      r += vr;
+      m += vm;
+    }
+  }
+  if (lane == 31) {
+    s_a[warp] = r;
+    s_b[warp] = m;
+  }
+  __syncthreads();
+  unsigned long long pr = 0, pm = 0;
+  for (int w = 0; w < warp; ++w) {
+    pr += s_a[w];
+    pm += s_b[w];
+  }
+  r += pr;
+  m += pm;
+  const unsigned long long h0 = G.heads[0], h1 = G.heads[1];
+  __syncthreads();  // every thread has read the heads before the last one moves them
+  part[2 * t] = h0 + r - own_r;  // the block's first row and index entry
+  part[2 * t + 1] = h1 + m - own_m;
+  if (t == kRingBlocks - 1) {
+    G.heads[0] = h0 + r;
+    G.heads[1] = h1 + m;
+  }
+}
+
+static __global__ void __launch_bounds__(kRingThreads) k_ring_reserve(const RunDev R, unsigned n_slots,
+                                                                      const unsigned long long* part) {
+  __shared__ unsigned long long s_a[kRingThreads / 32], s_b[kRingThreads / 32];
+  unsigned lo, hi;
+  order_range(n_slots + *R.ent_count, lo, hi);
+  unsigned long long rbase = part[2 * blockIdx.x], mbase = part[2 * blockIdx.x + 1];
+  for (unsigned c0 = lo; c0 < hi; c0 += blockDim.x) {  // block-uniform
+    const unsigned s = c0 + threadIdx.x;
+    const int k = s < hi ? ring_record_rows(R, s, n_slots) : 0;
+    const bool take = k > 0;
+    unsigned long long rows = take ? (unsigned long long)k : 0, recs = take ? 1 : 0;
+    ring_block_scan(rows, recs, s_a, s_b);  // inclusive
     if (take) {
-      const unsigned long long r0 = rbase + rows - (unsigned long long)n_rec;
-      const unsigned long long m0 = mbase + __popc(mask & ((1u << lane) - 1u));
-      if (lens) {
+      const unsigned long long r0 = rbase + rows - (unsigned long long)k, m0 = mbase + recs - 1;
+      if (s < n_slots) {
         R.rec_r0[s] = r0;
         R.rec_m0[s] = m0;
       } else {
@@ -1235,6 +1315,15 @@ static __global__ void __launch_bounds__(256) k_ring_reserve(const RunDev R, uns
         R.ent_m0[s - n_slots] = m0;
       }
     }
+    // the chunk's totals: the last thread's inclusive sums
+    if (threadIdx.x == blockDim.x - 1) {
+      s_a[0] = rows;
+      s_b[0] = recs;
+    }
+    __syncthreads();
+    rbase += s_a[0];
+    mbase += s_b[0];
+    __syncthreads();
   }
 }
 

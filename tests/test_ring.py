@@ -85,9 +85,10 @@ def test_small_ring_keeps_the_latest_complete_records(engine):
     big = HBMRing(capacity_rows=100_000, capacity_molecules=10_000, stride=STRIDE)
     engine.run(cb, n, xdist=xs, vdist=vs, seed=5, ring=big)
     full = {rec.molecule: rec.rows for rec in big.read()}
-    # rows and index entries are reserved by two counters, so the latest index
-    # entries need not have the latest rows: give the rows room for ~150
-    # molecules and the index 40 entries
+    # rows and index entries are taken in one order (record slot order), so
+    # the latest index entries hold the latest rows: the records kept are the
+    # latest ones whose rows fit the 3000-row window (a record has at most
+    # ~5500 / 50 + 2 rows), a suffix of the last 40 index entries
     small = HBMRing(capacity_rows=3000, capacity_molecules=40, stride=STRIDE)
     engine.run(cb, n, xdist=xs, vdist=vs, seed=5, ring=small)
     n_rows, n_mol = small.counts()
@@ -95,6 +96,10 @@ def test_small_ring_keeps_the_latest_complete_records(engine):
     assert (n_rows, n_mol) == big.counts()
     kept = small.read()
     assert 0 < len(kept) <= 40
+    idx = small.index.cpu().numpy()
+    latest = [int(idx[e % 40][0]) for e in range(n_mol - 40, n_mol)]
+    assert [rec.molecule for rec in kept] == latest[40 - len(kept):]
+    assert sum(len(rec.rows) for rec in kept) <= 3000
     for rec in kept:
         np.testing.assert_array_equal(rec.rows, full[rec.molecule])
     # a second run appends after the first
