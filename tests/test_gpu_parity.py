@@ -78,6 +78,11 @@ def test_fp32_within_tolerance(engine, case):
     assert np.all(dtime[same] <= ttol[same]), dtime[same].max()
     # row counts agree except where rint(L/dz) sits on a rounding tie of vz
     assert np.mean(r.rows[same] == o["rows"][same]) > 0.999
+    # without per-molecule outputs the persistent pass defers the molecules'
+    # ends to k_lens_finish: the same counts and step totals
+    plain = engine.run(cb, n, precision=32, ics=fx["ics"])
+    np.testing.assert_array_equal(plain.counts, r.counts)
+    assert (plain.molecule_steps, plain.lens_steps) == (r.molecule_steps, r.lens_steps)
 
 
 @pytest.mark.parametrize("case", [c for c in CASES
@@ -350,3 +355,27 @@ def test_front_staging_overflow(engine):
         np.testing.assert_array_equal(batch[0].counts, ref.counts)
     finally:
         engine.set_tuning()
+
+
+def test_unusable_lens_step_count_raises(engine):
+    """A molecule entering a fixed-time-step lens with vz = 1e-9 m/s: rint(L /
+    dz) = 3e14 exceeds CTRAJ_MAX_LENS_STEPS, where the reference's step count
+    is unusable (electrostatic_lens.py:87-88).  The run finishes, credits the
+    molecule to the lens and raises OverflowError -- with and without
+    per-molecule outputs (molecule ends inside the pass or in k_lens_finish),
+    in both precisions, alone and beside a normal molecule."""
+    import ctraj
+    from ctraj.stark import hexapole_force
+
+    lens = ctraj.ElectrostaticLens(name="L", z0=0.0, L=0.3, d=0.02, V=30e3, dt=1e-6,
+                                   a_interp=hexapole_force(V=30e3, R=10e-3))
+    det = ctraj.CircularAperture(name="Det", z0=1.0, L=0.0, d=float("inf"))
+    cb = compile_beamline(ctraj.Beamline([lens, det]))
+    ics = np.array([[1e-3, 0.0], [0.0, 0.0], [0.0, 0.0], [0.0, 0.0], [0.0, 0.0], [1e-9, 184.0]])
+    for prec in (32, 64):
+        for outputs in (False, True):
+            for n in (1, 2):
+                with pytest.raises(OverflowError):
+                    engine.run(cb, n, precision=prec, ics=np.ascontiguousarray(ics[:, :n]), outputs=outputs)
+    ok = engine.run(cb, 1, precision=32, ics=np.ascontiguousarray(ics[:, 1:]))  # the normal one alone
+    assert ok.counter_dict().get("Detected", 0) == 1
