@@ -18,6 +18,8 @@ from ctraj.workloads import lens_beamline
 FD_REL = 1e-4       # adjoint vs central finite differences, h = 1e-4 relative
 FP64_REL = 1e-9     # CUDA FP64 vs torch FP64 (same arithmetic up to rounding order)
 FP32_REL = 1e-4     # CUDA FP32 adjoint vs the FP64 reference
+CKPT_REL = 3e-4     # FP32 gradients of two checkpoint intervals: the backward maps compose
+                    # over other segments, so their rounding differs (up to 1.2e-4 seen)
 V_TEST = 8e3        # lens voltage of the small cases: enough molecules pass to give a signal
 
 
@@ -195,7 +197,12 @@ def test_checkpoint_interval_does_not_change_the_gradient(engine):
         # the forward pass is the same; the backward maps compose over
         # different segments, so only rounding differs
         assert o.loss == outs[0].loss
-        assert rel_err(o.grad, outs[0].grad).max() < FP32_REL, (o.grad, outs[0].grad)
+        assert rel_err(o.grad, outs[0].grad).max() < CKPT_REL, (o.grad, outs[0].grad)
+    # in FP64 the intervals agree to rounding
+    o64 = [soft_transmission(problem(20_000, seed=5, checkpoint=k, precision=64), p0, engine=engine)
+           for k in (64, 17)]
+    assert o64[1].loss == o64[0].loss
+    assert rel_err(o64[1].grad, o64[0].grad).max() < FP64_REL, (o64[1].grad, o64[0].grad)
     again = soft_transmission(problem(50_000, seed=5, checkpoint=64), p0, engine=engine)
     np.testing.assert_array_equal(again.grad, outs[0].grad)  # deterministic
     # the forward-only call gives the same loss
