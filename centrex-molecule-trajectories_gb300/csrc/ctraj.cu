@@ -293,7 +293,7 @@ int enqueue_persistent(bool out, int mode, const Plan& P, const RunDev& R, int i
   CT_CUDA(cudaGetLastError());
   *launches += 4;
   if (done) {  // the molecules' ends, in full warps
-    finish_kernel(mode)<<<sms * 8, kFinishThreads, 0, s>>>(P, R, i, Qin, Qnext, done);
+    finish_kernel(mode)<<<sms * 8, kFinishThreads, 0, s>>>(P, R, i, Qin, Qnext, done, 0xFFFFFFFFu);
     CT_CUDA(cudaGetLastError());
     *launches += 1;
   }
@@ -583,6 +583,7 @@ int ctraj_destroy(ctraj_context* c) {
   c->ring_ent.release();
   c->lens_order.release();
   c->lens_done.release();
+  c->sweep_done.release();
   c->ring_part.release();
   c->sweep_order.release();
   if (c->sweep_exec) cudaGraphExecDestroy(c->sweep_exec);

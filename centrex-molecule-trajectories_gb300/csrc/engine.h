@@ -106,6 +106,7 @@ struct ctraj_context {
   ctraj::DevBuf lens_done;             // persistent lens pass: DoneRec per entrant (deferred ends)
   ctraj::DevBuf ring_part;             // ring recording: per-block row / entry sums and bases
   ctraj::DevBuf sweep_order;           // persistent sweep: per table bucket counts | entrant order
+  ctraj::DevBuf sweep_done;            // persistent sweep: per table DoneRec records (deferred ends)
   int chunk = 64;               // RK4 steps of the first lens chunk (compaction interval)
   int chunk_growth = 200;       // percent: each chunk's length relative to the previous
   int chunk_max = 1024;         // longest chunk
@@ -237,8 +238,9 @@ PersistKernel persist_kernel(bool out, int force, int mode, bool staged, int lan
 template <int F>  // one force law's configurations (k_persist_<law>.cu)
 PersistKernel persist_kernel_for(bool out, int mode, bool staged, int lanes, int mpt, int* threads, int* used_mpt);
 
-// k_lens_finish for a plain or batch pass (k_persist.cu).
-using FinishKernel = void (*)(const Plan, const RunDev, const int, const Queue, const Queue, const DoneRec*);
+// k_lens_finish for a plain, batch or sweep pass (k_persist.cu).
+using FinishKernel = void (*)(const Plan, const RunDev, const int, const Queue, const Queue, const DoneRec*,
+                              const unsigned);
 FinishKernel finish_kernel(int mode);
 constexpr size_t kDoneRecBytes = 64;
 

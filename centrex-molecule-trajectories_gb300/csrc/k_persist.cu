@@ -10,6 +10,7 @@ static_assert(sizeof(DoneRec) == kDoneRecBytes, "DoneRec layout");
 
 FinishKernel finish_kernel(int mode) {
   using M = Mol32<false, false>;
+  if (mode == kModeSweep) return k_lens_finish<M, kModeSweep>;
   return mode == kModeBatch ? k_lens_finish<M, kModeBatch> : k_lens_finish<M, kModePlain>;
 }
 

@@ -809,7 +809,8 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
                                              const int interval, const int service,
                                              const unsigned static_entries,
                                              const float4* s_tab, SwapSlot* s_swap, unsigned* s_wcount,
-                                             BlockTally& S, PersistAcc& acc, DoneRec* done = nullptr) {
+                                             BlockTally& S, PersistAcc& acc, DoneRec* done = nullptr,
+                                             const unsigned done_cap = 0xFFFFFFFFu) {
   constexpr bool kSweep = kMode == kModeSweep, kRing = kMode == kModeRing;
   const unsigned n_in = *(volatile unsigned*)Qin.count;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -895,13 +896,15 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
   // with `done`, only their state is written to their DoneRec and
   // k_lens_finish finishes them after the pass in full warps.
   auto finalize = [&](PersistSlot<M>& x) {
-    const bool fin = x.phase == kLost || x.phase == kExit || x.phase == kBad;
+    bool fin = x.phase == kLost || x.phase == kExit || x.phase == kBad;
     if (!__any_sync(kFull, fin)) return;
-    if constexpr (!kOut && (kMode == kModePlain || kMode == kModeBatch)) {
+    if constexpr (!kOut && (kMode == kModePlain || kMode == kModeBatch || kMode == kModeSweep)) {
       // a batch pass always defers (its host always passes `done`); a plain
-      // pass when given `done`
+      // pass or a sweep when given `done`, a sweep for the queue positions
+      // below done_cap (the records it has room for; the rest end here)
       if (kMode == kModeBatch || done) {
-        if (fin) {
+        const bool defer = fin && (kMode != kModeSweep || x.idx < done_cap);
+        if (defer) {
           int4* r = reinterpret_cast<int4*>(done + x.idx);
           r[0] = make_int4(__float_as_int(x.m.x), __float_as_int(x.m.y), __float_as_int(x.m.vx),
                            __float_as_int(x.m.vy));
@@ -913,7 +916,9 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
                            int(unsigned(x.phase) | (x.flags & 3u) << 3 | unsigned(x.n0) << 5));
           x.phase = kIdle;
         }
-        return;
+        if (kMode != kModeSweep) return;
+        fin = fin && !defer;
+        if (!__any_sync(kFull, fin)) return;
       }
     }
     if constexpr (kOut || kMode != kModeBatch) {
@@ -1076,20 +1081,21 @@ __global__ void __launch_bounds__(kT, 1) k_lens_persist(const __grid_constant__ 
 }
 
 // The deferred ends of a persistent pass's molecules (lens_finish), one
-// thread per queue position of Qin, in full warps, from the DoneRec records
-// the pass wrote (k_lens_persist with `done`; runs without per-molecule
-// outputs, plain or batch mode).  Grid-stride over the queue.
+// thread per queue position of Qin below `cap`, in full warps, from the
+// DoneRec records the pass wrote (k_lens_persist with `done`: runs without
+// per-molecule outputs, plain or batch mode; k_sweep_persist, per Stark
+// table).  Grid-stride over the queue.
 constexpr int kFinishThreads = 256;
 
 template <class M, int kMode>
 __global__ void __launch_bounds__(kFinishThreads) k_lens_finish(const __grid_constant__ Plan P, const RunDev R,
                                                                 const int li, const Queue Qin, const Queue Qnext,
-                                                                const DoneRec* done) {
+                                                                const DoneRec* done, const unsigned cap) {
   __shared__ BlockTally S;
   tally_init(S);
   __syncthreads();
   PersistAcc acc;
-  const unsigned n = *(volatile unsigned*)Qin.count;
+  const unsigned n = min(*(volatile unsigned*)Qin.count, cap);  // cap: the records written
   const unsigned stride = gridDim.x * blockDim.x;
   for (unsigned base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {  // warp-uniform
     const unsigned j = base + (threadIdx.x & 31);
@@ -1119,7 +1125,7 @@ __global__ void __launch_bounds__(kFinishThreads) k_lens_finish(const __grid_con
       flags = (unsigned(r3.w) >> 3) & 3u;
       n0 = int(unsigned(r3.w) >> 5);
       m.margin = INFINITY;
-      if (kMode == kModeBatch) cfg = Qin.cfg[j];
+      if (kMode != kModePlain) cfg = Qin.cfg[j];
     }
     // fresh = true: the exit-snap time comes from the record, not the queue
     lens_finish<M, false, kMode>(P, R, li, Qin, Qnext, fin, m, st, phase, flags, j, n0, true, cfg, S, acc);
@@ -1136,6 +1142,8 @@ struct SweepTabs {
   const unsigned* order[CTRAJ_MAX_TABLES];
   float s0[CTRAJ_MAX_TABLES];
   int n_int[CTRAJ_MAX_TABLES];
+  DoneRec* done[CTRAJ_MAX_TABLES];         // deferred molecule ends (nullptr: none)
+  unsigned done_cap[CTRAJ_MAX_TABLES];     // queue positions with a record
 };
 
 template <int F, bool kStaged>
@@ -1185,7 +1193,7 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_sweep_persist(const __gr
     L.n_smem = kStaged ? T.n_int[t] : 0;
     // no interleaved first entries: each CTA takes from its table's queue in order
     persist_pass<M, false, F, kStaged, kModeSweep>(P, R, li, Q, Q, L, T.order[t], interval, service, 0u, s_dyn,
-                                                  s_swap, s_wcount, S, acc);
+                                                  s_swap, s_wcount, S, acc, T.done[t], T.done_cap[t]);
   }
   persist_flush(S, R, P.n_labels, acc);
 }

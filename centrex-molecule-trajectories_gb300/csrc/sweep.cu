@@ -81,6 +81,8 @@ struct SweepLaunch {
   int force = kForceStark2;              // the lens's force law; kForceStark2Lin when every table
                                          // passes the linear form's test at its largest voltage
   unsigned* order[CTRAJ_MAX_TABLES] = {};  // persistent: bucket counts then entrant order, per table
+  DoneRec* done[CTRAJ_MAX_TABLES] = {};    // persistent: the molecules' end records, per table
+  unsigned done_cap[CTRAJ_MAX_TABLES] = {};
 };
 
 // The persistent sweep lens kernel of a force law; staged when every table fits.
@@ -147,12 +149,20 @@ int sweep_enqueue(ctraj_context* c, const Plan& P, const RunDev& R, const SweepL
       T.order[t] = hist + kOrderBuckets;
       T.s0[t] = W.la[t].s0;
       T.n_int[t] = W.la[t].n_int;
+      T.done[t] = W.done[t];
+      T.done_cap[t] = W.done_cap[t];
     }
     sweep_persist_kernel(W.force, sweep_staged(W))<<<c->sm_count, kPersistThreads,
                                                                   sweep_persist_smem(W), s>>>(
         P, R, W.lens, Qs, W.n_tab, T, W.la[0], c->lens_interval, c->lens_service);
     CT_CUDA(cudaGetLastError());
     ++launches;
+    for (int t = 0; t < W.n_tab; ++t) {  // the molecules' ends, in full warps
+      finish_kernel(kModeSweep)<<<c->sm_count * 8, kFinishThreads, 0, s>>>(P, R, W.lens, Qs.q[t], Qs.q[t],
+                                                                          W.done[t], W.done_cap[t]);
+      CT_CUDA(cudaGetLastError());
+      ++launches;
+    }
     if (c->timing) CT_CUDA(record(c->ev[3]));
     CT_CUDA(cudaMemcpyAsync(c->sweep_host, W.result, W.result_bytes, cudaMemcpyDeviceToHost, s));
     c->sweep_launches = launches;
@@ -303,6 +313,22 @@ extern "C" int ctraj_run_sweep(ctraj_context* c, const ctraj_sweep* sw, const ct
     for (int t = 0; t < W.n_tab; ++t) {
       W.order[t] = c->sweep_order.as<unsigned>() + off;
       off += kOrderBuckets + size_t(std::max<int64_t>(tab_n[t], 1));
+    }
+    // end records for the first eighth of each table's queue (at least 2^20
+    // positions): the lens entrants are a few percent of the molecules; the
+    // pass ends any molecule beyond that itself
+    size_t recs = 0, dcap[CTRAJ_MAX_TABLES];
+    for (int t = 0; t < W.n_tab; ++t) {
+      const size_t qcap = size_t(std::max<int64_t>(tab_n[t], 1));
+      dcap[t] = std::min(qcap, std::max<size_t>(size_t(1) << 20, qcap / 8));
+      recs += dcap[t];
+    }
+    if ((st = ens(c->sweep_done, recs * kDoneRecBytes))) return st;
+    size_t o = 0;
+    for (int t = 0; t < W.n_tab; ++t) {
+      W.done[t] = reinterpret_cast<DoneRec*>(c->sweep_done.as<char>() + o * kDoneRecBytes);
+      W.done_cap[t] = unsigned(dcap[t]);
+      o += dcap[t];
     }
   }
   for (int t = 0; t < W.n_tab; ++t) {
