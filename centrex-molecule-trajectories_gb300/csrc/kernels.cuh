@@ -229,24 +229,43 @@ __device__ __forceinline__ void ring_entry(const ctraj_ring& G, unsigned long lo
 // per warp on the queue's single counter.  The staging area holds
 // front_stage(threads) entries; a warp whose entrants do not all fit appends
 // the rest itself (queue_slot), so no warp waits for another before the end.
+//
+// Screening (FP32 runs without per-molecule outputs, device draws with a
+// Gaussian position, element 0 a circular or rectangular aperture): most
+// molecules of such a beamline are stopped at element 0's entrance plane by
+// their x alone, which the first of a molecule's two Philox calls decides
+// (Mol32::screened_out).  Those are tallied there; the others wait in a
+// per-warp buffer (index, vx, vy, vz, x) and are taken 32 at a time, in full
+// warps, for the second call and the walk -- the same results as the full
+// walk of every molecule, with the second call, a Box-Muller pair and the
+// walk's divergent work left out for the screened ones.
 template <class M>
 struct FrontEntry {
   M m;
   LensStep st;
 };
 
-__host__ __device__ constexpr unsigned front_stage(int threads) { return unsigned(threads + kFrontSlack); }
+struct ScreenSlot {
+  int32_t i;
+  float vx, vy, vz, x;
+};
+constexpr int kScreenSlots = 64;  // per warp: under 32 waiting plus one iteration's 32
+
+__host__ __device__ constexpr unsigned front_stage(int threads) { return unsigned(threads / 2 + kFrontSlack); }
 
 template <class M>
 __host__ __device__ constexpr size_t front_smem(int threads) {
-  return size_t(front_stage(threads)) * sizeof(FrontEntry<M>);
+  return size_t(front_stage(threads)) * sizeof(FrontEntry<M>) +
+         size_t(threads / 32) * kScreenSlots * sizeof(ScreenSlot);
 }
 
 template <class M, bool kOut, int kMode = kModePlain>
 __global__ void __launch_bounds__(kFrontMaxThreads) k_front(const __grid_constant__ Plan P, const RunDev R,
                                                     const Queue Q) {
-  extern __shared__ unsigned char s_front[];
+  extern __shared__ __align__(16) unsigned char s_front[];
   FrontEntry<M>* stage = reinterpret_cast<FrontEntry<M>*>(s_front);
+  ScreenSlot* scr = reinterpret_cast<ScreenSlot*>(s_front + size_t(front_stage(blockDim.x)) * sizeof(FrontEntry<M>)) +
+                    (threadIdx.x >> 5) * kScreenSlots;
   __shared__ BlockTally S;
   __shared__ unsigned s_n, s_base, s_max;
   tally_init(S);
@@ -265,14 +284,14 @@ __global__ void __launch_bounds__(kFrontMaxThreads) k_front(const __grid_constan
     if (kMode == kModeBatch) Q.cfg[slot] = R.run_tag;
   };
   unsigned long long steps = 0, band = 0, bad = 0;
-  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
-  for (int64_t base = int64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31); base < R.n; base += stride) {
-    const int64_t i = base + lane;
+  // molecule i of this lane (i < 0: none; ready: m already drawn) through
+  // the walk, the staging of lens entrants and the tally; all lanes of the
+  // warp call it together
+  auto one = [&](const int64_t i, M& m, const bool ready) {
     int label = kNone;
-    M m;
     LensStep st;
-    if (i < R.n) {
-      m.init(P, R, i);
+    if (i >= 0) {
+      if (!ready) m.init(P, R, i);
       int lens_at = -1;
       label = walk(m, P, 0, &lens_at);
       if (label == kQueued && !enter_lens_front(m, P, lens_at, st)) {
@@ -317,6 +336,66 @@ __global__ void __launch_bounds__(kFrontMaxThreads) k_front(const __grid_constan
       }
     }
     tally_warp(S, label, P.n_labels);
+  };
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  const int64_t first = int64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31);  // warp-uniform loops
+  bool screen = false;
+  if constexpr (M::kScreenable) {
+    const ctraj_element& e0 = P.el[0];
+    screen = R.ic_mode == CTRAJ_IC_DEVICE_DRAW && R.xd.kind != CTRAJ_DIST_DISC_POSITION &&
+             isfinite(float(R.xd.p[1])) && P.n_el > 0 &&
+             (e0.type == CTRAJ_CIRCULAR_APERTURE || e0.type == CTRAJ_RECTANGULAR_APERTURE);
+  }
+  if (screen) {
+    if constexpr (M::kScreenable) {
+      int waiting = 0;  // warp-uniform: molecules in this warp's buffer
+      // the last k waiting molecules, one per lane, through the walk
+      auto take = [&](const int k) {
+        M m;
+        int64_t i = -1;
+        if (lane < k) {
+          const ScreenSlot e = scr[waiting - k + lane];
+          i = e.i;
+          m.vx = e.vx;
+          m.vy = e.vy;
+          m.vz = e.vz;
+          m.x = e.x;
+          m.screen_rest(P, R, i);
+        }
+        __syncwarp();
+        waiting -= k;
+        one(i, m, true);
+      };
+      const int label0 = P.el[0].label;
+      for (int64_t base = first; base < R.n; base += stride) {
+        const int64_t i = base + lane;
+        M m;
+        bool wait = false;
+        int label = kNone;
+        if (i < R.n) {
+          m.screen_draw(R, i);
+          if (m.screened_out(P, R.gap0f)) {
+            label = label0;
+            steps += 1;  // the walk's one row: the flight to element 0
+          } else {
+            wait = true;
+          }
+        }
+        const unsigned wm = __ballot_sync(kFull, wait);
+        if (wait) scr[waiting + __popc(wm & lanes_lt)] = ScreenSlot{int32_t(i), m.vx, m.vy, m.vz, m.x};
+        waiting += __popc(wm);
+        tally_warp(S, label, P.n_labels);
+        __syncwarp();
+        if (waiting >= 32) take(32);
+      }
+      while (waiting > 0) take(min(waiting, 32));
+    }
+  } else {
+    for (int64_t base = first; base < R.n; base += stride) {
+      const int64_t i = base + lane;
+      M m;
+      one(i < R.n ? i : -1, m, false);
+    }
   }
   // the staged entrants to the queue
   __syncthreads();

@@ -372,6 +372,7 @@ struct RowSink {
 // ===========================================================================
 template <bool kRec>
 struct Mol64 {
+  static constexpr bool kScreenable = false;  // the front's screening is FP32's (Mol32)
   double x[3], v[3], a[3], t;
   double margin;
   int rows;
@@ -644,6 +645,53 @@ struct Mol32 {
     ay = -P.gf;
     if (kOut || kRec) zc = z_ic;
     if (kRec) sink->write(x, y, zc, vx, vy, vz, ax, ay, 0.0, t);
+  }
+
+  // The device draw of init in two parts, for the front's screening of
+  // element 0 (FP32 runs without per-molecule outputs, Gaussian positions):
+  // screen_draw: the first Philox call's words, vx, vy, vz and x exactly as
+  // init draws them; screen_rest: the second call (y) and the rest of init.
+  static constexpr bool kScreenable = !kOut && !kRec;
+  __device__ void screen_draw(const RunDev& R, int64_t i) {
+    const Philox4 a = philox4x32_10(R.offset + uint64_t(i), 0u, R.key);
+    float n0, n1, n2, n3;
+    box_muller(a.v[0], a.v[1], n0, n1);
+    box_muller(a.v[2], a.v[3], n2, n3);
+    const double* vp = R.vd.p;
+    vx = __fmaf_rn(float(vp[1]), n0, float(vp[0]));
+    vy = __fmaf_rn(float(vp[3]), n1, float(vp[2]));
+    vz = __fmaf_rn(float(vp[5]), n2, float(vp[4]));
+    x = __fmul_rn(float(R.xd.p[0]), n3);
+  }
+  __device__ void screen_rest(const Plan& P, const RunDev& R, int64_t i) {
+    const Philox4 b = philox4x32_10(R.offset + uint64_t(i), 1u, R.key);
+    float n4, n5;
+    box_muller(b.v[0], b.v[1], n4, n5);
+    y = __fmul_rn(float(R.xd.p[1]), n4);
+    id = int32_t(i);
+    margin = INFINITY;
+    rows = 0;
+    gap0 = R.gap0f;
+    inv_vz = __frcp_rn(vz);
+    t = 0.0f;
+    ax = 0.0f;
+    ay = -P.gf;
+  }
+  // True when the walk would stop this molecule (vx, vz, x from screen_draw)
+  // at the entrance plane of element 0, a circular or rectangular aperture,
+  // whatever its y: after the flight x' = fma(0, h, fma(vx, dt, x)) of the
+  // walk, x'^2 > R^2 makes fma(y', y', x'^2) > R^2 for every finite y' (the
+  // rounding is monotone), and x' outside (x1, x2) fails the rectangle.  y'
+  // is finite when h, vy dt and g h are (y itself is finite, its sigma
+  // being so: the caller checks); otherwise the molecule is not screened.
+  // The molecule then has the walk's one trajectory row.
+  __device__ bool screened_out(const Plan& P, const float gap0f) const {
+    const float dt = __fmul_rn(gap0f, __frcp_rn(vz));  // the walk's first flight (fly, element 0)
+    const float h = __fmul_rn(__fmul_rn(0.5f, dt), dt);
+    if (!(isfinite(h) && fabsf(__fmul_rn(vy, dt)) < 1e30f && fabsf(__fmul_rn(P.gf, h)) < 1e30f)) return false;
+    const float xe = __fmaf_rn(0.0f, h, __fmaf_rn(vx, dt, x));
+    const float* c = P.ef[0].c;
+    return P.el[0].type == CTRAJ_CIRCULAR_APERTURE ? __fmul_rn(xe, xe) > c[0] : !(c[0] < xe && xe < c[1]);
   }
 
   // ballistic flight of dt with stored acceleration (ax, ay); afterwards a = (0, -g)

@@ -379,3 +379,37 @@ def test_unusable_lens_step_count_raises(engine):
                     engine.run(cb, n, precision=prec, ics=np.ascontiguousarray(ics[:, :n]), outputs=outputs)
     ok = engine.run(cb, 1, precision=32, ics=np.ascontiguousarray(ics[:, 1:]))  # the normal one alone
     assert ok.counter_dict().get("Detected", 0) == 1
+
+
+@pytest.mark.parametrize("first", ["circle", "rectangle", "lens"])
+def test_front_screening_matches_the_full_walk(engine, first):
+    """Runs without per-molecule outputs screen molecules at element 0 (a
+    circular or rectangular aperture) on their x alone, from the first Philox
+    call; runs with outputs walk every molecule.  Both must give the same
+    counts and step totals for every seed and offset, including a first
+    aperture a beam mostly misses, one it mostly passes, and no aperture at
+    all (no screening)."""
+    import ctraj
+    from ctraj.distributions import device_spec
+    from ctraj.workloads import lens_beamline, source
+
+    if first == "circle":
+        bl = lens_beamline()
+    elif first == "rectangle":
+        rect = ctraj.RectangularAperture(name="R0", z0=0.30, L=1e-3, w=10e-3, h=8e-3)
+        base = lens_beamline().elements
+        bl = ctraj.Beamline([rect] + [e for e in base if e.name != "A1"])
+    else:
+        bl = ctraj.Beamline([e for e in lens_beamline().elements if e.name != "A1"])
+    cb = compile_beamline(bl)
+    xd, vd = (device_spec(d, r) for d, r in zip(source(), ("position", "velocity")))
+    for seed, offset, n in ((3, 0, 300_000), (4, 12_345, 100_001), (5, 7, 33)):
+        full = engine.run(cb, n, xdist=xd, vdist=vd, seed=seed, offset=offset, outputs=True)
+        fast = engine.run(cb, n, xdist=xd, vdist=vd, seed=seed, offset=offset)
+        np.testing.assert_array_equal(fast.counts, full.counts)
+        assert (fast.molecule_steps, fast.lens_steps) == (full.molecule_steps, full.lens_steps)
+    narrow = device_spec(ctraj.CeNTREXVelocityDistribution(sigmax=1.0, sigmay=1.0), "velocity")
+    full = engine.run(cb, 200_000, xdist=xd, vdist=narrow, seed=9, outputs=True)
+    fast = engine.run(cb, 200_000, xdist=xd, vdist=narrow, seed=9)
+    np.testing.assert_array_equal(fast.counts, full.counts)
+    assert fast.molecule_steps == full.molecule_steps
