@@ -424,21 +424,25 @@ template <class M>
 __global__ void __launch_bounds__(kFrontMaxThreads) k_sweep_front(const __grid_constant__ Plan P, const RunDev R,
                                                           const __grid_constant__ SweepQueues Qs,
                                                           const int n_tables) {
+  // the screening buffers of k_front (one per warp), with the configuration
+  extern __shared__ __align__(16) unsigned char s_sweep[];
+  ScreenSlot* scr = reinterpret_cast<ScreenSlot*>(s_sweep) + (threadIdx.x >> 5) * kScreenSlots;
+  int* scr_cfg = reinterpret_cast<int*>(s_sweep + size_t(blockDim.x / 32) * kScreenSlots * sizeof(ScreenSlot)) +
+                 (threadIdx.x >> 5) * kScreenSlots;
   __shared__ BlockTally S;
   tally_init(S);
   __syncthreads();
   const int lane = threadIdx.x & 31;
+  const unsigned lanes_lt = (1u << lane) - 1u;
   unsigned long long steps = 0, bad = 0;
-  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
-  for (int64_t base = int64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31); base < R.n; base += stride) {
-    const int64_t i = base + lane;
-    int label = kNone, cfg = 0, tab = -1;
-    M m;
+  // molecule i (configuration cfg) of this lane through the walk, its Stark
+  // table's lens queue and the tallies (i < 0: none; ready: m already drawn)
+  auto one = [&](const int64_t i, const int cfg, M& m, const bool ready) {
+    int label = kNone, tab = -1;
     LensStep st;
-    if (i < R.n) {
-      cfg = find_cfg(R, i);
+    if (i >= 0) {
       tab = __ldg(R.cfg_table + cfg);
-      m.init(P, R, i);
+      if (!ready) m.init(P, R, i);
       int lens_at = -1;
       label = walk(m, P, 0, &lens_at);
       if (label == kQueued && !enter_lens_front(m, P, lens_at, st)) {
@@ -450,10 +454,82 @@ __global__ void __launch_bounds__(kFrontMaxThreads) k_sweep_front(const __grid_c
     for (int t = 0; t < n_tables; ++t) push_lens<kTagCarry>(Qs.q[t], label == kQueued && tab == t, m, st, cfg);
     tally_warp(S, label, P.n_labels);
     tally_cfg(R, cfg, label, P.n_labels);
+  };
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  const int64_t first = int64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31);  // warp-uniform loops
+  bool screen = false;
+  if constexpr (M::kScreenable) {
+    const ctraj_element& e0 = P.el[0];
+    screen = R.ic_mode == CTRAJ_IC_DEVICE_DRAW && R.xd.kind != CTRAJ_DIST_DISC_POSITION &&
+             isfinite(float(R.xd.p[1])) && P.n_el > 0 &&
+             (e0.type == CTRAJ_CIRCULAR_APERTURE || e0.type == CTRAJ_RECTANGULAR_APERTURE);
+  }
+  if (screen) {
+    if constexpr (M::kScreenable) {
+      int waiting = 0;  // warp-uniform
+      auto take = [&](const int k) {  // the last k waiting molecules, one per lane
+        M m;
+        int64_t i = -1;
+        int cfg = 0;
+        if (lane < k) {
+          const ScreenSlot e = scr[waiting - k + lane];
+          cfg = scr_cfg[waiting - k + lane];
+          i = e.i;
+          m.vx = e.vx;
+          m.vy = e.vy;
+          m.vz = e.vz;
+          m.x = e.x;
+          m.screen_rest(P, R, i);
+        }
+        __syncwarp();
+        waiting -= k;
+        one(i, cfg, m, true);
+      };
+      const int label0 = P.el[0].label;
+      for (int64_t base = first; base < R.n; base += stride) {
+        const int64_t i = base + lane;
+        M m;
+        bool wait = false;
+        int label = kNone, cfg = 0;
+        if (i < R.n) {
+          cfg = find_cfg(R, i);
+          m.screen_draw(R, i);
+          if (m.screened_out(P, R.gap0f)) {
+            label = label0;
+            steps += 1;  // the walk's one row: the flight to element 0
+          } else {
+            wait = true;
+          }
+        }
+        const unsigned wm = __ballot_sync(kFull, wait);
+        if (wait) {
+          const int at = waiting + __popc(wm & lanes_lt);
+          scr[at] = ScreenSlot{int32_t(i), m.vx, m.vy, m.vz, m.x};
+          scr_cfg[at] = cfg;
+        }
+        waiting += __popc(wm);
+        tally_warp(S, label, P.n_labels);
+        tally_cfg(R, cfg, label, P.n_labels);
+        __syncwarp();
+        if (waiting >= 32) take(32);
+      }
+      while (waiting > 0) take(min(waiting, 32));
+    }
+  } else {
+    for (int64_t base = first; base < R.n; base += stride) {
+      const int64_t i = base + lane;
+      M m;
+      one(i < R.n ? i : -1, i < R.n ? find_cfg(R, i) : 0, m, false);
+    }
   }
   stat_add(S, kStatSteps, steps);
   stat_add(S, kStatBadSteps, bad);
   tally_flush(S, R, P.n_labels);
+}
+
+// Dynamic shared memory of k_sweep_front (the screening buffers).
+__host__ __device__ constexpr size_t sweep_front_smem(int threads) {
+  return size_t(threads / 32) * kScreenSlots * (sizeof(ScreenSlot) + sizeof(int));
 }
 
 // ---------------------------------------------------------------------------

@@ -123,12 +123,13 @@ int sweep_enqueue(ctraj_context* c, const Plan& P, const RunDev& R, const SweepL
   if (R.n > 0) {
     auto kf = k_sweep_front<Mol32<false, false>>;
     const int ft = c->front_threads;
-    const int bps = blocks_per_sm(kf, ft, 0);
+    const size_t fsmem = sweep_front_smem(ft);  // its size limit is set before any capture (below)
+    const int bps = blocks_per_sm(kf, ft, fsmem);
     const int64_t want = (R.n + ft - 1) / ft;
     const int grid = int(std::min<int64_t>(want, int64_t(bps) * c->sm_count * c->front_waves));
     SweepQueues Qs{};
     for (int t = 0; t < W.n_tab; ++t) Qs.q[t] = W.qa[t];
-    kf<<<grid, ft, 0, s>>>(P, R, Qs, W.n_tab);
+    kf<<<grid, ft, fsmem, s>>>(P, R, Qs, W.n_tab);
     CT_CUDA(cudaGetLastError());
     ++launches;
   }
@@ -461,6 +462,8 @@ extern "C" int ctraj_run_sweep(ctraj_context* c, const ctraj_sweep* sw, const ct
   if (W.persistent)
     CT_CUDA(cudaFuncSetAttribute(sweep_persist_kernel(W.force, sweep_staged(W)),
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(sweep_persist_smem(W))));
+  CT_CUDA(cudaFuncSetAttribute(k_sweep_front<Mol32<false, false>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               int(sweep_front_smem(kFrontMaxThreads))));
   c->timing = timing;
   if (sw->use_graph) {
     if (!c->sweep_exec) {
