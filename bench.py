@@ -94,7 +94,7 @@ WORKLOAD = ("lens beamline: aperture r=6mm@0.30m, hexapole lens z0=0.80m L=0.60m
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=40)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--molecules", type=float, default=1e7)

@@ -50,7 +50,7 @@ def axes():
             [dict(front_threads=ft) for ft in (128, 256, 512)]]
 
 
-BATCH_GROUPS = (1, 2, 4, 8, 10, 16)
+BATCH_GROUPS = (1, 2, 4, 8, 10, 16, 20, 32)
 BATCH_LENS_THREADS = (512, 768, 1024)
 BATCH_SERVICE = (32, 64, 128, 256)
 
