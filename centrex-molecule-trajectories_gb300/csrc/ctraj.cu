@@ -108,6 +108,7 @@ int build_lens_tables(ctraj_context* c) {
   c->lens_offset.assign(n_el, 0);
   c->lens_n_int.assign(n_el, 0);
   c->lens_n_smem.assign(n_el, 0);
+  c->lens_outward.assign(n_el, 0);
   std::vector<float4> host;
   for (int i = 0; i < n_el; ++i) {
     const ctraj_element& e = c->elements[i];
@@ -142,6 +143,23 @@ int build_lens_tables(ctraj_context* c) {
           host.push_back(make_float4(float(qa), float(qb), float(qc), 0.f));
         }
       }
+    }
+    // a Stark table whose w >= 0 at every piece's ends (the linear form) or
+    // interval's ends (the quadratic), up to 1e-5 of its largest |w| (the
+    // spline's wiggle at |E| = 0), pushes molecules outward: the lens
+    // defocuses, which the entrant order uses
+    if (t.kind != CTRAJ_TABLE_RADIAL_LINEAR) {
+      float wmax = 0.f;
+      for (size_t k = c->lens_offset[i]; k < host.size(); ++k)
+        wmax = std::max(wmax, std::max(std::fabs(host[k].x), std::fabs(host[k].z)));
+      const float tol = -1e-5f * wmax;
+      bool out = true;
+      for (size_t k = c->lens_offset[i]; k < host.size() && out; ++k) {
+        const float4 q = host[k];
+        out = lin ? (q.x >= tol && q.x + q.y >= tol && q.z >= tol && q.z + q.w >= tol)
+                  : (q.x >= tol && q.x + q.y + q.z >= tol);
+      }
+      c->lens_outward[i] = out ? 1 : 0;
     }
     // the whole table goes to shared memory when it takes at most 96 KiB
     // (128 KiB in the linear form)
@@ -225,6 +243,7 @@ int build_plan(ctraj_context* c, const ctraj_run_args* a, Plan& P) {
       L.q = c->lens_tables.as<float4>(c->lens_offset[i] * sizeof(float4));
       L.n_int = c->lens_n_int[i];
       L.n_smem = c->lens_n_smem[i];
+      L.outward = c->lens_outward[i];
       L.force = lens_force_kind(c, e);
       if (t.kind == CTRAJ_TABLE_RADIAL_LINEAR) {
         L.beta = float(1.0 / h);
@@ -286,9 +305,9 @@ int enqueue_persistent(bool out, int mode, const Plan& P, const RunDev& R, int i
   unsigned* hist = order_buf;
   unsigned* order = hist + kOrderBuckets;
   CT_CUDA(cudaMemsetAsync(hist, 0, kOrderBuckets * sizeof(unsigned), s));
-  k_order_count<<<sms, kOrderThreads, 0, s>>>(P, i, Qin, hist);
+  k_order_count<<<sms, kOrderThreads, 0, s>>>(P, i, Qin, hist, P.lf[i].outward);
   k_order_scan<<<1, kOrderBuckets, 0, s>>>(hist);
-  k_order_place<<<sms, kOrderThreads, 0, s>>>(P, i, Qin, hist, order);
+  k_order_place<<<sms, kOrderThreads, 0, s>>>(P, i, Qin, hist, order, P.lf[i].outward);
   k<<<sms, kt, smem, s>>>(P, R, i, Qin, Qnext, lens_args(P, i, true), order, interval, service, done);
   CT_CUDA(cudaGetLastError());
   *launches += 4;

@@ -91,6 +91,7 @@ struct ctraj_context {
   bool lens_tables_dirty = true;
   std::vector<size_t> lens_offset;
   std::vector<int> lens_n_int, lens_n_smem;
+  std::vector<int> lens_outward;     // per lens: its FP32 force points away from the axis everywhere
   ctraj::DevBuf queue[3];              // lens queues: current chunk, continuation, next lens
   ctraj::DevBuf qctl;                  // queue counters (2 x unsigned per queue) + counts + stats
   ctraj::DevBuf ics;

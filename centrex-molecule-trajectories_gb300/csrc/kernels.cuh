@@ -715,10 +715,25 @@ __global__ void __launch_bounds__(kLensThreads, 2) k_lens_chunk(const __grid_con
 // result: molecules are independent and tallies are integer sums.
 constexpr int kOrderBuckets = 1024;
 
-// bucket 0 = most steps, for a queue whose largest step count is max_steps
-__device__ __forceinline__ int order_bucket(const ctraj_element& e, float vz, float scale) {
+// bucket 0 = most steps, for a queue whose largest step count is max_steps.
+// outward (a lens whose force points away from the axis everywhere, the
+// defocused high-field seekers): such a lens loses a molecule no later than
+// free flight would carry it to the bore radius R, so its steps are at most
+// t vz / dz with |(x, y) + (vx, vy) t| = R -- the molecules the lens loses
+// early go last, and those that cross it first, whatever their speed.  The
+// key only orders the work; it changes no result.
+__device__ __forceinline__ int order_bucket(const ctraj_element& e, const Queue& Q, const unsigned j,
+                                            const float scale, const int outward) {
+  const float vz = Q.vz[j];
   const float dz = e.step_mode == CTRAJ_STEP_DT ? fabsf(vz) * float(e.p[2]) : float(e.p[1]);
-  const float u = float(kOrderBuckets - 1) - (float(e.p[7]) / dz) * scale;  // NaN, -inf -> 0
+  float steps = float(e.p[7]) / dz;
+  if (outward) {
+    const float x = Q.x[j], y = Q.y[j], vx = Q.vx[j], vy = Q.vy[j], R = 0.5f * float(e.p[0]);
+    const float a = vx * vx + vy * vy, b = x * vx + y * vy, c = x * x + y * y - R * R;
+    const float t = (sqrtf(fmaxf(b * b - a * c, 0.0f)) - b) / a;  // a = 0: inf or NaN, no bound
+    steps = fminf(steps, t * fabsf(vz) / dz);
+  }
+  const float u = float(kOrderBuckets - 1) - steps * scale;  // NaN, -inf -> 0
   return u > 0.0f ? (u < float(kOrderBuckets - 1) ? int(u) : kOrderBuckets - 1) : 0;
 }
 
@@ -738,7 +753,7 @@ __device__ __forceinline__ void order_range(unsigned n, unsigned& lo, unsigned& 
 }
 
 static __global__ void __launch_bounds__(kOrderThreads) k_order_count(const __grid_constant__ Plan P, const int li,
-                                                               const Queue Q, unsigned* hist) {
+                                                               const Queue Q, unsigned* hist, const int outward) {
   __shared__ unsigned h[kOrderBuckets];
   for (int b = threadIdx.x; b < kOrderBuckets; b += blockDim.x) h[b] = 0;
   __syncthreads();
@@ -746,7 +761,7 @@ static __global__ void __launch_bounds__(kOrderThreads) k_order_count(const __gr
   unsigned lo, hi;
   order_range(*Q.count, lo, hi);
   for (unsigned j = lo + threadIdx.x; j < hi; j += blockDim.x)
-    atomicAdd(h + order_bucket(P.el[li], Q.vz[j], scale), 1u);
+    atomicAdd(h + order_bucket(P.el[li], Q, j, scale, outward), 1u);
   __syncthreads();
   for (int b = threadIdx.x; b < kOrderBuckets; b += blockDim.x)
     if (h[b]) atomicAdd(hist + b, h[b]);
@@ -771,7 +786,8 @@ static __global__ void __launch_bounds__(kOrderBuckets) k_order_scan(unsigned* h
 // bucket with one global atomic per bucket, then places them with
 // shared-memory atomics.
 static __global__ void __launch_bounds__(kOrderThreads) k_order_place(const __grid_constant__ Plan P, const int li,
-                                                               const Queue Q, unsigned* cursor, unsigned* order) {
+                                                               const Queue Q, unsigned* cursor, unsigned* order,
+                                                               const int outward) {
   __shared__ unsigned h[kOrderBuckets];
   for (int b = threadIdx.x; b < kOrderBuckets; b += blockDim.x) h[b] = 0;
   __syncthreads();
@@ -779,13 +795,13 @@ static __global__ void __launch_bounds__(kOrderThreads) k_order_place(const __gr
   unsigned lo, hi;
   order_range(*Q.count, lo, hi);
   for (unsigned j = lo + threadIdx.x; j < hi; j += blockDim.x)
-    atomicAdd(h + order_bucket(P.el[li], Q.vz[j], scale), 1u);
+    atomicAdd(h + order_bucket(P.el[li], Q, j, scale, outward), 1u);
   __syncthreads();
   for (int b = threadIdx.x; b < kOrderBuckets; b += blockDim.x)
     h[b] = h[b] ? atomicAdd(cursor + b, h[b]) : 0u;
   __syncthreads();
   for (unsigned j = lo + threadIdx.x; j < hi; j += blockDim.x)
-    order[atomicAdd(h + order_bucket(P.el[li], Q.vz[j], scale), 1u)] = j;
+    order[atomicAdd(h + order_bucket(P.el[li], Q, j, scale, outward), 1u)] = j;
 }
 
 // ---------------------------------------------------------------------------

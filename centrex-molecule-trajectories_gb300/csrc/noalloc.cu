@@ -214,6 +214,7 @@ int noalloc_plan(const ctraj_element* el, int n_el, int n_labels, const ctraj_fo
     L.q = dev_tables + offset;
     L.n_int = entries;
     L.n_smem = entries <= (lin ? kMaxStagedLinear : kMaxStagedIntervals) ? entries : 0;
+    L.outward = 0;  // entrants ordered by step count alone
     if (t.kind == CTRAJ_TABLE_RADIAL_LINEAR) {
       L.force = kForceRadial;
       L.beta = float(1.0 / h);

@@ -44,6 +44,7 @@ struct LensF {
   int n_smem;       // leading intervals staged in shared memory
   int force;        // kForce*
   int cols;         // honeycomb: q = cell centres (x, y, 0, 0), n_int = cells, cols = cells per row
+  int outward;      // stark: w >= 0 over the whole table, the force points away from the axis
 };
 
 // The FP32 constants of the one lens a k_lens_chunk launch integrates, passed

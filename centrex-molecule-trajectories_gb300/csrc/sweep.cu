@@ -141,9 +141,10 @@ int sweep_enqueue(ctraj_context* c, const Plan& P, const RunDev& R, const SweepL
       Qs.q[t] = W.qa[t];
       unsigned* hist = W.order[t];
       CT_CUDA(cudaMemsetAsync(hist, 0, kOrderBuckets * sizeof(unsigned), s));
-      k_order_count<<<c->sm_count, kOrderThreads, 0, s>>>(P, W.lens, W.qa[t], hist);
+      // ordered by step count alone: a configuration's force has its own scale
+      k_order_count<<<c->sm_count, kOrderThreads, 0, s>>>(P, W.lens, W.qa[t], hist, 0);
       k_order_scan<<<1, kOrderBuckets, 0, s>>>(hist);
-      k_order_place<<<c->sm_count, kOrderThreads, 0, s>>>(P, W.lens, W.qa[t], hist, hist + kOrderBuckets);
+      k_order_place<<<c->sm_count, kOrderThreads, 0, s>>>(P, W.lens, W.qa[t], hist, hist + kOrderBuckets, 0);
       CT_CUDA(cudaGetLastError());
       launches += 3;
       T.q[t] = W.la[t].q;
