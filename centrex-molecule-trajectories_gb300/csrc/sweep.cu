@@ -83,6 +83,7 @@ struct SweepLaunch {
   unsigned* order[CTRAJ_MAX_TABLES] = {};  // persistent: bucket counts then entrant order, per table
   DoneRec* done[CTRAJ_MAX_TABLES] = {};    // persistent: the molecules' end records, per table
   unsigned done_cap[CTRAJ_MAX_TABLES] = {};
+  int outward = 0;                         // every configuration's force points away from the axis
 };
 
 // The persistent sweep lens kernel of a force law; staged when every table fits.
@@ -141,10 +142,10 @@ int sweep_enqueue(ctraj_context* c, const Plan& P, const RunDev& R, const SweepL
       Qs.q[t] = W.qa[t];
       unsigned* hist = W.order[t];
       CT_CUDA(cudaMemsetAsync(hist, 0, kOrderBuckets * sizeof(unsigned), s));
-      // ordered by step count alone: a configuration's force has its own scale
-      k_order_count<<<c->sm_count, kOrderThreads, 0, s>>>(P, W.lens, W.qa[t], hist, 0);
+      k_order_count<<<c->sm_count, kOrderThreads, 0, s>>>(P, W.lens, W.qa[t], hist, W.outward);
       k_order_scan<<<1, kOrderBuckets, 0, s>>>(hist);
-      k_order_place<<<c->sm_count, kOrderThreads, 0, s>>>(P, W.lens, W.qa[t], hist, hist + kOrderBuckets, 0);
+      k_order_place<<<c->sm_count, kOrderThreads, 0, s>>>(P, W.lens, W.qa[t], hist, hist + kOrderBuckets,
+                                                          W.outward);
       CT_CUDA(cudaGetLastError());
       launches += 3;
       T.q[t] = W.la[t].q;
@@ -285,6 +286,26 @@ extern "C" int ctraj_run_sweep(ctraj_context* c, const ctraj_sweep* sw, const ct
       lin = stark_linear(ht.kind, ht.n, ht.knots.data(), ht.coef.data(), ex);
     }
     if (lin) W.force = kForceStark2Lin;
+    // the force kappa_c W'(E) (kappa_c = -2 alpha_c / m) points away from the
+    // axis for every configuration when no alpha_c is negative and every
+    // table's slope W'(E) <= 0 (at its intervals' quarter points, up to 1e-5
+    // of its largest): the entrant order then bounds steps by free flight
+    bool out = true;
+    for (int k = 0; k < n_cfg && out; ++k) out = sw->alpha[k] >= 0.0;
+    for (int t = 0; t < W.n_tab && out; ++t) {
+      const HostTable& ht = c->tables[tab_id[t]];
+      const double h = (ht.knots[ht.n - 1] - ht.knots[0]) / double(ht.n - 1);
+      double wmax = 0.0;
+      for (int j = 0; j < ht.n - 1; ++j) wmax = std::max(wmax, std::fabs(ht.coef[size_t(j) * 4 + 2]));
+      for (int j = 0; j < ht.n - 1 && out; ++j) {
+        const double* cj = &ht.coef[size_t(j) * 4];
+        for (int q = 0; q <= 4 && out; ++q) {
+          const double u = 0.25 * q;
+          out = cj[2] + u * (2.0 * cj[1] * h + u * 3.0 * cj[0] * h * h) <= 1e-5 * wmax;
+        }
+      }
+    }
+    W.outward = out ? 1 : 0;
   }
   const bool lin = W.force == kForceStark2Lin;
   const double piece_scale = lin ? double(kLinearPieces) : 1.0;  // table coordinate units per knot interval
@@ -407,6 +428,7 @@ extern "C" int ctraj_run_sweep(ctraj_context* c, const ctraj_sweep* sw, const ct
   put(&c->lens_service, sizeof c->lens_service);
   put(&c->front_threads, sizeof c->front_threads);
   put(&W.force, sizeof W.force);
+  put(&W.outward, sizeof W.outward);
   const bool same = key == c->sweep_key;
   cudaStream_t s = c->stream;
   if (!same) {
