@@ -120,6 +120,8 @@ def parse():
     p.add_argument("--front-threads", type=int, default=128, help="--profile: threads per front block")
     p.add_argument("--batch-lens-threads", type=int, default=1024,
                    help="--profile batch: threads per CTA of the shared lens pass")
+    p.add_argument("--lens-interval", type=int, default=256,
+                   help="--profile: RK4 steps between the persistent pass's compactions once its queue is empty")
     return p.parse_args()
 
 
@@ -137,7 +139,8 @@ def run_profile(args):
     xs, vs = device_spec(xd, "position"), device_spec(vd, "velocity")
     eng = Engine(0)
     eng.set_tuning(lens_mode=0 if args.lens_mode == "persistent" else 1, batch_group=args.batch_group,
-                   front_threads=args.front_threads, batch_lens_threads=args.batch_lens_threads)
+                   front_threads=args.front_threads, batch_lens_threads=args.batch_lens_threads,
+                   lens_interval=args.lens_interval)
     n = int(args.molecules)
     for k in range(args.steps):
         if args.profile == "sweep":
