@@ -95,22 +95,37 @@ __device__ __forceinline__ double log1p_(double a) { return log1p(a); }
 __device__ __forceinline__ unsigned to_uint_rz(float a) { return __float2uint_rz(a); }
 __device__ __forceinline__ unsigned to_uint_rz(double a) { return __double2uint_rz(a); }
 
-// log sigma(z) and sigma(-z) = d log sigma(z) / dz
+// log sigma(z) and sigma(-z) = d log sigma(z) / dz.  With e = exp(-|z|) in
+// (0, 1]: log sigma(z) = -log(1 + e) for z >= 0 and z - log(1 + e) below;
+// sigma(-z) = e / (1 + e) for z >= 0 and 1 / (1 + e) below.
+// FP32 without a branch, so that the lens pass's bore tests interleave with
+// its RK4 steps (a branch on z there doubled the step time): log(1 + e) =
+// 2 atanh(s), s = e / (2 + e) <= 1/3, from the series 2 s (1 + s^2/3 + ... +
+// s^14/15), whose next term is below 4e-9 relative; the two quotients by the
+// fast division (2 ulp).  FP64: log1p and the IEEE reciprocal.
 template <class T>
 __device__ __forceinline__ void log_sigmoid(T z, T& ls, T& dls) {
-  if (std::is_same<T, float>::value && z >= T(12)) {
-    // e = exp(-z) <= 6.2e-6: log1p(e) = e (1 - e/2) and e / (1 + e) = e (1 - e)
-    // up to relative terms e^2 / 3 < 1.3e-11, far below float precision
-    // (most bore tests of a molecule inside the lens are this far from the edge)
-    const T e = exp_(-z);
-    ls = -mul_(e, fma_(T(-0.5), e, T(1)));
-    dls = mul_(e, add_(T(1), -e));
-    return;
+  if constexpr (std::is_same<T, float>::value) {
+    const float e = exp_(-fabsf(z));
+    const float s = __fdividef(e, add_(2.0f, e));
+    const float s2 = mul_(s, s);
+    float p = 1.0f / 15.0f;
+    p = fma_(p, s2, 1.0f / 13.0f);
+    p = fma_(p, s2, 1.0f / 11.0f);
+    p = fma_(p, s2, 1.0f / 9.0f);
+    p = fma_(p, s2, 1.0f / 7.0f);
+    p = fma_(p, s2, 1.0f / 5.0f);
+    p = fma_(p, s2, 1.0f / 3.0f);
+    p = fma_(p, s2, 1.0f);
+    const float l = mul_(mul_(2.0f, s), p);
+    ls = z >= 0.0f ? -l : add_(z, -l);
+    dls = mul_(z >= 0.0f ? e : 1.0f, __fdividef(1.0f, add_(1.0f, e)));
+  } else {
+    const T e = exp_(z >= T(0) ? -z : z);
+    const T l = log1p_(e);
+    ls = z >= T(0) ? -l : add_(z, -l);
+    dls = mul_(z >= T(0) ? e : T(1), rcp_(add_(T(1), e)));
   }
-  const T e = exp_(z >= T(0) ? -z : z);  // in (0, 1]
-  const T l = log1p_(e);
-  ls = z >= T(0) ? -l : add_(z, -l);
-  dls = mul_(z >= T(0) ? e : T(1), rcp_(add_(T(1), e)));
 }
 
 // The soft test of an edge of radius R at (x, y): log weight ls and its
@@ -647,7 +662,7 @@ __global__ void __launch_bounds__(kSoftThreads) k_soft_lens(const __grid_constan
     int n = 0;
     // One lens step plus the bore test of the state before it (the state
     // after the previous step; the entrance test was done by m.front).  The
-    // test does not feed the dynamics, so its latency overlaps the step's.
+    // test does not feed the dynamics.
     auto step = [&](int k) {
       const T qx = x, qy = y;
       soft_step<T, true>(C, s_tab, x, y, vx, vy, cx, cy, cvx, cvy, L.dt, L.hdt, L.c2, L.dt6, L.dt26, nullptr);
@@ -662,16 +677,51 @@ __global__ void __launch_bounds__(kSoftThreads) k_soft_lens(const __grid_constan
       c[4 * cap] = cx; c[5 * cap] = cy; c[6 * cap] = cvx; c[7 * cap] = cvy;
     };
     if (K % 8 == 0) {
-      // groups of 8 steps without a branch; checkpoints and the floor test in between
+      // Groups of 8 steps without a branch, software-pipelined: a group's
+      // steps run beside the bore tests of the previous group's 8 states,
+      // which do not depend on them, so the two chains' latencies overlap
+      // (with the branch-free FP32 log sigmoid, the slowest molecule's step
+      // 550 -> ~370 cycles); the tests are added to the log
+      // weight in step order, as one at a time would add them.  The floor
+      // test after a group sees the tests up to the previous group: the log
+      // weight only decreases, so the same molecules are dropped, up to 8
+      // steps later.  Checkpoints between groups.
+      T qx[8], qy[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) qx[u] = qy[u] = T(0);
+      bool pend = false;  // qx, qy hold the states before steps pn .. pn + 7
+      int pn = 0;
       for (; n + 8 <= L.N; n += 8) {
         if (kGrad && n % K == 0) store_ckpt(n);
 #pragma unroll
-        for (int u = 0; u < 8; ++u) step(n + u);
+        for (int u = 0; u < 8; ++u) {
+          const T sx = x, sy = y;
+          soft_step<T, true>(C, s_tab, x, y, vx, vy, cx, cy, cvx, cvy, L.dt, L.hdt, L.c2, L.dt6, L.dt26, nullptr);
+          T ls, d;
+          soft_test(qx[u], qy[u], bore, inv_w, ls, d);
+          const bool use = pend && pn + u > 0;
+          m.lw = add_(m.lw, use ? ls : T(0));
+          m.d_bore = add_(m.d_bore, use ? d : T(0));
+          qx[u] = sx;
+          qy[u] = sy;
+        }
+        pend = true;
+        pn = n;
         if (!(m.lw >= floor_)) {
           alive = false;
           n += 8;
           break;
         }
+      }
+      if (alive && pend) {  // the last group's tests
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          T ls, d;
+          soft_test(qx[u], qy[u], bore, inv_w, ls, d);
+          m.lw = add_(m.lw, pn + u > 0 ? ls : T(0));
+          m.d_bore = add_(m.d_bore, pn + u > 0 ? d : T(0));
+        }
+        if (!(m.lw >= floor_)) alive = false;
       }
     }
     for (; alive && n < L.N; ++n) {
