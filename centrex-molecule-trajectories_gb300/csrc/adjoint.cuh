@@ -99,25 +99,14 @@ __device__ __forceinline__ unsigned to_uint_rz(double a) { return __double2uint_
 // (0, 1]: log sigma(z) = -log(1 + e) for z >= 0 and z - log(1 + e) below;
 // sigma(-z) = e / (1 + e) for z >= 0 and 1 / (1 + e) below.
 // FP32 without a branch, so that the lens pass's bore tests interleave with
-// its RK4 steps (a branch on z there doubled the step time): log(1 + e) =
-// 2 atanh(s), s = e / (2 + e) <= 1/3, from the series 2 s (1 + s^2/3 + ... +
-// s^14/15), whose next term is below 4e-9 relative; the two quotients by the
-// fast division (2 ulp).  FP64: log1p and the IEEE reciprocal.
+// its RK4 steps (a branch on z there doubled the step time): log(1 + e) from
+// the atanh series (log1p_atanh), 1 / (1 + e) by the fast division (2 ulp).
+// FP64: log1p and the IEEE reciprocal.
 template <class T>
 __device__ __forceinline__ void log_sigmoid(T z, T& ls, T& dls) {
   if constexpr (std::is_same<T, float>::value) {
     const float e = exp_(-fabsf(z));
-    const float s = __fdividef(e, add_(2.0f, e));
-    const float s2 = mul_(s, s);
-    float p = 1.0f / 15.0f;
-    p = fma_(p, s2, 1.0f / 13.0f);
-    p = fma_(p, s2, 1.0f / 11.0f);
-    p = fma_(p, s2, 1.0f / 9.0f);
-    p = fma_(p, s2, 1.0f / 7.0f);
-    p = fma_(p, s2, 1.0f / 5.0f);
-    p = fma_(p, s2, 1.0f / 3.0f);
-    p = fma_(p, s2, 1.0f);
-    const float l = mul_(mul_(2.0f, s), p);
+    const float l = log1p_atanh(e);
     ls = z >= 0.0f ? -l : add_(z, -l);
     dls = mul_(z >= 0.0f ? e : 1.0f, __fdividef(1.0f, add_(1.0f, e)));
   } else {
