@@ -1308,7 +1308,8 @@ __global__ void __launch_bounds__(kFinishThreads) k_lens_finish(const __grid_con
 // Batched sweep: the Stark tables' lens queues in one launch.  Each CTA
 // starts on a table, chosen so that CTAs are spread over the tables in
 // proportion to their queues, and when that queue is used up moves on to the
-// next table with molecules left, staging its table.
+// next table with molecules left, staging its table.  kT threads per CTA
+// (one CTA per SM).
 struct SweepTabs {
   const float4* q[CTRAJ_MAX_TABLES];
   const unsigned* order[CTRAJ_MAX_TABLES];
@@ -1318,8 +1319,8 @@ struct SweepTabs {
   unsigned done_cap[CTRAJ_MAX_TABLES];     // queue positions with a record
 };
 
-template <int F, bool kStaged>
-__global__ void __launch_bounds__(kPersistThreads, 1) k_sweep_persist(const __grid_constant__ Plan P, const RunDev R,
+template <int F, bool kStaged, int kT = kPersistThreads>
+__global__ void __launch_bounds__(kT, 1) k_sweep_persist(const __grid_constant__ Plan P, const RunDev R,
                                                                       const int li,
                                                                       const __grid_constant__ SweepQueues Qs,
                                                                       const int n_tab,
@@ -1329,7 +1330,7 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_sweep_persist(const __gr
   using M = Mol32<false, false>;
   extern __shared__ float4 s_dyn[];
   __shared__ BlockTally S;
-  __shared__ unsigned s_wcount[kPersistThreads / 32];
+  __shared__ unsigned s_wcount[kT / 32];
   __shared__ int s_left;
   int max_int = 0;
   for (int t = 0; t < n_tab; ++t) max_int = max(max_int, T.n_int[t]);
@@ -1364,7 +1365,7 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_sweep_persist(const __gr
     L.n_int = T.n_int[t];
     L.n_smem = kStaged ? T.n_int[t] : 0;
     // no interleaved first entries: each CTA takes from its table's queue in order
-    persist_pass<M, false, F, kStaged, kModeSweep>(P, R, li, Q, Q, L, T.order[t], interval, service, 0u, s_dyn,
+    persist_pass<M, false, F, kStaged, kModeSweep, kT>(P, R, li, Q, Q, L, T.order[t], interval, service, 0u, s_dyn,
                                                   s_swap, s_wcount, S, acc, T.done[t], T.done_cap[t]);
   }
   persist_flush(S, R, P.n_labels, acc);

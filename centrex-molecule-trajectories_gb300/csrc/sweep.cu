@@ -84,14 +84,21 @@ struct SweepLaunch {
   DoneRec* done[CTRAJ_MAX_TABLES] = {};    // persistent: the molecules' end records, per table
   unsigned done_cap[CTRAJ_MAX_TABLES] = {};
   int outward = 0;                         // every configuration's force points away from the axis
+  int threads = kPersistThreads;           // persistent: threads per CTA of k_sweep_persist
 };
 
-// The persistent sweep lens kernel of a force law; staged when every table fits.
+// The persistent sweep lens kernel of a force law; staged when every table
+// fits.  Linear tables staged in shared memory run with `threads` (512, 768
+// or 1024) per CTA, the others with 512.
 using SweepPersistKernel = void (*)(const Plan, const RunDev, const int, const SweepQueues, const int,
                                     const SweepTabs, const LensArgs, const int, const int);
-SweepPersistKernel sweep_persist_kernel(int force, bool staged) {
-  if (force == kForceStark2Lin)
-    return staged ? k_sweep_persist<kForceStark2Lin, true> : k_sweep_persist<kForceStark2Lin, false>;
+SweepPersistKernel sweep_persist_kernel(int force, bool staged, int threads) {
+  if (force == kForceStark2Lin && staged) {
+    if (threads == 768) return k_sweep_persist<kForceStark2Lin, true, 768>;
+    if (threads == 1024) return k_sweep_persist<kForceStark2Lin, true, 1024>;
+    return k_sweep_persist<kForceStark2Lin, true>;
+  }
+  if (force == kForceStark2Lin) return k_sweep_persist<kForceStark2Lin, false>;
   if (staged)
     return force == kForceStark1 ? k_sweep_persist<kForceStark1, true> : k_sweep_persist<kForceStark2, true>;
   return force == kForceStark1 ? k_sweep_persist<kForceStark1, false> : k_sweep_persist<kForceStark2, false>;
@@ -106,7 +113,7 @@ bool sweep_staged(const SweepLaunch& W) {
 size_t sweep_persist_smem(const SweepLaunch& W) {
   int max_int = 0;
   for (int t = 0; t < W.n_tab; ++t) max_int = std::max(max_int, W.la[t].n_int);
-  return (sweep_staged(W) ? size_t(max_int) * sizeof(float4) : 0) + kPersistThreads * sizeof(SwapSlot);
+  return (sweep_staged(W) ? size_t(max_int) * sizeof(float4) : 0) + size_t(W.threads) * sizeof(SwapSlot);
 }
 
 // The whole sweep on c->stream (forking to one side stream per table).  Every
@@ -155,8 +162,8 @@ int sweep_enqueue(ctraj_context* c, const Plan& P, const RunDev& R, const SweepL
       T.done[t] = W.done[t];
       T.done_cap[t] = W.done_cap[t];
     }
-    sweep_persist_kernel(W.force, sweep_staged(W))<<<c->sm_count, kPersistThreads,
-                                                                  sweep_persist_smem(W), s>>>(
+    sweep_persist_kernel(W.force, sweep_staged(W), W.threads)<<<c->sm_count, W.threads,
+                                                                             sweep_persist_smem(W), s>>>(
         P, R, W.lens, Qs, W.n_tab, T, W.la[0], c->lens_interval, c->lens_service);
     CT_CUDA(cudaGetLastError());
     ++launches;
@@ -407,6 +414,7 @@ extern "C" int ctraj_run_sweep(ctraj_context* c, const ctraj_sweep* sw, const ct
     L.n_smem = L.n_int <= (lin ? kMaxStagedLinear : kMaxStagedIntervals) ? L.n_int : 0;
   }
   W.chunks = sweep_chunks(c, sweep_step_estimate(e, a));
+  W.threads = W.force == kForceStark2Lin && sweep_staged(W) ? c->lens_threads : kPersistThreads;
 
   // what a captured graph depends on
   std::vector<char> key;
@@ -429,6 +437,7 @@ extern "C" int ctraj_run_sweep(ctraj_context* c, const ctraj_sweep* sw, const ct
   put(&c->front_threads, sizeof c->front_threads);
   put(&W.force, sizeof W.force);
   put(&W.outward, sizeof W.outward);
+  put(&W.threads, sizeof W.threads);
   const bool same = key == c->sweep_key;
   cudaStream_t s = c->stream;
   if (!same) {
@@ -483,7 +492,7 @@ extern "C" int ctraj_run_sweep(ctraj_context* c, const ctraj_sweep* sw, const ct
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   }
   if (W.persistent)
-    CT_CUDA(cudaFuncSetAttribute(sweep_persist_kernel(W.force, sweep_staged(W)),
+    CT_CUDA(cudaFuncSetAttribute(sweep_persist_kernel(W.force, sweep_staged(W), W.threads),
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(sweep_persist_smem(W))));
   CT_CUDA(cudaFuncSetAttribute(k_sweep_front<Mol32<false, false>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                int(sweep_front_smem(kFrontMaxThreads))));

@@ -271,9 +271,11 @@ int ctraj_set_beamline(ctraj_context* ctx, const ctraj_element* elements,
  *                 per-molecule outputs in persistent lens mode; other runs,
  *                 and batch_group 1, run one at a time.           default 4
  *   lens_threads  molecules per CTA of the persistent FP32 lens pass (one CTA
- *                 per SM): 512, 768 or 1024; at one molecule per thread that
- *                 is 16, 24 or 32 warps per SM within a register budget of
- *                 128, 80 or 64 per thread.                     default 512
+ *                 per SM) of a run and of a batched sweep: 512, 768 or 1024;
+ *                 at one molecule per thread that is 16, 24 or 32 warps per
+ *                 SM within a register budget of 128, 80 or 64 per thread
+ *                 (sweeps: linear Stark tables staged in shared memory;
+ *                 others run 512).                              default 512
  *   lens_molecules molecules each thread of the persistent FP32 lens pass
  *                 steps in turn (1 or 2; with 2 the CTA has lens_threads / 2
  *                 threads, and each RK4 step has a second molecule's

@@ -128,7 +128,8 @@ def test_graph_replay_equals_direct_launches(engine):
 def test_persistent_and_chunked_sweeps_agree(engine, use_graph):
     """The one-launch persistent lens pass (default) and the chunked one give
     the same per-configuration counts and steps: the same molecules through
-    the same arithmetic, in another order."""
+    the same arithmetic, in another order, at every CTA size of the
+    persistent pass."""
     from ctraj.sweep import run_sweep
 
     cfg = small_configs(10_000, 40_000, seed=5)
@@ -137,8 +138,9 @@ def test_persistent_and_chunked_sweeps_agree(engine, use_graph):
     try:
         engine.set_tuning(lens_mode=1)
         chunked = run_sweep(bl, cfg, xdist=xs, vdist=vs, seed=4, use_graph=use_graph, engine=engine)
-        for interval, service in ((256, 64), (7, 3), (256, 500)):
-            engine.set_tuning(lens_interval=interval, lens_service=service)
+        for interval, service, threads in ((256, 64, 512), (7, 3, 512), (256, 500, 512), (128, 64, 768),
+                                           (5, 9, 1024)):
+            engine.set_tuning(lens_interval=interval, lens_service=service, lens_threads=threads)
             pers = run_sweep(bl, cfg, xdist=xs, vdist=vs, seed=4, use_graph=use_graph, engine=engine)
             np.testing.assert_array_equal(pers.counts, chunked.counts)
             assert pers.molecule_steps == chunked.molecule_steps and pers.lens_steps == chunked.lens_steps
