@@ -185,8 +185,49 @@ struct SoftQueue {
 
 // Per (survivor, segment): the segment's backward map
 //   lambda_in = A^T lambda_out + b,  dlw/dV += c . lambda_out + d
-// as 25 values A[4][4] (row q = the image of the unit vector e_q), b[4], c[4], d.
+// as 25 values A[4][4] (row q = the image of the unit vector e_q), b[4], c[4], d,
+// stored as one record of kSoftSegStride values (padded to 16-byte vectors)
+// per (survivor, segment), the survivor's segments consecutive: k_soft_compose
+// walks a survivor's segments in order and reads each record whole (with the
+// 25 values in 25 planes it read 25 scattered sectors per segment).
 constexpr int kSoftSegFields = 25;
+constexpr int kSoftSegStride = 28;
+
+template <class T>
+__device__ __forceinline__ void seg_store(T* o, const T (&v)[kSoftSegStride]) {
+  if constexpr (std::is_same<T, float>::value) {
+    float4* p = reinterpret_cast<float4*>(o);
+#pragma unroll
+    for (int k = 0; k < kSoftSegStride / 4; ++k) p[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+  } else {
+    double2* p = reinterpret_cast<double2*>(o);
+#pragma unroll
+    for (int k = 0; k < kSoftSegStride / 2; ++k) p[k] = make_double2(v[2 * k], v[2 * k + 1]);
+  }
+}
+
+template <class T>
+__device__ __forceinline__ void seg_load(const T* o, T (&v)[kSoftSegStride]) {
+  if constexpr (std::is_same<T, float>::value) {
+    const float4* p = reinterpret_cast<const float4*>(o);
+#pragma unroll
+    for (int k = 0; k < kSoftSegStride / 4; ++k) {
+      const float4 a = __ldg(p + k);
+      v[4 * k] = a.x;
+      v[4 * k + 1] = a.y;
+      v[4 * k + 2] = a.z;
+      v[4 * k + 3] = a.w;
+    }
+  } else {
+    const double2* p = reinterpret_cast<const double2*>(o);
+#pragma unroll
+    for (int k = 0; k < kSoftSegStride / 2; ++k) {
+      const double2 a = __ldg(p + k);
+      v[2 * k] = a.x;
+      v[2 * k + 1] = a.y;
+    }
+  }
+}
 
 // Per-molecule terms (double): weight, then the six gradient terms.  They are
 // written to (kSoftAcc, count) columns indexed by molecule and summed in a
@@ -770,17 +811,17 @@ __global__ void __launch_bounds__(kSoftThreads) k_soft_lens(const __grid_constan
 // over segments: recompute the segment from its checkpoint into the tape, then
 // run the transposed step Jacobians backwards over it for the four unit
 // vectors and the affine part (the segment's own bore tests), giving the
-// segment's backward map (A, b, c, d).  seg_out: (kSoftSegFields, bcap * max_seg).
+// segment's backward map (A, b, c, d).  seg_out: (bcap * max_seg) records of
+// kSoftSegStride values.
 template <class T>
 __global__ void __launch_bounds__(kSoftThreads) k_soft_seg(const __grid_constant__ SoftPlan S, const SoftQueue Q,
                                                            const Coef4<T>* __restrict__ table,
                                                            const T* __restrict__ ckpt, size_t cap,
-                                                           T* __restrict__ seg_out, int max_seg, size_t bcap) {
+                                                           T* __restrict__ seg_out, int max_seg) {
   extern __shared__ unsigned char s_raw[];
   Coef4<T>* s_tab = reinterpret_cast<Coef4<T>*>(s_raw);
   stage_table(S, table, s_tab);
   const size_t n_work = size_t(*Q.bcount) * size_t(max_seg);
-  const size_t plane = bcap * size_t(max_seg);
   const T inv_w = T(S.inv_w), bore = T(S.bore);
   const SoftK<T> C(S);
   const int K = S.checkpoint;
@@ -815,16 +856,19 @@ __global__ void __launch_bounds__(kSoftThreads) k_soft_seg(const __grid_constant
       check_adjoint(bore, inv_w, ax, ay, lam[4][0], lam[4][1]);
       soft_step_adjoint<T, 5>(C, tape[k - k0], L.dt, L.hdt, L.c2, L.dt6, L.dt26, lam, gv);
     }
-    T* o = seg_out + wi;
+    T rec[kSoftSegStride];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
 #pragma unroll
-      for (int r = 0; r < 4; ++r) o[(q * 4 + r) * plane] = lam[q][r];
-      o[(20 + q) * plane] = gv[q];
+      for (int r = 0; r < 4; ++r) rec[q * 4 + r] = lam[q][r];
+      rec[20 + q] = gv[q];
     }
 #pragma unroll
-    for (int r = 0; r < 4; ++r) o[(16 + r) * plane] = lam[4][r];
-    o[24 * plane] = gv[4];
+    for (int r = 0; r < 4; ++r) rec[16 + r] = lam[4][r];
+    rec[24] = gv[4];
+#pragma unroll
+    for (int k = kSoftSegFields; k < kSoftSegStride; ++k) rec[k] = T(0);
+    seg_store(seg_out + wi * kSoftSegStride, rec);
   }
 }
 
@@ -835,10 +879,9 @@ __global__ void __launch_bounds__(kSoftThreads) k_soft_seg(const __grid_constant
 template <class T>
 __global__ void __launch_bounds__(kSoftThreads) k_soft_compose(const __grid_constant__ SoftPlan S, const SoftQueue Q,
                                                                const T* __restrict__ seg_out, int max_seg,
-                                                               size_t bcap, double* __restrict__ contrib,
+                                                               double* __restrict__ contrib,
                                                                size_t cap) {
   const unsigned nb = *Q.bcount;
-  const size_t plane = bcap * size_t(max_seg);
   const T inv_w = T(S.inv_w), bore = T(S.bore);
   for (unsigned b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
     const int64_t i = Q.bid[b];
@@ -858,19 +901,20 @@ __global__ void __launch_bounds__(kSoftThreads) k_soft_compose(const __grid_cons
     // unrolled so that the next segments' loads are issued while this one's
     // products wait (a thread walks its segments in order; the maps are read
     // once each)
-#pragma unroll 4
+#pragma unroll 2
     for (int sg = n_seg - 1; sg >= 0; --sg) {
-      const T* o = seg_out + size_t(b) * size_t(max_seg) + size_t(sg);
+      T o[kSoftSegStride];
+      seg_load(seg_out + (size_t(b) * size_t(max_seg) + size_t(sg)) * kSoftSegStride, o);
       const T lo[4] = {lx, ly, lvx, lvy};
       T ln[4];
 #pragma unroll
-      for (int r = 0; r < 4; ++r) ln[r] = o[(16 + r) * plane];
-      T g = o[24 * plane];
+      for (int r = 0; r < 4; ++r) ln[r] = o[16 + r];
+      T g = o[24];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
 #pragma unroll
-        for (int r = 0; r < 4; ++r) ln[r] = fma_(o[(q * 4 + r) * plane], lo[q], ln[r]);
-        g = fma_(o[(20 + q) * plane], lo[q], g);
+        for (int r = 0; r < 4; ++r) ln[r] = fma_(o[q * 4 + r], lo[q], ln[r]);
+        g = fma_(o[20 + q], lo[q], g);
       }
       gV = add_(gV, g);
       lx = ln[0];

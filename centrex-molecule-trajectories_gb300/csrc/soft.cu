@@ -173,7 +173,7 @@ int soft_run(ctraj_context* c, const ctraj_soft_args* a, SoftPlan& S, int li, ct
       }
       if (a->want_grad) {
         if ((st = c->soft_ckpt.ensure(n_seg * 8 * cap * sizeof(T), 25))) return st;
-        if ((st = c->soft_seg.ensure(size_t(kSoftSegFields) * cap * size_t(max_seg) * sizeof(T), 25))) return st;
+        if ((st = c->soft_seg.ensure(size_t(kSoftSegStride) * cap * size_t(max_seg) * sizeof(T), 25))) return st;
       }
       grid = int((cap + kSoftThreads - 1) / kSoftThreads);
       kl<<<grid, kSoftThreads, tb, s>>>(S, Q, c->soft_table.as<Coef4<T>>(), c->soft_ckpt.as<T>(), cap, contrib,
@@ -189,11 +189,11 @@ int soft_run(ctraj_context* c, const ctraj_soft_args* a, SoftPlan& S, int li, ct
           CT_CUDA(cudaFuncSetAttribute(ks, cudaFuncAttributeMaxDynamicSharedMemorySize, int(tb)));
           const int gs = blocks_per_sm(ks, kSoftThreads, tb) * c->sm_count * 4;
           ks<<<gs, kSoftThreads, tb, s>>>(S, Q, c->soft_table.as<Coef4<T>>(), c->soft_ckpt.as<T>(), cap,
-                                          c->soft_seg.as<T>(), max_seg, cap);
+                                          c->soft_seg.as<T>(), max_seg);
           CT_CUDA(cudaGetLastError());
           ++launches;
         }
-        k_soft_compose<T><<<grid, kSoftThreads, 0, s>>>(S, Q, c->soft_seg.as<T>(), max_seg, cap, contrib, cap);
+        k_soft_compose<T><<<grid, kSoftThreads, 0, s>>>(S, Q, c->soft_seg.as<T>(), max_seg, contrib, cap);
         CT_CUDA(cudaGetLastError());
         ++launches;
       }
