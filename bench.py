@@ -122,6 +122,8 @@ def parse():
                    help="--profile batch: threads per CTA of the shared lens pass")
     p.add_argument("--lens-interval", type=int, default=256,
                    help="--profile: RK4 steps between the persistent pass's compactions once its queue is empty")
+    p.add_argument("--lens-threads", type=int, default=512,
+                   help="--profile lens/sweep: threads per CTA of a run's or a sweep's persistent lens pass")
     return p.parse_args()
 
 
@@ -140,7 +142,7 @@ def run_profile(args):
     eng = Engine(0)
     eng.set_tuning(lens_mode=0 if args.lens_mode == "persistent" else 1, batch_group=args.batch_group,
                    front_threads=args.front_threads, batch_lens_threads=args.batch_lens_threads,
-                   lens_interval=args.lens_interval)
+                   lens_interval=args.lens_interval, lens_threads=args.lens_threads)
     n = int(args.molecules)
     for k in range(args.steps):
         if args.profile == "sweep":
