@@ -164,14 +164,16 @@ class TrajectorySimulator:
 
     def run_simulations(self, beamline, run_names, vdist=CeNTREXVelocityDistribution(),
                         xdist=CeNTREXPositionDistribution(), N_traj: int = 1000, n_jobs=1, *,
-                        seeds=None, precision: int | None = None, g: float = G):
+                        seeds=None, precision: int | None = None, g: float = G, l2_flush_bytes: int = 0):
         """The caller's loop ``for name in run_names: run_simulation(beamline,
         name, ...)`` as one call: every batch of N_traj molecules is its own run
         (own seed, own Counter under results[name]), and the runs are pipelined
         on the device (ctraj_run_batch), so one batch's ballistic front overlaps
         the previous batch's lens pass.  Trajectories are not kept
         (apertures_of_interest empty); last_runs holds the per-batch RunResults
-        and last_run the last one."""
+        and last_run the last one.  l2_flush_bytes > 0: that many bytes of
+        device scratch are written before each batch (cold caches between
+        batches, for timing)."""
         names = list(run_names)
         n = simulated_count(N_traj, n_jobs)
         prec = precision or self.precision
@@ -195,7 +197,8 @@ class TrajectorySimulator:
                     x = np.asarray(xdist.draw(per), dtype=np.float64).reshape(3, per)
                     chunks.append(np.vstack((x, v)))
                 ics.append(np.ascontiguousarray(np.hstack(chunks)))
-        runs = eng.run_batch(cb, n, seeds, precision=prec, ics=ics, xdist=xs, vdist=vs, g=g)
+        runs = eng.run_batch(cb, n, seeds, precision=prec, ics=ics, xdist=xs, vdist=vs, g=g,
+                             l2_flush_bytes=int(l2_flush_bytes))
         self.last_runs = runs
         for k, (name, res) in enumerate(zip(names, runs)):
             self.last_run = res
