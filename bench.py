@@ -729,7 +729,9 @@ def main():
                      batch=batch_measure(eng, cb, n, run_kw, runs=args.steps, l2_flush_bytes=flush.numel()))
     for k in range(args.warmup):
         step(seed=k)
-    eng.run_batch(cb, n, list(range(max(2, args.warmup))), precision=32, xdist=xs, vdist=vs, offset=rank * n,
+    # a batch of as many runs as the timed one: its groups' buffers are sized
+    # before the timed region (with cached knobs the tuner runs no batch)
+    eng.run_batch(cb, n, list(range(max(2, args.steps))), precision=32, xdist=xs, vdist=vs, offset=rank * n,
                   l2_flush_bytes=flush.numel())
     peak = fp32_peak(local)
     probe = step_probe(local, bl)
