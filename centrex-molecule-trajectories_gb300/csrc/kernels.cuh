@@ -931,6 +931,21 @@ __device__ __forceinline__ void lens_finish(const Plan& P, const RunDev& R, cons
   }
 }
 
+// lens_finish as a call of its own, for the batched sweep's pass: a sweep ends
+// in the pass only the molecules beyond its end records, and inlined there
+// the end's code set the pass's register count (126 at 512 threads, spills
+// at 768 and 1024); called, it costs a stack frame on that cold path and the
+// pass fits 79 registers at 768 threads (lens pass of the bench's sweep 17.3
+// -> 16.1 ms at 768, 16.8 -> 15.8 ms at 1024 threads).
+template <class M, bool kOut, int kMode>
+__device__ __noinline__ void lens_finish_call(const Plan& P, const RunDev& R, const int li, const Queue& Qin,
+                                              const Queue& Qnext, const bool fin, M& m, LensStep& st,
+                                              const int phase, const unsigned flags, const unsigned idx,
+                                              const int n0, const bool fresh, const int cfg, BlockTally& S,
+                                              PersistAcc& acc) {
+  lens_finish<M, kOut, kMode>(P, R, li, Qin, Qnext, fin, m, st, phase, flags, idx, n0, fresh, cfg, S, acc);
+}
+
 // A molecule's state after its last RK4 step in a persistent pass whose end
 // (lens_finish) is deferred to k_lens_finish: written at its queue position,
 // 64 bytes, read back coalesced.  word = phase | flags << 3 | n0 << 5.
@@ -1093,7 +1108,11 @@ __device__ __forceinline__ void persist_pass(const Plan& P, const RunDev& R, con
         if (!__any_sync(kFull, fin)) return;
       }
     }
-    if constexpr (kOut || kMode != kModeBatch) {
+    if constexpr (kMode == kModeSweep) {
+      lens_finish_call<M, kOut, kMode>(P, R, li, Qin, Qnext, fin, x.m, x.st, x.phase, x.flags, x.idx, x.n0,
+                                       x.fresh, x.cfg, S, acc);
+      if (fin) x.phase = kIdle;
+    } else if constexpr (kOut || kMode != kModeBatch) {
       lens_finish<M, kOut, kMode>(P, R, li, Qin, Qnext, fin, x.m, x.st, x.phase, x.flags, x.idx, x.n0, x.fresh,
                                   x.cfg, S, acc);
       if (fin) x.phase = kIdle;
