@@ -720,6 +720,11 @@ int ctraj_set_beamline(ctraj_context* c, const ctraj_element* el, int32_t n_el, 
     if ((e.type == CTRAJ_ELECTROSTATIC_LENS || e.type == CTRAJ_HONEYCOMB) && (e.table < 0 || e.table >= CTRAJ_MAX_TABLES))
       return fail(CTRAJ_EINVAL, "element %d: table id %d out of range", i, e.table);
   }
+  // the beamline already set (a caller that sets it before every run): its
+  // device tables and everything derived from it stay valid
+  if (c->have_beamline && c->n_labels == n_labels && c->elements.size() == size_t(n_el) &&
+      (n_el == 0 || std::memcmp(c->elements.data(), el, size_t(n_el) * sizeof(ctraj_element)) == 0))
+    return CTRAJ_OK;
   c->elements.assign(el, el + n_el);
   c->n_labels = n_labels;
   c->have_beamline = true;
@@ -728,9 +733,23 @@ int ctraj_set_beamline(ctraj_context* c, const ctraj_element* el, int32_t n_el, 
   return CTRAJ_OK;
 }
 
+// The table already set under this id, bit for bit (knots and coefficients
+// or values).
+static bool same_table(const HostTable& ht, const ctraj_force_table* t) {
+  if (ht.n == 0 || ht.kind != t->kind || ht.n != t->n_knots || !t->knots) return false;
+  if (std::memcmp(ht.knots.data(), t->knots, size_t(t->n_knots) * sizeof(double)) != 0) return false;
+  if (t->kind == CTRAJ_TABLE_STARK_SPLINE)
+    return t->coef && ht.coef.size() == size_t(t->n_knots - 1) * 4 &&
+           std::memcmp(ht.coef.data(), t->coef, ht.coef.size() * sizeof(double)) == 0;
+  return t->values && ht.values.size() == size_t(t->n_knots) &&
+         std::memcmp(ht.values.data(), t->values, ht.values.size() * sizeof(double)) == 0;
+}
+
 int ctraj_set_force_table(ctraj_context* c, int32_t id, const ctraj_force_table* t) {
   if (!c || !t) return fail(CTRAJ_EINVAL, "NULL argument");
   if (id < 0 || id >= CTRAJ_MAX_TABLES) return fail(CTRAJ_EINVAL, "table id %d out of range", id);
+  // the table already set (validated then): nothing to copy, rebuild or upload
+  if (same_table(c->tables[id], t)) return CTRAJ_OK;
   if (t->kind == CTRAJ_TABLE_MESH) {
     if (t->n_knots < 1 || !t->knots || !t->values) return fail(CTRAJ_EINVAL, "mesh table needs at least one cell");
     for (int j = 0; j < t->n_knots; ++j)

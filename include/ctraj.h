@@ -237,7 +237,8 @@ int ctraj_set_stream(ctraj_context* ctx, void* cuda_stream);
 int ctraj_synchronize(ctraj_context* ctx);
 
 /* Beamline.__post_init__ / sort_elements (beamline.py:17-18,40-45): elements
- * must already be sorted by z0; n_labels counter slots. */
+ * must already be sorted by z0; n_labels counter slots.  Setting the same
+ * elements again (bit for bit) changes nothing and costs a comparison. */
 int ctraj_set_beamline(ctraj_context* ctx, const ctraj_element* elements,
                        int32_t n_elements, int32_t n_labels);
 
@@ -311,7 +312,9 @@ int ctraj_get_tuning(ctraj_context* ctx, ctraj_tuning* tuning);
 
 /* ElectrostaticLens.a_interp / lens_acceleration table (electrostatic_lens.py:174-213),
  * or the cell centres of a Honeycomb (meshes.py:53-62, kind CTRAJ_TABLE_MESH,
- * at least one cell). */
+ * at least one cell).  Setting the table already set under this id again
+ * (knots and coefficients or values bit for bit) changes nothing: the device
+ * copies and the lens tables built from it stay. */
 int ctraj_set_force_table(ctraj_context* ctx, int32_t table_id,
                           const ctraj_force_table* table);
 
