@@ -133,6 +133,11 @@ struct ctraj_context {
   ctraj::DevBuf sweep_queue[2 * CTRAJ_MAX_TABLES];
   // soft transmission (ctraj_soft_transmission)
   ctraj::DevBuf soft_table, soft_queue, soft_ckpt, soft_ctl, soft_contrib, soft_seg, soft_post;
+  // what soft_table holds: built from table soft_table_id at generation
+  // soft_table_gen in elements of soft_table_size bytes, scaled by soft_table_f
+  uint64_t soft_table_gen = ~uint64_t(0);
+  int soft_table_id = -1, soft_table_size = 0;
+  double soft_table_f = 1.0;
   unsigned long long* sweep_host = nullptr;  // pinned: per-configuration counts, totals, stats
   size_t sweep_host_words = 0;
   cudaStream_t side[CTRAJ_MAX_TABLES] = {};

@@ -96,34 +96,46 @@ int soft_plan(const ctraj_context* c, const ctraj_soft_args* a, const double* pr
 template <class T>
 int soft_run(ctraj_context* c, const ctraj_soft_args* a, SoftPlan& S, int li, ctraj_soft_result* out) {
   cudaStream_t s = c->stream;
-  const HostTable& t = c->tables[c->elements[li].table];
+  const int tid = c->elements[li].table;
+  const HostTable& t = c->tables[tid];
   const double h = (t.knots[t.n - 1] - t.knots[0]) / double(t.n - 1);
-  // table f W'(E) = q0 + q1 u + q2 u^2 on each interval, in T, with a power of
-  // two f that brings the largest coefficient near 1 (W' is ~1e-29 J m/V and
-  // kappa beta ~1e40 would overflow float); kappa and kappa1 carry 1/f
-  double qmax = 0.0;
-  for (int j = 0; j < t.n - 1; ++j) {
-    const double* cj = &t.coef[size_t(j) * 4];
-    qmax = std::max({qmax, std::fabs(cj[2]), std::fabs(2.0 * cj[1] * h), std::fabs(3.0 * cj[0] * h * h)});
-  }
-  const double f = qmax > 0.0 && std::isfinite(qmax) ? std::ldexp(1.0, -std::ilogb(qmax)) : 1.0;
-  S.kappa /= f;
-  S.kappa1 /= f;
-  std::vector<Coef4<T>> host(t.n - 1);
-  for (int j = 0; j < t.n - 1; ++j) {
-    const double* cj = &t.coef[size_t(j) * 4];
-    host[j] = Coef4<T>{T(f * cj[2]), T(f * (2.0 * cj[1] * h)), T(f * (3.0 * cj[0] * h * h)), T(0)};
-  }
-  const size_t tb = host.size() * sizeof(Coef4<T>);
+  const size_t tb = size_t(t.n - 1) * sizeof(Coef4<T>);
   if (tb > 200 * 1024) return fail(CTRAJ_EINVAL, "soft transmission: the lens table (%d knots) is too large", t.n);
   int st;
+  // table f W'(E) = q0 + q1 u + q2 u^2 on each interval, in T, with a power of
+  // two f that brings the largest coefficient near 1 (W' is ~1e-29 J m/V and
+  // kappa beta ~1e40 would overflow float); kappa and kappa1 carry 1/f.  It
+  // depends on the Stark table alone, not on the parameters: built and
+  // uploaded again only when the table (or anything set since) changed, so a
+  // gradient loop does not rebuild it per call.
+  if (c->soft_table_gen != c->generation || c->soft_table_id != tid || c->soft_table_size != int(sizeof(T))) {
+    double qmax = 0.0;
+    for (int j = 0; j < t.n - 1; ++j) {
+      const double* cj = &t.coef[size_t(j) * 4];
+      qmax = std::max({qmax, std::fabs(cj[2]), std::fabs(2.0 * cj[1] * h), std::fabs(3.0 * cj[0] * h * h)});
+    }
+    const double f = qmax > 0.0 && std::isfinite(qmax) ? std::ldexp(1.0, -std::ilogb(qmax)) : 1.0;
+    std::vector<Coef4<T>> host(t.n - 1);
+    for (int j = 0; j < t.n - 1; ++j) {
+      const double* cj = &t.coef[size_t(j) * 4];
+      host[j] = Coef4<T>{T(f * cj[2]), T(f * (2.0 * cj[1] * h)), T(f * (3.0 * cj[0] * h * h)), T(0)};
+    }
+    c->soft_table_gen = ~uint64_t(0);  // until the copy is enqueued
+    if ((st = c->soft_table.ensure(tb))) return st;
+    CT_CUDA(cudaMemcpyAsync(c->soft_table.p, host.data(), tb, cudaMemcpyHostToDevice, s));
+    CT_CUDA(cudaStreamSynchronize(s));  // host goes out of scope
+    c->soft_table_gen = c->generation;
+    c->soft_table_id = tid;
+    c->soft_table_size = int(sizeof(T));
+    c->soft_table_f = f;
+  }
+  S.kappa /= c->soft_table_f;
+  S.kappa1 /= c->soft_table_f;
   const int64_t chunk = std::min<int64_t>(std::max<int64_t>(a->n, 1), kSoftChunk);
-  if ((st = c->soft_table.ensure(tb))) return st;
   if ((st = c->soft_queue.ensure(size_t(chunk) * 4 * 3))) return st;
   if ((st = c->soft_ctl.ensure(kSoftCtlBytes))) return st;
   if ((st = c->soft_contrib.ensure(size_t(chunk) * kSoftAcc * 8))) return st;
   const bool post_grad = a->want_grad && S.n_post > 0;
-  CT_CUDA(cudaMemcpyAsync(c->soft_table.p, host.data(), tb, cudaMemcpyHostToDevice, s));
   if (a->ic_mode == CTRAJ_IC_HOST && a->n > 0) {
     const size_t b = size_t(a->n) * 5 * 8;
     if ((st = c->ics.ensure(b))) return st;
